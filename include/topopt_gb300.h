@@ -1,0 +1,162 @@
+/*
+ * topopt_gb300.h -- C ABI of the GB300 transient solve-and-sensitivity path.
+ *
+ * Drop-in boundary for the classes TopOpt_in_PETSc_Transient's main.cc calls
+ * on its hot path (LinearElasticity, PDEFilt/Filter, MMA).  Every entry point
+ * takes plain pointers and sizes and returns an int status (0 = TOPO_OK).
+ * Host-pointer entry points take arrays exactly as VecGetArray() hands them out
+ * on one rank: DMDA natural ordering, node (i,j,k) -> i + nx*(j + ny*k),
+ * displacement DOF 3*node + component, element (i,j,k) -> i + (nx-1)*(j + (ny-1)*k).
+ * The *_dev variants take device pointers of the same layout.
+ * All computation runs on the current CUDA device; there is no CPU fallback:
+ * without a usable GPU every compute entry point returns TOPO_ERR_CUDA.
+ */
+#ifndef TOPOPT_GB300_H
+#define TOPOPT_GB300_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (PetscErrorCode-compatible: 0 = success) */
+#define TOPO_OK 0
+#define TOPO_ERR_ARG 1            /* invalid argument / unsupported option       */
+#define TOPO_ERR_CUDA 2           /* CUDA runtime error or no device             */
+#define TOPO_ERR_OOM 3            /* device allocation failed                    */
+#define TOPO_ERR_NOT_CONVERGED 4  /* Krylov solve hit maxit                      */
+#define TOPO_ERR_BREAKDOWN 5      /* non-positive curvature in CG                */
+#define TOPO_ERR_NAN 6            /* NaN/Inf encountered                         */
+#define TOPO_ERR_STATE 7          /* call order violated                         */
+#define TOPO_ERR_SYNC_TIMEOUT 8   /* a bounded device-side wait gave up          */
+
+typedef struct topo_le topo_le;
+typedef struct topo_pdefilt topo_pdefilt;
+typedef struct topo_mma topo_mma;
+
+/* Parameters of LinearElasticity(...) (LinearElasticity.h:29) plus the mesh
+ * geometry the reference reads off its DMDA (SetUpBC, LinearElasticity.cc:337-391)
+ * and the GB300 solver controls. */
+typedef struct topo_le_params {
+    int nx, ny, nz;          /* nodes per direction (-nx -ny -nz)                  */
+    double hx, hy, hz;       /* element size                                        */
+    double nu;               /* Poisson ratio (-nu)                                 */
+    int nlvls;               /* multigrid levels (-nlvls)                           */
+    int ncp, tsc;            /* checkpoint blocks, steps per block (-ncp -tsc)      */
+    double t1;               /* final time (-t1), dt = t1/(ncp*tsc)                 */
+    int ti;                  /* 0 backward Euler, 1 Newmark (-ti)                   */
+    int objective;           /* 0..6 (-objective)                                   */
+    int sInt, mInt;          /* interpolation (-sInt, -massInterpolation)           */
+    int boundaries;          /* 0 MBB, 1 cantilever (-boundaries)                   */
+    int loadloc;             /* 0 MBB, 1 cantilever (-loadloc)                      */
+    int optregion;           /* 0..3 (-optimizationRegion)                          */
+    int loadsignal;          /* 0 reference pulse (LinearElasticity.cc:597-606),
+                                1 sin(2 pi t) for t < 0.5                          */
+    double dalpha, dbeta;    /* Rayleigh damping (-dalph, -dbeta)                   */
+    /* GB300 solver controls */
+    int mixed;               /* 1: FP32 multigrid inside FP64 flexible CG           */
+    double rtol;             /* relative residual of every solve (reference 1e-10)  */
+    int maxit;               /* Krylov iteration cap                                */
+    int smooth;              /* Chebyshev degree of pre/post smoothing              */
+    double cheb_ratio;       /* Chebyshev lower bound = max(lo_bound, hi/ratio)     */
+    int use_graphs;          /* 1: CUDA graphs with device-side loop control        */
+} topo_le_params;
+
+typedef struct topo_le_stats {
+    long long cg_iterations;  /* outer Krylov iterations since creation */
+    long long solves;         /* linear solves since creation           */
+    double device_bytes;      /* HBM held by the object                 */
+    double last_fx;           /* last objective                         */
+} topo_le_stats;
+
+/* fills p with the reference defaults for a cantilever of nelx x nely x nelz
+ * unit elements (TopOpt.cc:75-159) and the GB300 solver defaults */
+void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz);
+
+/* LinearElasticity::LinearElasticity, LinearElasticity.h:29 / LinearElasticity.cc:13-127 */
+int topo_le_create(topo_le **out, const topo_le_params *p);
+/* LinearElasticity::~LinearElasticity */
+void topo_le_destroy(topo_le *le);
+
+/* LinearElasticity::CompleteInitialState, LinearElasticity.h:81 / .cc:956-1206 */
+int topo_le_complete_initial_state(topo_le *le, const double *xPhys, double Emin, double Emax, double Rmin,
+                                   double Rmax, double penalK, double penalM);
+int topo_le_complete_initial_state_dev(topo_le *le, const double *xPhys_dev, double Emin, double Emax,
+                                       double Rmin, double Rmax, double penalK, double penalM);
+/* LinearElasticity::GenerateCheckPoints, LinearElasticity.h:83 / .cc:1208-1280 */
+int topo_le_generate_checkpoints(topo_le *le);
+/* LinearElasticity::ComputeObjectiveSensitivities, LinearElasticity.h:42 / .cc:1625-1908.
+ * Overwrites *fx and dfdx (nel values).  Material parameters are the ones of
+ * the preceding CompleteInitialState (main.cc passes the same values). */
+int topo_le_compute_objective_sensitivities(topo_le *le, double *fx, double *dfdx);
+int topo_le_compute_objective_sensitivities_dev(topo_le *le, double *fx, double *dfdx_dev);
+/* LinearElasticity::VolumeConstraint, LinearElasticity.h:85 / .cc:1283-1296 */
+int topo_le_volume_constraint(topo_le *le, double *gx, double *dgdx, const double *xPhys, double volfrac);
+int topo_le_volume_constraint_dev(topo_le *le, double *gx, double *dgdx_dev, const double *xPhys_dev,
+                                  double volfrac);
+
+/* inspection (tests / output): which = 0 U, 1 DU, 2 DDU of step j of the
+ * resident block (j = -1: block start state); copies 3*nn values to host */
+int topo_le_get_state(topo_le *le, int which, int j, double *out);
+/* weighted products K x and M x with the current densities (no masking) */
+int topo_le_apply_km(topo_le *le, const double *x, double *Kx, double *Mx);
+int topo_le_get_stats(topo_le *le, topo_le_stats *out);
+/* CUDA-event timing of the matrix-free operator apply on the object's stream:
+ * `precision` 0 = FP64 (outer Krylov), 1 = FP32 (multigrid smoother);
+ * `reps` back-to-back launches after `warmup`; returns mean ms per launch */
+int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double *ms_per_launch);
+/* 24x24 box element matrices (E = 1, unit density) as applied by the
+ * matrix-free kernels, in the local node order of DMDAGetElements_3D
+ * (LinearElasticity.cc:3067-3074), row-major: the Hex8IsoparametricKE/ME
+ * products of LinearElasticity.cc:3089-3333.  Pure host arithmetic. */
+void topo_box_element_matrices(double hx, double hy, double hz, double nu, double *KE, double *ME);
+
+/* PDEFilt (PDEFilter.h:29-74): Helmholtz filter on the nodal grid */
+int topo_pdefilt_create(topo_pdefilt **out, int nx, int ny, int nz, double hx, double hy, double hz, double rmin,
+                        double rtol, int maxit);
+void topo_pdefilt_destroy(topo_pdefilt *f);
+/* PDEFilt::FilterProject (PDEFilter.cc:193-222) == PDEFilt::Gradients (:224) */
+int topo_pdefilt_filter_project(topo_pdefilt *f, const double *x, double *xout);
+int topo_pdefilt_filter_project_dev(topo_pdefilt *f, const double *x_dev, double *xout_dev);
+
+/* Filter::FilterProject for filter = 2 with optional smoothed Heaviside
+ * projection (Filter.cc:60-119, Filter.h:80-83) */
+int topo_filter_project(topo_pdefilt *f, const double *x, double *xTilde, double *xPhys, int projection,
+                        double beta, double eta);
+int topo_filter_project_dev(topo_pdefilt *f, const double *x_dev, double *xTilde_dev, double *xPhys_dev,
+                            int projection, double beta, double eta);
+/* Filter::Gradients for filter = 2 (Filter.cc:122-206): dfdx and the m
+ * constraint gradients dgdx[m*nel] are chain-ruled and filtered in place */
+int topo_filter_gradients(topo_pdefilt *f, const double *xTilde, double *dfdx, int m, double *dgdx, int projection,
+                          double beta, double eta);
+int topo_filter_gradients_dev(topo_pdefilt *f, const double *xTilde_dev, double *dfdx_dev, int m, double *dgdx_dev,
+                              int projection, double beta, double eta);
+/* Filter::GetMND (Filter.cc:208-227) */
+int topo_filter_mnd(topo_pdefilt *f, const double *x, double *mnd);
+int topo_filter_mnd_dev(topo_pdefilt *f, const double *x_dev, double *mnd);
+
+/* MMA (MMA.h:9-120), design variables resident on the device */
+int topo_mma_create(topo_mma **out, int n, int m, const double *a, const double *c, const double *d);
+void topo_mma_destroy(topo_mma *mma);
+int topo_mma_set_asymptotes(topo_mma *mma, double init, double decrease, double increase);
+/* MMA::SetOuterMovelimit (MMA.cc:374-393) */
+int topo_mma_set_outer_movelimit_dev(topo_mma *mma, double Xmin, double Xmax, double movlim, const double *x_dev,
+                                     double *xmin_dev, double *xmax_dev);
+/* MMA::Update (MMA.cc:487-507): xval updated in place; gx has m host values */
+int topo_mma_update(topo_mma *mma, double *xval, const double *dfdx, const double *gx, const double *dgdx,
+                    const double *xmin, const double *xmax);
+int topo_mma_update_dev(topo_mma *mma, double *xval_dev, const double *dfdx_dev, const double *gx,
+                        const double *dgdx_dev, const double *xmin_dev, const double *xmax_dev);
+/* MMA::DesignChange (MMA.cc:395-414): inf-norm change, xold <- x */
+int topo_mma_design_change_dev(topo_mma *mma, const double *x_dev, double *xold_dev, double *ch);
+/* MMA::KKTresidual (MMA.cc:416-484) */
+int topo_mma_kkt_residual_dev(topo_mma *mma, const double *x_dev, const double *dfdx_dev, const double *fx,
+                              const double *dgdx_dev, const double *xmin_dev, const double *xmax_dev, double *norm2,
+                              double *normInf);
+
+/* last error message of the calling thread, and a name for a status code */
+const char *topo_last_error(void);
+const char *topo_status_str(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

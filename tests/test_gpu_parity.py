@@ -1,0 +1,221 @@
+"""GPU parity: the sm_103a library, called through the C ABI, against the
+FP64 oracle on the same seeded inputs.
+
+Tolerances: plain FP64 path (FP64 multigrid inside FP64 flexible CG, solves
+to rtol 1e-12): objective 1e-10 relative, sensitivities 1e-9 of max|dfdx|.
+Mixed path (FP32 multigrid inside FP64 flexible CG): same solve tolerance on
+the FP64 residual, so the same bounds hold; the FP32 only changes iteration
+counts.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+MAT = dict(Emin=1e-9, Emax=1.0, Rmin=1e-3, Rmax=1.0, penalK=3.0, penalM=1.0)
+M6 = (MAT["Emin"], MAT["Emax"], MAT["Rmin"], MAT["Rmax"], MAT["penalK"], MAT["penalM"])
+
+
+def _le(n, **kw):
+    from topopt_in_petsc_transient_gb300 import LinearElasticity
+    return LinearElasticity(*n, **kw)
+
+
+def _run_gpu(le, x):
+    xd = torch.tensor(x, dtype=torch.float64, device="cuda")
+    df = torch.zeros_like(xd)
+    le.CompleteInitialState(xd, *M6)
+    le.GenerateCheckPoints()
+    fx = le.ComputeObjectiveSensitivities(df)
+    return fx, df.cpu().numpy()
+
+
+def _rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
+
+
+def test_operator_apply_matches_assembled_matrices(gpu):
+    n = (16, 8, 8)
+    rng = np.random.default_rng(0)
+    x = 0.1 + 0.8 * rng.random(np.prod(n))
+    le = _le(n, nlvls=3, ncp=1, tsc=2, t1=0.02, mixed=False)
+    le.CompleteInitialState(x, *M6)
+    ref = O.LinearElasticity(*n, ncp=1, tsc=2, t1=0.02)
+    ref.CompleteInitialState(x)
+    v = rng.standard_normal(le.ndof)
+    K, M = le.apply_km(v)
+    K2, M2 = ref.apply_KM(v)
+    assert _rel(K, K2) < 1e-13
+    assert _rel(M, M2) < 1e-13
+
+
+@pytest.mark.parametrize("objective", range(7))
+@pytest.mark.parametrize("mixed", [False, True])
+def test_objective_and_sensitivities_match_oracle(gpu, objective, mixed):
+    n = (8, 4, 4)
+    kw = dict(ncp=2, tsc=5, t1=0.5, objective=objective, loadsignal=1, dalpha=0.01, dbeta=0.01,
+              mInt=1 if objective == 4 else 0)
+    rng = np.random.default_rng(10 + objective)
+    x = 0.1 + 0.5 * rng.random(np.prod(n))
+    le = _le(n, nlvls=2, mixed=mixed, rtol=1e-12, **{k: v for k, v in kw.items() if k != "mInt"},
+             massInterpolation=kw["mInt"])
+    fx, df = _run_gpu(le, x)
+    ref = O.LinearElasticity(*n, **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert rc == 0
+    assert abs(fx - fx_r) <= 1e-10 * abs(fx_r), (fx, fx_r)
+    assert _rel(df, df_r) < 1e-9
+
+
+@pytest.mark.parametrize("ncp,tsc,graphs", [(1, 12, True), (3, 4, True), (4, 3, False)])
+def test_states_and_checkpointing(gpu, ncp, tsc, graphs):
+    n = (16, 8, 8)
+    rng = np.random.default_rng(3)
+    x = 0.12 + 0.04 * rng.random(np.prod(n))
+    kw = dict(ncp=ncp, tsc=tsc, t1=0.12, objective=3, loadsignal=1, dalpha=0.0, dbeta=1e-3)
+    le = _le(n, nlvls=3, mixed=True, rtol=1e-12, use_graphs=graphs, **kw)
+    fx, df = _run_gpu(le, x)
+    ref = O.LinearElasticity(*n, **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert abs(fx - fx_r) <= 1e-10 * abs(fx_r)
+    assert _rel(df, df_r) < 1e-9
+    # after the reverse sweep block 0 is resident: compare its last state
+    U, DU, DDU = ref.last_block_state(tsc - 1)
+    assert _rel(le.state(0, tsc - 1), U) < 1e-10
+    assert _rel(le.state(1, tsc - 1), DU) < 1e-9
+    assert _rel(le.state(2, tsc - 1), DDU) < 1e-8
+
+
+def test_reference_pulse_and_defaults(gpu):
+    # reference defaults: Emax 1e3, Rmax 4.1667e-4, reference load pulse, dt = 0.4
+    n = (8, 4, 4)
+    kw = dict(ncp=4, tsc=10, t1=16.0, objective=0, loadsignal=0, dalpha=1e-4, dbeta=1e-4)
+    mat = (1e-6, 1e3, 4.1667e-7, 4.1667e-4, 3.0, 1.0)
+    rng = np.random.default_rng(4)
+    x = 0.3 + 0.2 * rng.random(np.prod(n))
+    le = _le(n, nlvls=2, mixed=False, rtol=1e-12, **kw)
+    xd = torch.tensor(x, dtype=torch.float64, device="cuda")
+    df = torch.zeros_like(xd)
+    le.CompleteInitialState(xd, *mat)
+    le.GenerateCheckPoints()
+    fx = le.ComputeObjectiveSensitivities(df)
+    ref = O.LinearElasticity(*n, Emin=mat[0], Emax=mat[1], Rmin=mat[2], Rmax=mat[3], **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert abs(fx - fx_r) <= 1e-10 * abs(fx_r)
+    assert _rel(df.cpu().numpy(), df_r) < 1e-9
+
+
+def test_golden_fixture(gpu):
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "oracle_small.npz"))
+    for obj in (0, 3, 6):
+        le = _le((4, 2, 2), nlvls=2, ncp=2, tsc=3, t1=0.6, objective=obj, loadsignal=1, dalpha=0.01, dbeta=0.01,
+                 mixed=False, rtol=1e-13)
+        fx, df = _run_gpu(le, g["x"])
+        assert abs(fx - g["fx%d" % obj]) <= 1e-10 * abs(g["fx%d" % obj])
+        assert _rel(df, g["df%d" % obj]) < 1e-9
+
+
+def test_host_and_device_entry_points_agree(gpu):
+    n = (8, 4, 4)
+    rng = np.random.default_rng(6)
+    x = 0.2 + 0.3 * rng.random(np.prod(n))
+    kw = dict(nlvls=2, ncp=2, tsc=4, t1=0.4, objective=3, loadsignal=1, dbeta=1e-3, dalpha=0.0)
+    a = _le(n, **kw)
+    fx1, df1 = _run_gpu(a, x)
+    b = _le(n, **kw)
+    b.CompleteInitialState(x, *M6)
+    b.GenerateCheckPoints()
+    df2 = np.zeros(np.prod(n))
+    fx2 = b.ComputeObjectiveSensitivities(df2)
+    assert fx1 == fx2 and np.array_equal(df1, df2)  # deterministic kernels: bitwise
+    dg = np.zeros(np.prod(n))
+    gx = b.VolumeConstraint(dg, x, 0.3)
+    assert abs(gx - (x.mean() - 0.3)) < 1e-14 and np.allclose(dg, 1.0 / x.size)
+
+
+def test_pde_filter_and_projection(gpu):
+    from topopt_in_petsc_transient_gb300 import Filter, PDEFilt
+    n = (16, 8, 8)
+    rng = np.random.default_rng(8)
+    x = rng.random(np.prod(n))
+    f = PDEFilt(*n, 2.0, rtol=1e-13)
+    out = np.zeros_like(x)
+    f.FilterProject(x, out)
+    assert _rel(out, O.pde_filter(*n, x, 2.0)) < 1e-10
+    F = Filter(*n, 2, 2.0, rtol=1e-13)
+    xt, xp = np.zeros_like(x), np.zeros_like(x)
+    F.FilterProject(x, xt, xp, True, 4.0, 0.3)
+    xt_r, xp_r = O.filter_project(*n, x, 2.0, True, 4.0, 0.3)
+    assert _rel(xt, xt_r) < 1e-10 and _rel(xp, xp_r) < 1e-10
+    df = rng.standard_normal(x.size)
+    dg = np.full(x.size, 1.0 / x.size)
+    df_r, dg_r = O.filter_gradients(*n, xt_r, df, dg, 2.0, True, 4.0, 0.3)
+    F.Gradients(x, xt, df, 1, dg, True, 4.0, 0.3)
+    assert _rel(df, df_r) < 1e-9 and _rel(dg, dg_r) < 1e-9
+    assert abs(F.GetMND(xp) - O.filter_mnd(xp)) < 1e-13
+
+
+def test_mma_matches_oracle(gpu):
+    from topopt_in_petsc_transient_gb300 import MMA
+    n = 2000
+    rng = np.random.default_rng(9)
+    c = rng.random(n)
+    x = np.full(n, 0.5)
+    xo = x.copy()
+    mo = O.MMA(n, 1, x)
+    mo.SetAsymptotes(0.1, 0.6, 1.05)
+    mg = MMA(n, 1)
+    mg.SetAsymptotes(0.1, 0.6, 1.05)
+    xg = torch.tensor(x, dtype=torch.float64, device="cuda")
+    lo = torch.zeros_like(xg)
+    hi = torch.zeros_like(xg)
+    for it in range(5):
+        df = 2 * (xo - c) * (1 + 0.1 * it)
+        g = np.array([xo.mean() - 0.4])
+        dg = np.full(n, 1.0 / n)
+        lo_r, hi_r = O.MMA.SetOuterMovelimit(0.0, 1.0, 0.2, xo)
+        mo.Update(xo, df, g, dg, lo_r, hi_r)
+        mg.SetOuterMovelimit(0.0, 1.0, 0.2, xg, lo, hi)
+        mg.Update(xg, torch.tensor(df, device="cuda"), g, torch.tensor(dg, device="cuda"), lo, hi)
+        assert _rel(xg.cpu().numpy(), xo) < 1e-10, it
+
+
+def test_solver_failures_are_reported(gpu):
+    from topopt_in_petsc_transient_gb300 import TopoError
+    with pytest.raises(TopoError) as e:
+        _le((8, 4, 4), nlvls=4)  # 4 elements cannot be halved 3 times (TopOpt.cc:200-219)
+    assert e.value.status == 1
+    le = _le((8, 4, 4), nlvls=2, ncp=2, tsc=2, t1=0.2, loadsignal=1)
+    with pytest.raises(TopoError) as e:
+        le.GenerateCheckPoints()  # before CompleteInitialState
+    assert e.value.status == 7
+    # an iteration cap of 1 must surface as "not converged", not as a wrong answer
+    le = _le((8, 4, 4), nlvls=2, ncp=2, tsc=2, t1=0.2, loadsignal=1, maxit=1, rtol=1e-14)
+    x = np.full(128, 0.3)
+    with pytest.raises(TopoError) as e:
+        le.CompleteInitialState(x, *M6)
+        le.GenerateCheckPoints()
+    assert e.value.status == 4
+
+
+def test_finite_difference_check_on_gpu(gpu):
+    # central differences h = 1e-4 on seeded elements (the check of the
+    # 192x96x96 workload, here on a small mesh)
+    n = (8, 4, 4)
+    kw = dict(nlvls=2, ncp=2, tsc=5, t1=0.5, objective=3, loadsignal=1, dalpha=0.0, dbeta=1e-3, mixed=True,
+              rtol=1e-13)
+    rng = np.random.default_rng(11)
+    x = 0.12 + 0.02 * (2 * rng.random(np.prod(n)) - 1)
+    le = _le(n, **kw)
+    fx, df = _run_gpu(le, x)
+    h = 1e-4
+    for e in rng.choice(x.size, 6, replace=False):
+        xp, xm = x.copy(), x.copy()
+        xp[e] += h
+        xm[e] -= h
+        fd = (_run_gpu(le, xp)[0] - _run_gpu(le, xm)[0]) / (2 * h)
+        assert abs(fd - df[e]) <= 1e-6 * np.abs(df).max(), (e, fd, df[e])

@@ -1,0 +1,11 @@
+"""GB300-native transient solve-and-sensitivity path of TopOpt_in_PETSc_Transient.
+
+The compute backend is libtopopt_gb300.so (sm_103a CUDA kernels behind the C
+ABI in include/topopt_gb300.h).  Importing the package does not load it; the
+first object construction does, and fails loudly if it is missing.
+"""
+from ._lib import TopoError, load  # noqa: F401
+from .topopt import MMA, Filter, LinearElasticity, PDEFilt  # noqa: F401
+from .design import TopOpt, design_iteration  # noqa: F401
+
+__all__ = ["LinearElasticity", "PDEFilt", "Filter", "MMA", "TopOpt", "design_iteration", "TopoError", "load"]

@@ -1,0 +1,214 @@
+// common.cuh -- shared device machinery for the GB300 transient topology
+// optimisation path: structured-grid descriptors, the hex8 element operator in
+// the per-axis sum/difference ("mode") basis, and deterministic reductions.
+//
+// Data layout (identical to the reference DMDA natural ordering so host
+// buffers cross the C ABI without permutation, LinearElasticity.cc:3033-3087):
+//   node (i,j,k)    -> n = i + nx*(j + ny*k), displacement DOF 3*n + c
+//   element (i,j,k) -> e = i + ex*(j + ey*k)
+// Every nodal vector is DOF-interleaved (xyz per node); FP64 for states,
+// FP32 copies inside the multigrid preconditioner.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/topopt_gb300.h"
+
+namespace topo {
+
+// status codes TOPO_OK / TOPO_ERR_* come from the C ABI header
+// ---------------------------------------------------------------------------
+// one level of the structured node/element grid
+// ---------------------------------------------------------------------------
+struct GridDesc {
+    int nx, ny, nz;  // nodes
+    int ex, ey, ez;  // elements = nodes - 1
+    __host__ __device__ long long nn() const { return (long long)nx * ny * nz; }
+    __host__ __device__ long long nel() const { return (long long)ex * ey * ez; }
+};
+
+// Constants of the hex8 element operator on an hx*hy*hz box in the mode basis.
+//
+// Per axis the two nodal values (v0, v1) of an element edge are mapped to
+// s = v0 + v1 and d = v1 - v0; the trilinear field is then
+//   u = sum_m U_m psi_p(xi) psi_q(eta) psi_r(zeta),  psi_s = 1/2, psi_d = xi - 1/2,
+// with m = p + 2q + 4r (bit set = difference mode).  In this basis the 2x2x2
+// Gauss-integrated (exact for a box) mass matrix is diagonal with weights
+// W_m = V prod(w), w_s = 1/4, w_d = 1/12, and the isotropic stiffness couples
+// only a handful of modes (d/dx psi_d = 2 psi_s).  The element matrices are
+// therefore applied with ~290 flops instead of the 1536 of the dense 24x24
+// products of LinearElasticity.cc:3089-3333, with identical results up to
+// rounding (the reference's truncated Gauss abscissa differs by 2e-16).
+template <class T>
+struct ElemConst {
+    T W[8];     // V * w_p * w_q * w_r
+    T g[3];     // 2 / h_a
+    T lam, mu;  // Lame parameters for E = 1 (LinearElasticity.cc:3134-3135)
+};
+
+template <class T>
+__host__ __device__ inline ElemConst<T> make_elem_const(double hx, double hy, double hz, double nu) {
+    ElemConst<T> c;
+    double V = hx * hy * hz;
+    const double w[2] = {0.25, 1.0 / 12.0};
+    for (int m = 0; m < 8; m++) c.W[m] = (T)(V * w[m & 1] * w[(m >> 1) & 1] * w[(m >> 2) & 1]);
+    c.g[0] = (T)(2.0 / hx);
+    c.g[1] = (T)(2.0 / hy);
+    c.g[2] = (T)(2.0 / hz);
+    c.lam = (T)(nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
+    c.mu = (T)(1.0 / (2.0 * (1.0 + nu)));
+    return c;
+}
+
+// nodal -> mode transform of one component (local node L = ax + 2ay + 4az)
+template <class T>
+__host__ __device__ __forceinline__ void mode_fwd(T v[8]) {
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        const int b = 1 << s;
+#pragma unroll
+        for (int L = 0; L < 8; L++) {
+            if (L & b) continue;
+            T a0 = v[L], a1 = v[L | b];
+            v[L] = a0 + a1;
+            v[L | b] = a1 - a0;
+        }
+    }
+}
+
+// transpose of mode_fwd: mode -> nodal (used for operator outputs y = T^t Y)
+template <class T>
+__host__ __device__ __forceinline__ void mode_bwd(T v[8]) {
+#pragma unroll
+    for (int s = 2; s >= 0; s--) {
+        const int b = 1 << s;
+#pragma unroll
+        for (int L = 0; L < 8; L++) {
+            if (L & b) continue;
+            T sv = v[L], dv = v[L | b];
+            v[L] = sv - dv;
+            v[L | b] = sv + dv;
+        }
+    }
+}
+
+// Y = Khat U : element stiffness (E = 1) in mode space, without density factor.
+// G_ab(m) = d u_b / d x_a on modes with bit a clear; strain energy density
+// lam (div u)^2 + mu sum g_ab^2 + mu sum g_ab g_ba (isotropic, Voigt C of
+// LinearElasticity.cc:3141-3146).
+template <class T>
+__host__ __device__ __forceinline__ void mode_stiffness(const ElemConst<T> &C, const T U[3][8], T Y[3][8]) {
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int m = 0; m < 8; m++) Y[b][m] = T(0);
+    T D[8];
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+        T acc = T(0);
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+            if (!(m & (1 << a))) acc += C.g[a] * U[a][m | (1 << a)];
+        D[m] = acc;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                if (m & (1 << a)) continue;
+                T gab = C.g[a] * U[b][m | (1 << a)];
+                T sym = gab;
+                if (!(m & (1 << b))) sym += C.g[b] * U[a][m | (1 << b)];
+                T S = C.mu * sym;
+                if (a == b) S += C.lam * D[m];
+                Y[b][m | (1 << a)] += C.g[a] * (C.W[m] * S);
+            }
+}
+
+// y_e = ck * KE u_e + cm * ME u_e for one element: in/out indexed [comp][L]
+template <class T>
+__host__ __device__ __forceinline__ void elem_apply(const ElemConst<T> &C, T ck, T cm, T u[3][8], T y[3][8]) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) mode_fwd(u[c]);
+    mode_stiffness(C, u, y);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+#pragma unroll
+        for (int m = 0; m < 8; m++) y[c][m] = ck * y[c][m] + (cm * C.W[m]) * u[c][m];
+        mode_bwd(y[c]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// deterministic grid-wide reductions: per-CTA partials, last CTA sums in a
+// fixed order (no floating-point atomics, bitwise reproducible)
+// ---------------------------------------------------------------------------
+template <int NV>
+struct Partials {
+    double *part;           // [gridDim][NV]
+    unsigned int *counter;  // one counter per reduction site, reset by last CTA
+};
+
+template <int NT, int NV>
+__device__ __forceinline__ void block_reduce(double v[NV], double *smem /* [NV][NT/32] */) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        double x = v[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) smem[i * (NT / 32) + wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+            double s = 0.0;
+            for (int w = 0; w < NT / 32; w++) s += smem[i * (NT / 32) + w];
+            v[i] = s;
+        }
+    }
+}
+
+// Called by every thread of every CTA (1D-linearised block id).  Returns true
+// in exactly one thread (thread 0 of the last CTA to finish); on that thread
+// `tot` holds the grid sums.
+template <int NT, int NV>
+__device__ __forceinline__ bool grid_reduce(double v[NV], const Partials<NV> &P, double tot[NV]) {
+    __shared__ double sred[NV * (NT / 32)];
+    __shared__ bool last;
+    block_reduce<NT, NV>(v, sred);
+    const unsigned int nblk = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) P.part[(size_t)bid * NV + i] = v[i];
+        __threadfence();
+        unsigned int t = atomicAdd(P.counter, 1u);
+        last = (t == nblk - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    // every thread of the last CTA sums a fixed strided subset, then a fixed
+    // shuffle tree: the summation order depends only on the grid size
+    double s[NV];
+#pragma unroll
+    for (int i = 0; i < NV; i++) s[i] = 0.0;
+    for (unsigned int b = threadIdx.x; b < nblk; b += NT)
+#pragma unroll
+        for (int i = 0; i < NV; i++) s[i] += ((volatile double *)P.part)[(size_t)b * NV + i];
+    __syncthreads();
+    block_reduce<NT, NV>(s, sred);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) tot[i] = s[i];
+        *P.counter = 0u;
+        return true;
+    }
+    return false;
+}
+
+}  // namespace topo

@@ -1,0 +1,407 @@
+// kernels.cuh -- element-wise, transfer, coarse-solve, Krylov-scalar,
+// time-integration and sensitivity kernels of the transient path.
+#pragma once
+#include "policies.cuh"
+
+namespace topo {
+
+constexpr int EW = 256;  // threads of element-wise kernels
+
+__host__ inline unsigned ew_blocks(long long n) {
+    long long b = (n + EW - 1) / EW;
+    return (unsigned)(b < 1 ? 1 : (b > 65535LL * 64 ? 65535LL * 64 : b));
+}
+
+// ---------------------------------------------------------------------------
+// material interpolation, InterpolateStiffness / InterpolateMass
+// (LinearElasticity.cc:1580-1623)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void interp_dev(int type, double vmax, double vmin, double pen, double x, double &f,
+                                           double &df) {
+    if (type == 0) {
+        f = vmin + x * (vmax - vmin);
+        df = vmax - vmin;
+    } else if (type == 1) {
+        f = vmin + pow(x, pen) * (vmax - vmin);
+        df = pen * pow(x, pen - 1) * (vmax - vmin);
+    } else {
+        f = vmin + x / (1 + pen * (1 - x)) * (vmax - vmin);
+        double q = 1 + pen * (1 - x);
+        df = (1 + pen) / (q * q) * (vmax - vmin);
+    }
+}
+
+struct MatParams {
+    int sInt, mInt;
+    double Emin, Emax, penalK, Rmin, Rmax, penalM;
+};
+
+static __global__ void k_interp(long long nel, const double *__restrict__ x, MatParams mp, double *kf, double *dkf, double *mf,
+                         double *dmf, float *kff, float *mff) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
+        double k, dk, m, dm;
+        interp_dev(mp.sInt, mp.Emax, mp.Emin, mp.penalK, x[e], k, dk);
+        interp_dev(mp.mInt, mp.Rmax, mp.Rmin, mp.penalM, x[e], m, dm);
+        kf[e] = k;
+        dkf[e] = dk;
+        mf[e] = m;
+        dmf[e] = dm;
+        kff[e] = (float)k;
+        mff[e] = (float)m;
+    }
+}
+
+// coarse element density factors: mean of the 8 children (rediscretised
+// coarse operators of the geometric multigrid)
+static __global__ void k_coarsen(GridDesc gf, GridDesc gc, const double *__restrict__ kf, const double *__restrict__ mf,
+                          double *kc, double *mc, float *kcf, float *mcf) {
+    long long nel = gc.nel();
+    for (long long E = blockIdx.x * (long long)blockDim.x + threadIdx.x; E < nel; E += (long long)gridDim.x * blockDim.x) {
+        int I = (int)(E % gc.ex), J = (int)((E / gc.ex) % gc.ey), K = (int)(E / ((long long)gc.ex * gc.ey));
+        double sk = 0.0, sm = 0.0;
+        for (int c = 0; c < 8; c++) {
+            long long e = (2 * I + (c & 1)) + (long long)gf.ex * ((2 * J + ((c >> 1) & 1)) + (long long)gf.ey * (2 * K + (c >> 2)));
+            sk += kf[e];
+            sm += mf[e];
+        }
+        kc[E] = 0.125 * sk;
+        mc[E] = 0.125 * sm;
+        kcf[E] = (float)(0.125 * sk);
+        mcf[E] = (float)(0.125 * sm);
+    }
+}
+
+// inverse of the assembled diagonal of (N A N + I - N), A = sum_e (sK kf_e KE + sM mf_e ME)
+static __global__ void k_dinv(GridDesc g, const uint8_t *__restrict__ fixed, const double *__restrict__ kf,
+                       const double *__restrict__ mf, double sK, double sM, double dK0, double dK1, double dK2, double dM,
+                       double *dinvd, float *dinvf) {
+    long long nn = g.nn();
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
+        double sk = 0.0, sm = 0.0;
+        for (int c = 0; c < 8; c++) {
+            int ei = i - (c & 1), ej = j - ((c >> 1) & 1), ek = k - (c >> 2);
+            if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ex || ej >= g.ey || ek >= g.ez) continue;
+            long long e = ei + (long long)g.ex * (ej + (long long)g.ey * ek);
+            if (kf) sk += kf[e];
+            sm += mf[e];
+        }
+        uint8_t f = fixed[n];
+        const double dK[3] = {dK0, dK1, dK2};
+        for (int c = 0; c < 3; c++) {
+            double d = sK * sk * dK[c] + sM * sm * dM;
+            double v = ((f >> c) & 1) ? 1.0 : 1.0 / d;
+            dinvd[3 * n + c] = v;
+            dinvf[3 * n + c] = (float)v;
+        }
+    }
+}
+
+// Spectrum bounds of Dinv A from the element-wise Rayleigh-quotient argument:
+// x'Ax = sum_e x_e'(ck KE + cm ME)x_e <= sum_e sum_i x_ei^2 (ck lamK dK_i + cm lamM dM)
+// so lambda_max(Dinv A) <= max_{e,i} (ck lamK dK_i + cm lamMhi dM)/(ck dK_i + cm dM),
+// lambda_min(Dinv A) >= min_{e,i} cm lamMlo dM / (ck dK_i + cm dM)  (lamK_min = 0).
+// Non-negative doubles order like their bit patterns, so atomicMax/Min on the
+// bits is exact and order independent.
+static __global__ void k_bounds(long long nel, const double *__restrict__ kf, const double *__restrict__ mf, double sK,
+                         double sM, double dK0, double dK1, double dK2, double dM, double lamK, double lamMlo,
+                         double lamMhi, unsigned long long *bits /* [0]=max hi, [1]=min lo */) {
+    double hi = 0.0, lo = 1e300;
+    const double dK[3] = {dK0, dK1, dK2};
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
+        double ck = kf ? sK * kf[e] : 0.0, cm = sM * mf[e];
+        for (int c = 0; c < 3; c++) {
+            double den = ck * dK[c] + cm * dM;
+            if (den <= 0.0) continue;
+            hi = fmax(hi, (ck * lamK * dK[c] + cm * lamMhi * dM) / den);
+            lo = fmin(lo, (cm * lamMlo * dM) / den);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&bits[0], (unsigned long long)__double_as_longlong(hi));
+        atomicMin(&bits[1], (unsigned long long)__double_as_longlong(lo));
+    }
+}
+
+static __global__ void k_bounds_init(unsigned long long *bits) {
+    bits[0] = 0ull;
+    bits[1] = (unsigned long long)__double_as_longlong(1e300);
+}
+
+// Chebyshev interval: [max(lo_bound, hi/ratio), hi]; the Dirichlet identity
+// rows contribute eigenvalue 1 and are kept inside the interval.
+static __global__ void k_bounds_final(const unsigned long long *bits, double ratio, double *lohi) {
+    double hi = __longlong_as_double((long long)bits[0]);
+    double lo = __longlong_as_double((long long)bits[1]);
+    hi = fmax(hi, 1.0);
+    double l = fmax(lo, hi / ratio);
+    l = fmin(l, 1.0);
+    lohi[0] = l;
+    lohi[1] = hi;
+}
+
+// first Chebyshev step from a zero initial guess: d = Dinv b / theta, x = d
+template <class T>
+static __global__ void k_cheb0(long long ndof, const T *__restrict__ b, const T *__restrict__ dinv, const double *lohi, T *x,
+                        T *d) {
+    T c1, c2;
+    cheb_coeffs<T>(lohi, 0, c1, c2);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        T v = c2 * dinv[i] * b[i];
+        d[i] = v;
+        x[i] = v;
+    }
+}
+
+// Restriction = transpose of trilinear prolongation (the DMDA Q1
+// interpolation of DMCreateInterpolation, LinearElasticity.cc:2838-2842):
+// coarse node gathers fine nodes 2I-1..2I+1 with weights 1/2, 1, 1/2 per axis.
+template <class T>
+static __global__ void k_restrict(GridDesc gf, GridDesc gc, const uint8_t *__restrict__ fixc, const T *__restrict__ rf, T *bc) {
+    long long nn = gc.nn();
+    for (long long N = blockIdx.x * (long long)blockDim.x + threadIdx.x; N < nn; N += (long long)gridDim.x * blockDim.x) {
+        int I = (int)(N % gc.nx), J = (int)((N / gc.nx) % gc.ny), K = (int)(N / ((long long)gc.nx * gc.ny));
+        T acc[3] = {T(0), T(0), T(0)};
+        for (int dk = -1; dk <= 1; dk++) {
+            int k = 2 * K + dk;
+            if (k < 0 || k >= gf.nz) continue;
+            T wk = dk ? T(0.5) : T(1);
+            for (int dj = -1; dj <= 1; dj++) {
+                int j = 2 * J + dj;
+                if (j < 0 || j >= gf.ny) continue;
+                T wj = wk * (dj ? T(0.5) : T(1));
+                for (int di = -1; di <= 1; di++) {
+                    int i = 2 * I + di;
+                    if (i < 0 || i >= gf.nx) continue;
+                    T w = wj * (di ? T(0.5) : T(1));
+                    long long n = i + (long long)gf.nx * (j + (long long)gf.ny * k);
+                    acc[0] += w * rf[3 * n];
+                    acc[1] += w * rf[3 * n + 1];
+                    acc[2] += w * rf[3 * n + 2];
+                }
+            }
+        }
+        mask3(fixc[N], acc);
+        bc[3 * N] = acc[0];
+        bc[3 * N + 1] = acc[1];
+        bc[3 * N + 2] = acc[2];
+    }
+}
+
+// x_f += P x_c (trilinear), clamped DOFs untouched
+template <class T>
+static __global__ void k_prolong(GridDesc gf, GridDesc gc, const uint8_t *__restrict__ fixf, const T *__restrict__ xc, T *xf) {
+    long long nn = gf.nn();
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(n % gf.nx), j = (int)((n / gf.nx) % gf.ny), k = (int)(n / ((long long)gf.nx * gf.ny));
+        int I0 = i >> 1, J0 = j >> 1, K0 = k >> 1;
+        int I1 = I0 + (i & 1), J1 = J0 + (j & 1), K1 = K0 + (k & 1);
+        T acc[3] = {T(0), T(0), T(0)};
+        for (int c = 0; c < 8; c++) {
+            int I = (c & 1) ? I1 : I0, J = ((c >> 1) & 1) ? J1 : J0, K = (c >> 2) ? K1 : K0;
+            // duplicate corners (even index) carry weight 1 split over the two equal picks
+            T w = T(0.125);
+            long long N = I + (long long)gc.nx * (J + (long long)gc.ny * K);
+            acc[0] += w * xc[3 * N];
+            acc[1] += w * xc[3 * N + 1];
+            acc[2] += w * xc[3 * N + 2];
+        }
+        uint8_t f = fixf[n];
+        for (int c = 0; c < 3; c++)
+            if (!((f >> c) & 1)) xf[3 * n + c] += acc[c];
+    }
+}
+
+// y = A x for the explicit coarse inverse (one warp per row)
+template <class T>
+static __global__ void k_gemv(int n, const T *__restrict__ A, const T *__restrict__ x, T *y) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const T *row = A + (size_t)warp * n;
+    T acc = T(0);
+    for (int j = lane; j < n; j += 32) acc += row[j] * x[j];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[warp] = acc;
+}
+
+// dense coarsest-level operator, one thread per entry: sum over the (at most 8)
+// elements shared by the two nodes, fixed order (deterministic).  Element
+// matrices KE/ME are the 24x24 box matrices in lexicographic local order.
+static __global__ void k_coarse_assemble(GridDesc g, const uint8_t *__restrict__ fixed, const double *__restrict__ kf,
+                                  const double *__restrict__ mf, double sK, double sM, const double *__restrict__ KE,
+                                  const double *__restrict__ ME, double *A) {
+    long long nd = 3 * g.nn();
+    long long tot = nd * nd;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+        long long r = t / nd, s = t % nd;
+        long long nr = r / 3, ns = s / 3;
+        int cr = (int)(r % 3), cs = (int)(s % 3);
+        int ir = (int)(nr % g.nx), jr = (int)((nr / g.nx) % g.ny), kr = (int)(nr / ((long long)g.nx * g.ny));
+        int is = (int)(ns % g.nx), js = (int)((ns / g.nx) % g.ny), ks = (int)(ns / ((long long)g.nx * g.ny));
+        bool fr = (fixed[nr] >> cr) & 1, fs = (fixed[ns] >> cs) & 1;
+        double v = 0.0;
+        if (fr || fs) {
+            v = (r == s) ? 1.0 : 0.0;
+        } else if (abs(ir - is) <= 1 && abs(jr - js) <= 1 && abs(kr - ks) <= 1) {
+            for (int c = 0; c < 8; c++) {
+                int ei = ir - (c & 1), ej = jr - ((c >> 1) & 1), ek = kr - (c >> 2);
+                if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ex || ej >= g.ey || ek >= g.ez) continue;
+                int ax = is - ei, ay = js - ej, az = ks - ek;
+                if (ax < 0 || ax > 1 || ay < 0 || ay > 1 || az < 0 || az > 1) continue;
+                int La = c, Lb = ax + 2 * ay + 4 * az;
+                long long e = ei + (long long)g.ex * (ej + (long long)g.ey * ek);
+                int ia = 3 * La + cr, ib = 3 * Lb + cs;
+                double ck = kf ? sK * kf[e] : 0.0, cm = sM * mf[e];
+                v += ck * KE[ia * 24 + ib] + cm * ME[ia * 24 + ib];
+            }
+        }
+        A[t] = v;
+    }
+}
+
+// In-place Gauss-Jordan inversion (SPD, no pivoting), step k in two passes.
+static __global__ void k_gj_save(const double *A, int n, int k, double *rowk, double *colk) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        rowk[t] = A[(size_t)k * n + t];
+        colk[t] = A[(size_t)t * n + k];
+    }
+}
+static __global__ void k_gj_update(double *A, int n, int k, const double *__restrict__ rowk, const double *__restrict__ colk) {
+    long long tot = (long long)n * n;
+    double p = rowk[k];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(t / n), j = (int)(t % n);
+        double v;
+        if (i == k && j == k)
+            v = 1.0 / p;
+        else if (i == k)
+            v = rowk[j] / p;
+        else if (j == k)
+            v = -colk[i] / p;
+        else
+            v = A[t] - colk[i] * rowk[j] / p;
+        A[t] = v;
+    }
+}
+
+static __global__ void k_d2f(long long n, const double *__restrict__ a, float *b) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+static __global__ void k_copy(long long n, const double *__restrict__ a, double *b) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = a[i];
+}
+
+// ---------------------------------------------------------------------------
+// flexible CG (Notay's FCG(1)): p_{k+1} = z_{k+1} - (z_{k+1}.q_k / p_k.q_k) p_k
+// ---------------------------------------------------------------------------
+template <class TZ>
+static __global__ void k_fcg_dot(long long ndof, const TZ *__restrict__ z, const double *__restrict__ r,
+                          const double *__restrict__ q, SolveScalars *S, Partials<2> part) {
+    double v[2] = {0.0, 0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        double zi = (double)z[i];
+        v[0] += zi * r[i];
+        v[1] += zi * q[i];
+    }
+    double tot[2];
+    if (grid_reduce<EW, 2>(v, part, tot)) {
+        S->rho = tot[0];
+        S->gam = tot[1];
+        S->beta = (S->it == 0) ? 0.0 : -tot[1] / S->pq;
+        if (!isfinite(tot[0])) {
+            S->status = TOPO_ERR_NAN;
+            S->done = 1;
+        }
+    }
+}
+
+template <class TZ>
+static __global__ void k_fcg_p(long long ndof, const TZ *__restrict__ z, double *p, const SolveScalars *S) {
+    double beta = S->beta;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)
+        p[i] = (beta == 0.0) ? (double)z[i] : (double)z[i] + beta * p[i];
+}
+
+static __global__ void k_fcg_update(long long ndof, double *x, double *r, float *r32, const double *__restrict__ p,
+                             const double *__restrict__ q, SolveScalars *S, Partials<1> part,
+                             cudaGraphConditionalHandle cond, int has_cond) {
+    double alpha = S->alpha;
+    double v[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        x[i] += alpha * p[i];
+        double rv = r[i] - alpha * q[i];
+        r[i] = rv;
+        if (r32) r32[i] = (float)rv;
+        v[0] += rv * rv;
+    }
+    double tot[1];
+    if (grid_reduce<EW, 1>(v, part, tot)) {
+        S->rr = tot[0];
+        S->it += 1;
+        S->total_it += 1;
+        S->rho_old = S->rho;
+        if (!isfinite(tot[0])) {
+            S->status = TOPO_ERR_NAN;
+            S->done = 1;
+        } else if (tot[0] <= S->tol2 * S->bb) {
+            S->done = 1;
+        } else if (S->it >= S->maxit) {
+            S->status = TOPO_ERR_NOT_CONVERGED;
+            S->done = 1;
+        }
+        if (has_cond) cudaGraphSetConditional(cond, S->done ? 0u : 1u);
+    }
+}
+
+static __global__ void k_fcg_zero_x(long long ndof, double *x, const SolveScalars *S) {
+    if (!S->zero_x) return;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)
+        x[i] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Newmark corrector (SolveStateBlock, LinearElasticity.cc:1363-1375):
+//   du = a0 du- + a1 ddu- + a2 (u - u-),  ddu = -a3 du- - a4 ddu- + a5 (u - u-)
+// writes step j of the block history
+// ---------------------------------------------------------------------------
+struct Newmark {
+    double a[6];
+};
+
+static __global__ void k_newmark(long long ndof, const double *__restrict__ x, const StepCtx *st, const double *cp, double *Uh,
+                          double *DUh, double *DDUh, Newmark nm) {
+    int j = st->j;
+    const double *u, *du, *ddu;
+    if (j == 0) {
+        const double *base = cp + (long long)st->block * 3 * ndof;
+        u = base;
+        du = base + ndof;
+        ddu = base + 2 * ndof;
+    } else {
+        u = Uh + (long long)(j - 1) * ndof;
+        du = DUh + (long long)(j - 1) * ndof;
+        ddu = DDUh + (long long)(j - 1) * ndof;
+    }
+    double *uo = Uh + (long long)j * ndof, *duo = DUh + (long long)j * ndof, *dduo = DDUh + (long long)j * ndof;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        double un = x[i], dU = un - u[i];
+        uo[i] = un;
+        duo[i] = nm.a[0] * du[i] + nm.a[1] * ddu[i] + nm.a[2] * dU;
+        dduo[i] = -nm.a[3] * du[i] - nm.a[4] * ddu[i] + nm.a[5] * dU;
+    }
+}
+
+static __global__ void k_step_set(StepCtx *st, int block, int j) {
+    st->block = block;
+    st->j = j;
+}
+static __global__ void k_step_add(StepCtx *st, int delta) { st->j += delta; }
+
+}  // namespace topo

@@ -1,0 +1,1128 @@
+// le.cu -- GB300 LinearElasticity: transient Newmark forward solves, discrete
+// adjoint and element sensitivities of TopOpt_in_PETSc_Transient
+// (LinearElasticity.cc), matrix-free on one GPU.
+//
+// Per design iteration (main.cc:82-90):
+//   CompleteInitialState -> element factors, multigrid hierarchy, initial
+//     acceleration from the masked mass solve, checkpoint 0
+//   GenerateCheckPoints  -> forward blocks 0..ncp-1, checkpoints in HBM
+//   ComputeObjectiveSensitivities -> reverse block loop: recompute the block
+//     (skipped for the last block, whose history is still resident), adjoint
+//     steps with fused element sensitivities/objective, t = 0 mass solve.
+// Every linear solve is a flexible CG whose preconditioner is a geometric
+// multigrid V-cycle (Chebyshev-Jacobi smoothing, trilinear transfer,
+// rediscretised coarse operators, dense coarsest inverse), run either in FP64
+// ("plain") or in FP32 inside the FP64 outer iteration ("mixed").
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "le.h"
+#include "sens.cuh"
+
+namespace topo {
+
+#define CK(call)                                                                 \
+    do {                                                                         \
+        cudaError_t e_ = (call);                                                 \
+        if (e_ != cudaSuccess) {                                                 \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));      \
+            return TOPO_ERR_CUDA;                                                \
+        }                                                                        \
+    } while (0)
+
+static thread_local std::string g_last_error;
+void set_error(const std::string &s) { g_last_error = s; }
+const char *last_error() { return g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------
+// host helpers: element matrices of a box from the mode operator
+// ---------------------------------------------------------------------------
+void box_element_matrices(double hx, double hy, double hz, double nu, double *KE, double *ME) {
+    ElemConst<double> C = make_elem_const<double>(hx, hy, hz, nu);
+    for (int col = 0; col < 24; col++) {
+        double u[3][8] = {{0}}, y[3][8];
+        u[col % 3][col / 3] = 1.0;
+        double U[3][8];
+        memcpy(U, u, sizeof(U));
+        for (int c = 0; c < 3; c++) mode_fwd(U[c]);
+        mode_stiffness(C, U, y);
+        for (int c = 0; c < 3; c++) {
+            double t[8];
+            for (int m = 0; m < 8; m++) t[m] = y[c][m];
+            mode_bwd(t);
+            for (int L = 0; L < 8; L++) KE[(3 * L + c) * 24 + col] = t[L];
+            for (int m = 0; m < 8; m++) t[m] = C.W[m] * U[c][m];
+            mode_bwd(t);
+            for (int L = 0; L < 8; L++) ME[(3 * L + c) * 24 + col] = t[L];
+        }
+    }
+}
+
+// largest eigenvalue of diag(A)^-1/2 A diag(A)^-1/2 (24x24 SPD) by power iteration
+static double jacobi_scaled_lmax(const double *A) {
+    double d[24], v[24], w[24];
+    for (int i = 0; i < 24; i++) {
+        d[i] = 1.0 / sqrt(A[i * 24 + i]);
+        v[i] = 1.0 + 0.01 * i;
+    }
+    double lam = 0.0;
+    for (int it = 0; it < 2000; it++) {
+        double nrm = 0.0;
+        for (int i = 0; i < 24; i++) {
+            double s = 0.0;
+            for (int j = 0; j < 24; j++) s += d[i] * A[i * 24 + j] * d[j] * v[j];
+            w[i] = s;
+            nrm += s * s;
+        }
+        nrm = sqrt(nrm);
+        double l = 0.0;
+        for (int i = 0; i < 24; i++) l += v[i] * w[i];
+        double vn = 0.0;
+        for (int i = 0; i < 24; i++) vn += v[i] * v[i];
+        lam = l / vn;
+        for (int i = 0; i < 24; i++) v[i] = w[i] / nrm;
+    }
+    return lam;
+}
+
+// ---------------------------------------------------------------------------
+// device memory arena: every allocation of an object, released together
+// ---------------------------------------------------------------------------
+struct Arena {
+    std::vector<void *> ptrs;
+    size_t bytes = 0;
+    template <class T>
+    int get(T **p, size_t n) {
+        void *q = nullptr;
+        size_t b = sizeof(T) * (n ? n : 1);
+        cudaError_t e = cudaMalloc(&q, b);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error(std::string("cudaMalloc of ") + std::to_string(b) + " bytes failed: " + cudaGetErrorString(e));
+            return TOPO_ERR_OOM;
+        }
+        cudaMemset(q, 0, b);
+        ptrs.push_back(q);
+        bytes += b;
+        *p = (T *)q;
+        return TOPO_OK;
+    }
+    void release() {
+        for (void *p : ptrs) cudaFree(p);
+        ptrs.clear();
+        bytes = 0;
+    }
+};
+
+#define AG(p, n)                                 \
+    do {                                         \
+        int rc_ = arena.get(&(p), (size_t)(n));  \
+        if (rc_) return rc_;                     \
+    } while (0)
+
+template <class T, class Pol>
+static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, cudaStream_t s) {
+    static bool attr = false;
+    const size_t sm = tile_smem_bytes<T, Pol>();
+    if (!attr) {
+        cudaFuncSetAttribute(k_tile<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        attr = true;
+    }
+    k_tile<T, Pol><<<tile_grid(g), TILE_THREADS, sm, s>>>(g, C, pol);
+}
+
+// ---------------------------------------------------------------------------
+// multigrid hierarchy
+// ---------------------------------------------------------------------------
+struct Level {
+    GridDesc g;
+    double h[3];
+    ElemConst<double> Cd;
+    ElemConst<float> Cf;
+    double dK[3], dM, lamK;
+    uint8_t *fixed = nullptr;
+    double *kfd = nullptr, *mfd = nullptr;  // density factors on this level
+    float *kff = nullptr, *mff = nullptr;
+    // V-cycle work vectors
+    float *fb = nullptr, *fxa = nullptr, *fxb = nullptr, *fd = nullptr, *fr = nullptr;
+    double *db = nullptr, *dxa = nullptr, *dxb = nullptr, *dd = nullptr, *dr = nullptr;
+};
+
+struct OpLevel {
+    double *dinvd = nullptr;
+    float *dinvf = nullptr;
+    double *lohi = nullptr;  // device [2]
+};
+
+struct Operator {
+    double sK = 0.0, sM = 1.0;  // A = sK * K(kf) + sM * M(mf)
+    std::vector<OpLevel> lv;
+    double *Ainv_d = nullptr;
+    float *Ainv_f = nullptr;
+};
+
+struct TopoLE {
+    LEParams p;
+    GridDesc g;
+    long long nn = 0, nel = 0, ndof = 0;
+    int Ts = 0;
+    double dt = 0.0, a[6] = {0};
+    int nlev = 1;
+    std::vector<Level> L;
+    Operator ops[2];  // 0: Newmark effective operator, 1: mass
+    Arena arena;
+    cudaStream_t stream = nullptr;
+
+    // fine-level data
+    double *N_host_dummy = nullptr;
+    double *rhs0 = nullptr, *P = nullptr, *xPhys = nullptr;
+    double *kf = nullptr, *dkf = nullptr, *mf = nullptr, *dmf = nullptr;
+    float *cntP = nullptr;
+    double *cp = nullptr;                   // (ncp+1) x 3 x ndof
+    double *Uh = nullptr, *DUh = nullptr, *DDUh = nullptr;  // tsc x ndof
+    double *Lp1 = nullptr, *DLp1 = nullptr, *DDLp1 = nullptr, *DLc = nullptr, *DDLc = nullptr;
+    double *KL = nullptr, *ML = nullptr, *hK = nullptr, *hM = nullptr;
+    double *DDL0 = nullptr;
+    double *df = nullptr;
+    // solver vectors
+    double *sx = nullptr, *sb = nullptr, *sr = nullptr, *sp = nullptr, *sq = nullptr, *sz = nullptr;
+    float *sr32 = nullptr;
+    // coarse assembly scratch
+    double *KEc = nullptr, *MEc = nullptr, *Acoarse = nullptr, *gj_row = nullptr, *gj_col = nullptr;
+    int ncoarse = 0;
+    // control block
+    SolveScalars *S = nullptr;
+    StepCtx *st = nullptr;
+    double *part = nullptr;
+    unsigned int *counter = nullptr;
+    unsigned long long *bbits = nullptr;
+    int *err = nullptr;
+    long long nsolves = 0;
+    // graphs
+    cudaGraphExec_t gx_fwd = nullptr, gx_adj = nullptr;
+    int graphs_ok = 0;
+    // diagnostics
+    LEStats stats;
+    int last_block_resident = -1;
+    int design_ready = 0;
+};
+
+static Partials<1> P1(TopoLE *le) { return Partials<1>{le->part, le->counter}; }
+static Partials<2> P2(TopoLE *le) { return Partials<2>{le->part, le->counter}; }
+
+// ---------------------------------------------------------------------------
+// creation
+// ---------------------------------------------------------------------------
+int le_create(TopoLE **out, const LEParams *pp) {
+    *out = nullptr;
+    const LEParams &p = *pp;
+    if (p.nx < 2 || p.ny < 2 || p.nz < 2 || p.ncp < 1 || p.tsc < 1 || p.nlvls < 1 || p.hx <= 0 || p.hy <= 0 ||
+        p.hz <= 0 || p.t1 <= 0 || p.objective < 0 || p.objective > 6) {
+        set_error("invalid LinearElasticity parameters");
+        return TOPO_ERR_ARG;
+    }
+    // multigrid divisibility (TopOpt::SetUpMESH, TopOpt.cc:200-219)
+    int div = 1 << (p.nlvls - 1);
+    if ((p.nx - 1) % div || (p.ny - 1) % div || (p.nz - 1) % div) {
+        set_error("mesh dimension not compatible with the number of multigrid levels");
+        return TOPO_ERR_ARG;
+    }
+    TopoLE *le = new TopoLE();
+    le->p = p;
+    le->g = GridDesc{p.nx, p.ny, p.nz, p.nx - 1, p.ny - 1, p.nz - 1};
+    le->nn = le->g.nn();
+    le->nel = le->g.nel();
+    le->ndof = 3 * le->nn;
+    // constructor, LinearElasticity.cc:93-97; SetUpTimeIntegration :185-219
+    le->Ts = p.ncp * p.tsc + 1;
+    le->dt = p.t1 / (le->Ts - 1);
+    double dt = le->dt;
+    if (p.ti == 0) {
+        double a[6] = {0.0, 0.0, 1.0 / dt, 1.0 / dt, 0.0, 1.0 / (dt * dt)};
+        memcpy(le->a, a, sizeof(a));
+    } else {
+        double b = 0.25, gm = 0.5;
+        double a[6] = {1.0 - gm / b, (1.0 - gm / (2.0 * b)) * dt, gm / (b * dt), 1 / (b * dt), 1 / (2.0 * b) - 1.0,
+                       1.0 / (b * dt * dt)};
+        memcpy(le->a, a, sizeof(a));
+    }
+    int rc = le_alloc(le);
+    if (rc) {
+        le_destroy(le);
+        return rc;
+    }
+    *out = le;
+    return TOPO_OK;
+}
+
+int le_alloc(TopoLE *le) {
+    const LEParams &p = le->p;
+    Arena &arena = le->arena;
+    CK(cudaStreamCreateWithFlags(&le->stream, cudaStreamNonBlocking));
+    long long nd = le->ndof, ne = le->nel, nn = le->nn;
+    AG(le->rhs0, nd);
+    AG(le->P, ne);
+    AG(le->xPhys, ne);
+    AG(le->kf, ne);
+    AG(le->dkf, ne);
+    AG(le->mf, ne);
+    AG(le->dmf, ne);
+    AG(le->cntP, nn);
+    AG(le->cp, (size_t)(p.ncp + 1) * 3 * nd);
+    AG(le->Uh, (size_t)p.tsc * nd);
+    AG(le->DUh, (size_t)p.tsc * nd);
+    AG(le->DDUh, (size_t)p.tsc * nd);
+    AG(le->Lp1, nd);
+    AG(le->DLp1, nd);
+    AG(le->DDLp1, nd);
+    AG(le->DLc, nd);
+    AG(le->DDLc, nd);
+    AG(le->KL, nd);
+    AG(le->ML, nd);
+    AG(le->hK, nd);
+    AG(le->hM, nd);
+    AG(le->DDL0, nd);
+    AG(le->df, ne);
+    AG(le->sx, nd);
+    AG(le->sb, nd);
+    AG(le->sr, nd);
+    AG(le->sp, nd);
+    AG(le->sq, nd);
+    AG(le->sz, nd);
+    AG(le->sr32, nd);
+    AG(le->S, 1);
+    AG(le->st, 1);
+    AG(le->part, 4 * 65536);
+    AG(le->counter, 4);
+    AG(le->bbits, 2);
+    AG(le->err, 1);
+
+    // ---- host-side geometry: masks, load location, region (SetUpBC,
+    // LoadLocation, SetUpOptimizationRegion: LinearElasticity.cc:222-675) ----
+    std::vector<uint8_t> fixed(nn, 0);
+    std::vector<double> rhs0(nd, 0.0), P(ne, 0.0);
+    double xc[6] = {0, (p.nx - 1) * p.hx, 0, (p.ny - 1) * p.hy, 0, (p.nz - 1) * p.hz};
+    double epsi = std::fmin(p.hx * 0.05, std::fmin(p.hy * 0.05, p.hz * 0.05));
+    for (int k = 0; k < p.nz; k++)
+        for (int j = 0; j < p.ny; j++)
+            for (int i = 0; i < p.nx; i++) {
+                long long n = i + (long long)p.nx * (j + (long long)p.ny * k);
+                double x = i * p.hx, y = j * p.hy, z = k * p.hz;
+                if (p.boundaries == 0) {
+                    if (std::fabs(x - xc[0]) < epsi) fixed[n] |= 1 | 2;
+                    if (std::fabs(x - xc[1]) < epsi && std::fabs(z - xc[4]) < epsi) fixed[n] |= 2 | 4;
+                } else {
+                    if (std::fabs(x - xc[0]) < epsi) fixed[n] |= 7;
+                }
+                double zl = (p.loadloc == 0) ? xc[5] : xc[5] / 2.0;
+                double xl = (p.loadloc == 0) ? xc[0] : xc[1];
+                if (std::fabs(x - xl) < epsi && std::fabs(z - zl) < epsi) {
+                    rhs0[3 * n + 2] = 1.0;
+                    if (std::fabs(y - xc[2]) < epsi || std::fabs(y - xc[3]) < epsi) rhs0[3 * n + 2] = 0.5;
+                }
+            }
+    for (long long e = 0; e < ne; e++) {
+        int i = (int)(e % le->g.ex), j = (int)((e / le->g.ex) % le->g.ey), k = (int)(e / ((long long)le->g.ex * le->g.ey));
+        double ex = (i + 0.5) * p.hx, ey = (j + 0.5) * p.hy, ez = (k + 0.5) * p.hz, v = 0.0;
+        switch (p.optregion) {
+        case 0: v = (ez > xc[5] - 1 && ex < xc[0] + 1) ? 1.0 : 0.0; break;
+        case 1: v = (ez > xc[5] / 2.0 - 0.5 && ez < xc[5] / 2.0 + 0.5 && ex < xc[1] - 1) ? 1.0 : 0.0; break;
+        case 2: v = 1.0; break;
+        default:
+            v = (ex > 0.75 * xc[1] - 2.5 && ex < 0.75 * xc[1] + 2.5 && ey > 0.5 * xc[3] - 2.5 && ey < 0.5 * xc[3] + 2.5 &&
+                 ez > 0.5 * xc[5] - 2.5 && ez < 0.5 * xc[5] + 2.5)
+                    ? 1.0
+                    : 0.0;
+        }
+        P[e] = v;
+    }
+    {
+        StepCtx sc;
+        memset(&sc, 0, sizeof(sc));
+        sc.tsc = p.tsc;
+        sc.dt = le->dt;
+        CK(cudaMemcpy(le->st, &sc, sizeof(sc), cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpy(le->rhs0, rhs0.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(le->P, P.data(), sizeof(double) * ne, cudaMemcpyHostToDevice));
+    k_count_region<<<ew_blocks(nn), EW, 0, le->stream>>>(le->g, le->P, le->cntP);
+
+    // ---- multigrid levels ----
+    le->nlev = p.nlvls;
+    le->L.resize(le->nlev);
+    for (int l = 0; l < le->nlev; l++) {
+        Level &lv = le->L[l];
+        int f = 1 << l;
+        lv.g = GridDesc{(p.nx - 1) / f + 1, (p.ny - 1) / f + 1, (p.nz - 1) / f + 1, (p.nx - 1) / f, (p.ny - 1) / f,
+                        (p.nz - 1) / f};
+        lv.h[0] = p.hx * f;
+        lv.h[1] = p.hy * f;
+        lv.h[2] = p.hz * f;
+        lv.Cd = make_elem_const<double>(lv.h[0], lv.h[1], lv.h[2], p.nu);
+        lv.Cf = make_elem_const<float>(lv.h[0], lv.h[1], lv.h[2], p.nu);
+        double KE[576], ME[576];
+        box_element_matrices(lv.h[0], lv.h[1], lv.h[2], p.nu, KE, ME);
+        for (int c = 0; c < 3; c++) lv.dK[c] = KE[c * 24 + c];
+        lv.dM = ME[0];
+        lv.lamK = jacobi_scaled_lmax(KE);
+        long long lnn = lv.g.nn(), lnel = lv.g.nel(), lnd = 3 * lnn;
+        AG(lv.fixed, lnn);
+        std::vector<uint8_t> fl(lnn);
+        for (int k = 0; k < lv.g.nz; k++)
+            for (int j = 0; j < lv.g.ny; j++)
+                for (int i = 0; i < lv.g.nx; i++)
+                    fl[i + (long long)lv.g.nx * (j + (long long)lv.g.ny * k)] =
+                        fixed[(i * f) + (long long)p.nx * ((j * f) + (long long)p.ny * (k * f))];
+        CK(cudaMemcpy(lv.fixed, fl.data(), lnn, cudaMemcpyHostToDevice));
+        if (l > 0) {
+            AG(lv.kfd, lnel);
+            AG(lv.mfd, lnel);
+            AG(lv.kff, lnel);
+            AG(lv.mff, lnel);
+        }
+        AG(lv.fb, lnd);
+        AG(lv.fxa, lnd);
+        AG(lv.fxb, lnd);
+        AG(lv.fd, lnd);
+        AG(lv.fr, lnd);
+        AG(lv.db, lnd);
+        AG(lv.dxa, lnd);
+        AG(lv.dxb, lnd);
+        AG(lv.dd, lnd);
+        AG(lv.dr, lnd);
+        if (l == le->nlev - 1) {
+            le->ncoarse = (int)lnd;
+            if (le->ncoarse > 12288) {
+                set_error("coarsest multigrid level too large for the dense solve; increase nlvls");
+                return TOPO_ERR_ARG;
+            }
+            AG(le->KEc, 576);
+            AG(le->MEc, 576);
+            CK(cudaMemcpy(le->KEc, KE, sizeof(KE), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(le->MEc, ME, sizeof(ME), cudaMemcpyHostToDevice));
+            AG(le->Acoarse, (size_t)lnd * lnd);
+            AG(le->gj_row, lnd);
+            AG(le->gj_col, lnd);
+        }
+    }
+    le->L[0].kfd = le->kf;
+    le->L[0].mfd = le->mf;
+    // fine-level float factors
+    AG(le->L[0].kff, ne);
+    AG(le->L[0].mff, ne);
+
+    // operators: effective Newmark matrix K + a5 M + a2 C = (1 + a2 b) K + (a5 + a2 a) M
+    // (the negated A of LinearElasticity.cc:1022-1026), and the mass matrix.
+    le->ops[0].sK = 1.0 + le->a[2] * p.dbeta;
+    le->ops[0].sM = le->a[5] + le->a[2] * p.dalpha;
+    le->ops[1].sK = 0.0;
+    le->ops[1].sM = 1.0;
+    for (int o = 0; o < 2; o++) {
+        Operator &op = le->ops[o];
+        op.lv.resize(le->nlev);
+        for (int l = 0; l < le->nlev; l++) {
+            long long lnd = 3 * le->L[l].g.nn();
+            AG(op.lv[l].dinvd, lnd);
+            AG(op.lv[l].dinvf, lnd);
+            AG(op.lv[l].lohi, 2);
+        }
+        AG(op.Ainv_d, (size_t)le->ncoarse * le->ncoarse);
+        AG(op.Ainv_f, (size_t)le->ncoarse * le->ncoarse);
+    }
+    CK(cudaStreamSynchronize(le->stream));
+    le->stats.device_bytes = (double)arena.bytes;
+    return TOPO_OK;
+}
+
+void le_destroy(TopoLE *le) {
+    if (!le) return;
+    if (le->gx_fwd) cudaGraphExecDestroy(le->gx_fwd);
+    if (le->gx_adj) cudaGraphExecDestroy(le->gx_adj);
+    le->arena.release();
+    if (le->stream) cudaStreamDestroy(le->stream);
+    delete le;
+}
+
+// ---------------------------------------------------------------------------
+// per-design setup of the hierarchy (densities changed)
+// ---------------------------------------------------------------------------
+static int setup_operator(TopoLE *le, int o) {
+    Operator &op = le->ops[o];
+    cudaStream_t s = le->stream;
+    for (int l = 0; l < le->nlev; l++) {
+        Level &lv = le->L[l];
+        const double *kfp = (op.sK != 0.0) ? lv.kfd : nullptr;
+        k_dinv<<<ew_blocks(lv.g.nn()), EW, 0, s>>>(lv.g, lv.fixed, kfp, lv.mfd, op.sK, op.sM, lv.dK[0], lv.dK[1],
+                                                   lv.dK[2], lv.dM, op.lv[l].dinvd, op.lv[l].dinvf);
+        k_bounds_init<<<1, 1, 0, s>>>(le->bbits);
+        k_bounds<<<ew_blocks(lv.g.nel()), EW, 0, s>>>(lv.g.nel(), kfp, lv.mfd, op.sK, op.sM, lv.dK[0], lv.dK[1],
+                                                      lv.dK[2], lv.dM, lv.lamK, 0.125, 3.375, le->bbits);
+        k_bounds_final<<<1, 1, 0, s>>>(le->bbits, le->p.cheb_ratio, op.lv[l].lohi);
+    }
+    // dense coarsest operator and its inverse (FP64 Gauss-Jordan)
+    Level &lc = le->L[le->nlev - 1];
+    int n = le->ncoarse;
+    const double *kfp = (op.sK != 0.0) ? lc.kfd : nullptr;
+    k_coarse_assemble<<<ew_blocks((long long)n * n), EW, 0, s>>>(lc.g, lc.fixed, kfp, lc.mfd, op.sK, op.sM, le->KEc,
+                                                                 le->MEc, op.Ainv_d);
+    for (int k = 0; k < n; k++) {
+        k_gj_save<<<(n + EW - 1) / EW, EW, 0, s>>>(op.Ainv_d, n, k, le->gj_row, le->gj_col);
+        k_gj_update<<<ew_blocks((long long)n * n), EW, 0, s>>>(op.Ainv_d, n, k, le->gj_row, le->gj_col);
+    }
+    k_d2f<<<ew_blocks((long long)n * n), EW, 0, s>>>((long long)n * n, op.Ainv_d, op.Ainv_f);
+    CK(cudaGetLastError());
+    return TOPO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// V-cycle (returns the buffer holding the level solution)
+// ---------------------------------------------------------------------------
+template <class T>
+struct VW {
+    T *b, *xa, *xb, *d, *r;
+    const T *dinv;
+    const T *kf, *mf;
+    const ElemConst<T> *C;
+};
+template <class T>
+static VW<T> vw(TopoLE *le, int o, int l);
+template <>
+VW<float> vw<float>(TopoLE *le, int o, int l) {
+    Level &lv = le->L[l];
+    return VW<float>{lv.fb, lv.fxa, lv.fxb, lv.fd, lv.fr, le->ops[o].lv[l].dinvf, lv.kff, lv.mff, &lv.Cf};
+}
+template <>
+VW<double> vw<double>(TopoLE *le, int o, int l) {
+    Level &lv = le->L[l];
+    return VW<double>{lv.db, lv.dxa, lv.dxb, lv.dd, lv.dr, le->ops[o].lv[l].dinvd, lv.kfd, lv.mfd, &lv.Cd};
+}
+template <class T>
+static const T *ainv(TopoLE *le, int o);
+template <>
+const float *ainv<float>(TopoLE *le, int o) { return le->ops[o].Ainv_f; }
+template <>
+const double *ainv<double>(TopoLE *le, int o) { return le->ops[o].Ainv_d; }
+
+template <class T>
+static T *vcycle(TopoLE *le, int o, int l, const T *b) {
+    cudaStream_t s = le->stream;
+    Level &lv = le->L[l];
+    VW<T> w = vw<T>(le, o, l);
+    Operator &op = le->ops[o];
+    long long nd = 3 * lv.g.nn();
+    if (l == le->nlev - 1) {
+        int n = le->ncoarse;
+        k_gemv<T><<<(n * 32 + 255) / 256, 256, 0, s>>>(n, ainv<T>(le, o), b, w.xa);
+        return w.xa;
+    }
+    Weights<T> wt{op.sK != 0.0 ? w.kf : nullptr, w.mf, nullptr, (T)op.sK, (T)op.sM};
+    const double *lohi = op.lv[l].lohi;
+    const int nu = le->p.smooth;
+    T *x = w.xa, *xo = w.xb;
+    k_cheb0<T><<<ew_blocks(nd), EW, 0, s>>>(nd, b, w.dinv, lohi, x, w.d);
+    for (int k = 1; k < nu; k++) {
+        PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, lohi, k, {}};
+        launch_tile<T>(lv.g, *w.C, pc, s);
+        T *t = x;
+        x = xo;
+        xo = t;
+    }
+    PolResid<T> pr{lv.fixed, wt, x, b, w.r, {}};
+    launch_tile<T>(lv.g, *w.C, pr, s);
+    Level &lc = le->L[l + 1];
+    VW<T> wc = vw<T>(le, o, l + 1);
+    k_restrict<T><<<ew_blocks(lc.g.nn()), EW, 0, s>>>(lv.g, lc.g, lc.fixed, w.r, wc.b);
+    T *xc = vcycle<T>(le, o, l + 1, wc.b);
+    k_prolong<T><<<ew_blocks(lv.g.nn()), EW, 0, s>>>(lv.g, lc.g, lv.fixed, xc, x);
+    for (int k = 0; k < nu; k++) {
+        PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, lohi, k, {}};
+        launch_tile<T>(lv.g, *w.C, pc, s);
+        T *t = x;
+        x = xo;
+        xo = t;
+    }
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// flexible CG:  (N A N + I - N) x = b for operator o; sx holds the initial guess
+// ---------------------------------------------------------------------------
+__global__ void k_solve_prime(SolveScalars *S, double tol2, int maxit) {
+    S->tol2 = tol2;
+    S->maxit = maxit;
+    S->done = 0;
+    S->status = 0;
+    S->it = 0;
+}
+__global__ void k_solve_check(const SolveScalars *S, int *err) {
+    if (S->status != 0 && *err == 0) *err = S->status;
+}
+
+static void solve_init(TopoLE *le, int o, const double *b, cudaGraphConditionalHandle cond, int has_cond) {
+    Level &l0 = le->L[0];
+    Operator &op = le->ops[o];
+    Weights<double> wt{op.sK != 0.0 ? l0.kfd : nullptr, l0.mfd, nullptr, op.sK, op.sM};
+    PolInitResid<double> pi{l0.fixed, wt, le->sx, b, le->sr, le->p.mixed ? le->sr32 : nullptr,
+                            le->S, cond, has_cond, P2(le)};
+    launch_tile<double>(l0.g, l0.Cd, pi, le->stream);
+}
+
+static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, int has_cond) {
+    cudaStream_t s = le->stream;
+    Level &l0 = le->L[0];
+    Operator &op = le->ops[o];
+    long long nd = le->ndof;
+    unsigned nb = ew_blocks(nd);
+    if (le->p.mixed) {
+        float *z = vcycle<float>(le, o, 0, le->sr32);
+        k_fcg_dot<float><<<nb, EW, 0, s>>>(nd, z, le->sr, le->sq, le->S, P2(le));
+        k_fcg_p<float><<<nb, EW, 0, s>>>(nd, z, le->sp, le->S);
+    } else {
+        double *z = vcycle<double>(le, o, 0, le->sr);
+        k_fcg_dot<double><<<nb, EW, 0, s>>>(nd, z, le->sr, le->sq, le->S, P2(le));
+        k_fcg_p<double><<<nb, EW, 0, s>>>(nd, z, le->sp, le->S);
+    }
+    Weights<double> wt{op.sK != 0.0 ? l0.kfd : nullptr, l0.mfd, nullptr, op.sK, op.sM};
+    PolPQ<double> pq{l0.fixed, wt, le->sp, le->sq, le->S, P1(le)};
+    launch_tile<double>(l0.g, l0.Cd, pq, s);
+    k_fcg_update<<<nb, EW, 0, s>>>(nd, le->sx, le->sr, le->p.mixed ? le->sr32 : nullptr, le->sp, le->sq, le->S,
+                                   P1(le), cond, has_cond);
+}
+
+// direct launches, host checks convergence after every iteration
+static int solve_direct(TopoLE *le, int o, const double *b) {
+    k_solve_prime<<<1, 1, 0, le->stream>>>(le->S, le->p.rtol * le->p.rtol, le->p.maxit);
+    solve_init(le, o, b, 0, 0);
+    SolveScalars h;
+    for (;;) {
+        CK(cudaMemcpyAsync(&h, le->S, sizeof(h), cudaMemcpyDeviceToHost, le->stream));
+        CK(cudaStreamSynchronize(le->stream));
+        if (h.done) break;
+        solve_iteration(le, o, 0, 0);
+    }
+    k_fcg_zero_x<<<ew_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, le->sx, le->S);
+    k_solve_check<<<1, 1, 0, le->stream>>>(le->S, le->err);
+    le->nsolves++;
+    CK(cudaGetLastError());
+    return TOPO_OK;
+}
+
+// inside stream capture: the FCG loop becomes a conditional WHILE node whose
+// body is the iteration; the device sets the condition after each iteration
+static int solve_captured(TopoLE *le, int o, const double *b) {
+    cudaStream_t s = le->stream;
+    k_solve_prime<<<1, 1, 0, s>>>(le->S, le->p.rtol * le->p.rtol, le->p.maxit);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t graph;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edata = nullptr;
+    size_t ndeps = 0;
+    CK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, &edata, &ndeps));
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
+    solve_init(le, o, b, h, 1);
+    CK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, &edata, &ndeps));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    CK(cudaGraphAddNode(&cnode, graph, deps, edata, ndeps, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CK(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaStream_t bs;
+    CK(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    le->stream = bs;
+    solve_iteration(le, o, h, 1);
+    le->stream = s;
+    cudaGraph_t outg;
+    cudaError_t e1 = cudaStreamEndCapture(bs, &outg);
+    cudaStreamDestroy(bs);
+    CK(e1);
+    k_fcg_zero_x<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->S);
+    k_solve_check<<<1, 1, 0, s>>>(le->S, le->err);
+    return TOPO_OK;
+}
+
+static int solve(TopoLE *le, int o, const double *b, bool capturing) {
+    return capturing ? solve_captured(le, o, b) : solve_direct(le, o, b);
+}
+
+// ---------------------------------------------------------------------------
+// forward step j of block c (SolveStateBlock, LinearElasticity.cc:1317-1385)
+// ---------------------------------------------------------------------------
+static void fwd_rhs(TopoLE *le) {
+    const LEParams &p = le->p;
+    Level &l0 = le->L[0];
+    const double *a = le->a;
+    PolRhsFwd pr;
+    memset(&pr, 0, sizeof(pr));
+    pr.fixed = l0.fixed;
+    pr.w = Weights<double>{le->kf, le->mf, nullptr, 1.0, 1.0};
+    pr.cp = le->cp;
+    pr.Uh = le->Uh;
+    pr.DUh = le->DUh;
+    pr.DDUh = le->DDUh;
+    pr.ndof = le->ndof;
+    pr.rhs0 = le->rhs0;
+    pr.load_scale = 1.0 / (p.ny - 1);
+    pr.loadsignal = p.loadsignal;
+    // B1 u- + B2 du- + B3 ddu- = M (cM . s-) + K (cK . s-)  (LinearElasticity.cc:1028-1044)
+    pr.cM[0] = a[5] + a[2] * p.dalpha;
+    pr.cM[1] = a[3] - a[0] * p.dalpha;
+    pr.cM[2] = a[4] - a[1] * p.dalpha;
+    pr.cK[0] = a[2] * p.dbeta;
+    pr.cK[1] = -a[0] * p.dbeta;
+    pr.cK[2] = -a[1] * p.dbeta;
+    // Newmark predictor u- + dt du- + (1/2 - 1/4) dt^2 ddu- as initial guess
+    double dt = le->dt;
+    pr.pred[0] = 1.0;
+    pr.pred[1] = (p.ti == 0) ? 0.0 : dt;
+    pr.pred[2] = (p.ti == 0) ? 0.0 : 0.25 * dt * dt;
+    pr.st = le->st;
+    pr.b = le->sb;
+    pr.x0 = le->sx;
+    launch_tile<double>(l0.g, l0.Cd, pr, le->stream);
+}
+
+static int fwd_step(TopoLE *le, bool capturing) {
+    cudaStream_t s = le->stream;
+    fwd_rhs(le);
+    int rc = solve(le, 0, le->sb, capturing);
+    if (rc) return rc;
+    Newmark nm;
+    memcpy(nm.a, le->a, sizeof(nm.a));
+    k_newmark<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh, le->DUh, le->DDUh, nm);
+    k_step_add<<<1, 1, 0, s>>>(le->st, +1);
+    return TOPO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// adjoint step j (SolveLagrangen body) and the t = 0 pass (SolveLagrange0)
+// ---------------------------------------------------------------------------
+template <bool HK, bool HM>
+static void product(TopoLE *le, const double *x, double *y, const double *P, double sK, double sM) {
+    Level &l0 = le->L[0];
+    PolProduct<double, HK, HM> pp{Weights<double>{HK ? le->kf : nullptr, HM ? le->mf : nullptr, P, sK, sM}, x, y, {}};
+    launch_tile<double>(l0.g, l0.Cd, pp, le->stream);
+}
+
+// objective gradient products h (objectives 3-6) of the state `state_base`
+// (U/DU base pointers resolved by the step index, or the t = 0 state)
+__global__ void k_select_state(long long ndof, const StepCtx *st, const double *Uh, const double *DUh, int t0mode,
+                               const double *cp, double *outU, double *outDU) {
+    const double *u, *du;
+    if (t0mode) {
+        u = cp;
+        du = cp + ndof;
+    } else {
+        u = Uh + (long long)st->j * ndof;
+        du = DUh + (long long)st->j * ndof;
+    }
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        if (outU) outU[i] = u[i];
+        if (outDU) outDU[i] = du[i];
+    }
+}
+
+static void objective_products(TopoLE *le, int t0mode) {
+    int obj = le->p.objective;
+    if (obj < 3) return;
+    double dt = le->dt;
+    // stage the needed state vectors into the solver scratch (sp, sq are free here)
+    bool needU = (obj == 3 || obj == 5), needDU = (obj >= 4);
+    k_select_state<<<ew_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, le->st, le->Uh, le->DUh, t0mode, le->cp,
+                                                                 needU ? le->sp : nullptr, needDU ? le->sq : nullptr);
+    if (obj == 3) product<true, false>(le, le->sp, le->hK, le->P, dt, 0.0);
+    if (obj == 4) product<false, true>(le, le->sq, le->hM, le->P, 0.0, dt);
+    if (obj == 5) {
+        product<true, false>(le, le->sp, le->hK, le->P, dt, 0.0);
+        product<false, true>(le, le->sq, le->hM, le->P, 0.0, dt);
+    }
+    if (obj == 6) product<true, true>(le, le->sq, le->hK, le->P, dt * le->p.dbeta, dt * le->p.dalpha);
+}
+
+static AdjCombine adj_args(TopoLE *le, int t0mode) {
+    const LEParams &p = le->p;
+    const double *a = le->a;
+    AdjCombine A;
+    memset(&A, 0, sizeof(A));
+    A.fixed = le->L[0].fixed;
+    A.KL = le->KL;
+    A.ML = le->ML;
+    A.Lp1 = le->Lp1;
+    A.DLp1 = le->DLp1;
+    A.DDLp1 = le->DDLp1;
+    A.hK = le->hK;
+    A.hM = le->hM;
+    A.cntP = le->cntP;
+    A.Ustate = le->Uh;
+    A.DUstate = le->DUh;
+    A.DDUstate = le->DDUh;
+    A.cp = le->cp;
+    A.ndof = le->ndof;
+    A.objective = p.objective;
+    A.t0mode = t0mode;
+    A.dt = le->dt;
+    memcpy(A.a, a, sizeof(A.a));
+    A.cM[0] = a[5] + a[2] * p.dalpha;
+    A.cM[1] = a[3] - a[0] * p.dalpha;
+    A.cM[2] = a[4] - a[1] * p.dalpha;
+    A.cK[0] = a[2] * p.dbeta;
+    A.cK[1] = -a[0] * p.dbeta;
+    A.cK[2] = -a[1] * p.dbeta;
+    A.st = le->st;
+    A.DL = le->DLc;
+    A.DDL = le->DDLc;
+    A.b = le->sb;
+    A.x0 = le->sx;
+    return A;
+}
+
+static SensArgs sens_args(TopoLE *le, int t0mode) {
+    const LEParams &p = le->p;
+    const double *a = le->a;
+    SensArgs S;
+    memset(&S, 0, sizeof(S));
+    S.g = le->g;
+    S.lam = le->sx;
+    S.Uh = le->Uh;
+    S.DUh = le->DUh;
+    S.DDUh = le->DDUh;
+    S.cp = le->cp;
+    S.kf = le->kf;
+    S.dkf = le->dkf;
+    S.mf = le->mf;
+    S.dmf = le->dmf;
+    S.P = le->P;
+    double al = p.dalpha, be = p.dbeta;
+    if (t0mode) {
+        // DDL0' (dK u0 + dC du0 + dM ddu0), dC = alpha dM + beta dK (LinearElasticity.cc:2154-2162)
+        S.aK[0] = 1.0;
+        S.aK[1] = be;
+        S.aK[2] = 0.0;
+        S.aM[0] = 0.0;
+        S.aM[1] = al;
+        S.aM[2] = 1.0;
+    } else {
+        // lambda' (dA/dx u + dB1/dx u- + dB2/dx du- + dB3/dx ddu-) (LinearElasticity.cc:1996-2016)
+        S.aK[0] = -(1.0 + a[2] * be);
+        S.bK[0] = a[2] * be;
+        S.bK[1] = -a[0] * be;
+        S.bK[2] = -a[1] * be;
+        S.aM[0] = -(a[5] + a[2] * al);
+        S.bM[0] = a[5] + a[2] * al;
+        S.bM[1] = a[3] - a[0] * al;
+        S.bM[2] = a[4] - a[1] * al;
+    }
+    S.dt = le->dt;
+    S.dalpha = al;
+    S.dbeta = be;
+    S.t0mode = t0mode;
+    S.with_objective = 1;
+    S.st = le->st;
+    S.df = le->df;
+    S.fx = &le->st->fx;
+    S.part = P1(le);
+    return S;
+}
+
+template <int OBJ>
+static void launch_sens_obj(TopoLE *le, const SensArgs &S) {
+    k_sens<OBJ, double><<<ew_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cd);
+}
+static void launch_sens(TopoLE *le, int t0mode) {
+    SensArgs S = sens_args(le, t0mode);
+    switch (le->p.objective) {
+    case 0: launch_sens_obj<0>(le, S); break;
+    case 1: launch_sens_obj<1>(le, S); break;
+    case 2: launch_sens_obj<2>(le, S); break;
+    case 3: launch_sens_obj<3>(le, S); break;
+    case 4: launch_sens_obj<4>(le, S); break;
+    case 5: launch_sens_obj<5>(le, S); break;
+    default: launch_sens_obj<6>(le, S); break;
+    }
+}
+
+static int adj_step(TopoLE *le, bool capturing) {
+    cudaStream_t s = le->stream;
+    // K L+ and M L+ (the B1..B3 products of LinearElasticity.cc:897-899)
+    product<true, false>(le, le->Lp1, le->KL, nullptr, 1.0, 0.0);
+    product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
+    objective_products(le, 0);
+    k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 0));
+    int rc = solve(le, 0, le->sb, capturing);
+    if (rc) return rc;
+    launch_sens(le, 0);
+    k_adj_advance<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->DLc, le->DDLc, le->Lp1, le->DLp1, le->DDLp1);
+    k_step_add<<<1, 1, 0, s>>>(le->st, -1);
+    return TOPO_OK;
+}
+
+static int lagrange0(TopoLE *le) {
+    cudaStream_t s = le->stream;
+    product<true, false>(le, le->Lp1, le->KL, nullptr, 1.0, 0.0);
+    product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
+    objective_products(le, 1);
+    k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 1));
+    int rc = solve(le, 1, le->sb, false);
+    if (rc) return rc;
+    launch_sens(le, 1);
+    k_copy<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->DDL0);
+    return TOPO_OK;
+}
+
+// graph of one step, captured on first use and replayed for every step
+static int get_graph(TopoLE *le, int adjoint, cudaGraphExec_t *out) {
+    cudaGraphExec_t &gx = adjoint ? le->gx_adj : le->gx_fwd;
+    if (!gx) {
+        CK(cudaStreamBeginCapture(le->stream, cudaStreamCaptureModeRelaxed));
+        int rc = adjoint ? adj_step(le, true) : fwd_step(le, true);
+        cudaGraph_t g;
+        cudaError_t e = cudaStreamEndCapture(le->stream, &g);
+        if (rc) return rc;
+        CK(e);
+        cudaError_t e2 = cudaGraphInstantiate(&gx, g, 0);
+        cudaGraphDestroy(g);
+        CK(e2);
+    }
+    *out = gx;
+    return TOPO_OK;
+}
+
+static int run_block(TopoLE *le, int c, int adjoint) {
+    const int tsc = le->p.tsc;
+    k_step_set<<<1, 1, 0, le->stream>>>(le->st, c, adjoint ? tsc - 1 : 0);
+    if (le->p.use_graphs) {
+        cudaGraphExec_t gx;
+        int rc = get_graph(le, adjoint, &gx);
+        if (rc) return rc;
+        for (int j = 0; j < tsc; j++) CK(cudaGraphLaunch(gx, le->stream));
+        le->nsolves += tsc;
+    } else {
+        for (int j = 0; j < tsc; j++) {
+            int rc = adjoint ? adj_step(le, false) : fwd_step(le, false);
+            if (rc) return rc;
+        }
+    }
+    CK(cudaGetLastError());
+    return TOPO_OK;
+}
+
+static int check_err(TopoLE *le) {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, le->err, sizeof(int), cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaStreamSynchronize(le->stream));
+    if (h) {
+        set_error(std::string("linear solve failed with status ") + std::to_string(h));
+        int z = 0;
+        cudaMemcpy(le->err, &z, sizeof(int), cudaMemcpyHostToDevice);
+        return h;
+    }
+    return TOPO_OK;
+}
+
+__global__ void k_init_accel_rhs(long long nn, const uint8_t *fixed, const double *rhs0, double s, const double *Ku,
+                                 const double *Cdu, double *b) {
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+        uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) {
+            long long i = 3 * n + c;
+            b[i] = ((f >> c) & 1) ? 0.0 : (rhs0[i] * s - Cdu[i] - Ku[i]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// public operations
+// ---------------------------------------------------------------------------
+int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, double Emax, double Rmin, double Rmax,
+                              double penalK, double penalM) {
+    cudaStream_t s = le->stream;
+    const LEParams &p = le->p;
+    CK(cudaMemcpyAsync(le->xPhys, xPhys_dev, sizeof(double) * le->nel, cudaMemcpyDeviceToDevice, s));
+    MatParams mp{p.sInt, p.mInt, Emin, Emax, penalK, Rmin, Rmax, penalM};
+    k_interp<<<ew_blocks(le->nel), EW, 0, s>>>(le->nel, le->xPhys, mp, le->kf, le->dkf, le->mf, le->dmf, le->L[0].kff,
+                                               le->L[0].mff);
+    for (int l = 1; l < le->nlev; l++)
+        k_coarsen<<<ew_blocks(le->L[l].g.nel()), EW, 0, s>>>(le->L[l - 1].g, le->L[l].g, le->L[l - 1].kfd,
+                                                             le->L[l - 1].mfd, le->L[l].kfd, le->L[l].mfd,
+                                                             le->L[l].kff, le->L[l].mff);
+    int rc = setup_operator(le, 0);
+    if (rc) return rc;
+    rc = setup_operator(le, 1);
+    if (rc) return rc;
+    // initial acceleration: (N M N + I - N) ddu0 = N (f(0) - C du0 - K u0)
+    // (LinearElasticity.cc:1046-1078); u0 = du0 = 0 (LinearElasticity.cc:521-587)
+    long long nd = le->ndof;
+    CK(cudaMemsetAsync(le->cp, 0, sizeof(double) * 3 * nd, s));
+    product<true, false>(le, le->cp, le->KL, nullptr, 1.0, 0.0);
+    product<true, true>(le, le->cp + nd, le->ML, nullptr, p.dbeta, p.dalpha);
+    double s0 = 0.0;
+    {
+        // host evaluation of the load signal at t = 0 (same formula as the device)
+        if (p.loadsignal == 1)
+            s0 = 0.0;
+        else {
+            double t = 0.0 - 8.0, c = 1.1;
+            s0 = exp(-(t * t) / ((2 * c) * (2 * c))) * cos(4.0 * t) * cos(5.0 * t) * cos(6.0 * t) * cos(7.0 * t);
+        }
+        s0 /= (p.ny - 1);
+    }
+    k_init_accel_rhs<<<ew_blocks(le->nn), EW, 0, s>>>(le->nn, le->L[0].fixed, le->rhs0, s0, le->KL, le->ML, le->sb);
+    CK(cudaMemsetAsync(le->sx, 0, sizeof(double) * nd, s));
+    rc = solve(le, 1, le->sb, false);
+    if (rc) return rc;
+    k_copy<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sx, le->cp + 2 * nd);
+    rc = check_err(le);
+    if (rc) return rc;
+    le->design_ready = 1;
+    le->last_block_resident = -1;
+    return TOPO_OK;
+}
+
+int le_generate_checkpoints(TopoLE *le) {
+    if (!le->design_ready) {
+        set_error("GenerateCheckPoints called before CompleteInitialState");
+        return TOPO_ERR_STATE;
+    }
+    if (le->p.ncp <= 1) return TOPO_OK;
+    long long nd = le->ndof;
+    int tsc = le->p.tsc;
+    for (int c = 0; c < le->p.ncp; c++) {
+        int rc = run_block(le, c, 0);
+        if (rc) return rc;
+        double *dst = le->cp + (size_t)(c + 1) * 3 * nd;
+        CK(cudaMemcpyAsync(dst, le->Uh + (size_t)(tsc - 1) * nd, sizeof(double) * nd, cudaMemcpyDeviceToDevice, le->stream));
+        CK(cudaMemcpyAsync(dst + nd, le->DUh + (size_t)(tsc - 1) * nd, sizeof(double) * nd, cudaMemcpyDeviceToDevice,
+                           le->stream));
+        CK(cudaMemcpyAsync(dst + 2 * nd, le->DDUh + (size_t)(tsc - 1) * nd, sizeof(double) * nd,
+                           cudaMemcpyDeviceToDevice, le->stream));
+    }
+    le->last_block_resident = le->p.ncp - 1;
+    return check_err(le);
+}
+
+int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev) {
+    if (!le->design_ready) {
+        set_error("ComputeObjectiveSensitivities called before CompleteInitialState");
+        return TOPO_ERR_STATE;
+    }
+    cudaStream_t s = le->stream;
+    long long nd = le->ndof;
+    CK(cudaMemsetAsync(le->df, 0, sizeof(double) * le->nel, s));
+    CK(cudaMemsetAsync(le->Lp1, 0, sizeof(double) * nd, s));
+    CK(cudaMemsetAsync(le->DLp1, 0, sizeof(double) * nd, s));
+    CK(cudaMemsetAsync(le->DDLp1, 0, sizeof(double) * nd, s));
+    CK(cudaMemsetAsync(&le->st->fx, 0, sizeof(double), s));
+    for (int c = le->p.ncp - 1; c >= 0; c--) {
+        if (le->last_block_resident != c) {
+            int rc = run_block(le, c, 0);
+            if (rc) return rc;
+            le->last_block_resident = c;
+        }
+        int rc = run_block(le, c, 1);
+        if (rc) return rc;
+        if (c == 0) {
+            rc = lagrange0(le);
+            if (rc) return rc;
+        }
+    }
+    if (dfdx_dev) CK(cudaMemcpyAsync(dfdx_dev, le->df, sizeof(double) * le->nel, cudaMemcpyDeviceToDevice, s));
+    double h = 0.0;
+    CK(cudaMemcpyAsync(&h, &le->st->fx, sizeof(double), cudaMemcpyDeviceToHost, s));
+    int rc = check_err(le);
+    if (rc) return rc;
+    *fx = h;
+    le->stats.last_fx = h;
+    return TOPO_OK;
+}
+
+int le_get_state(TopoLE *le, int which, int j, double *out) {
+    if (which < 0 || which > 2 || j < -1 || j >= le->p.tsc) return TOPO_ERR_ARG;
+    long long nd = le->ndof;
+    const double *src;
+    if (j < 0) {
+        int blk = le->last_block_resident < 0 ? 0 : le->last_block_resident;
+        src = le->cp + (size_t)blk * 3 * nd + which * nd;
+    } else {
+        const double *base = which == 0 ? le->Uh : (which == 1 ? le->DUh : le->DDUh);
+        src = base + (size_t)j * nd;
+    }
+    CK(cudaMemcpyAsync(out, src, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaStreamSynchronize(le->stream));
+    return TOPO_OK;
+}
+
+int le_apply_km(TopoLE *le, const double *x_dev, double *Kx_dev, double *Mx_dev) {
+    product<true, false>(le, x_dev, Kx_dev, nullptr, 1.0, 0.0);
+    product<false, true>(le, x_dev, Mx_dev, nullptr, 0.0, 1.0);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(le->stream));
+    return TOPO_OK;
+}
+
+int le_stats(TopoLE *le, LEStats *out) {
+    SolveScalars h;
+    CK(cudaMemcpyAsync(&h, le->S, sizeof(h), cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaStreamSynchronize(le->stream));
+    le->stats.cg_iterations = h.total_it;
+    le->stats.solves = le->nsolves;
+    *out = le->stats;
+    return TOPO_OK;
+}
+
+long long le_nel(const TopoLE *le) { return le->nel; }
+long long le_ndof(const TopoLE *le) { return le->ndof; }
+void *le_stream(TopoLE *le) { return (void *)le->stream; }
+
+}  // namespace topo
+
+namespace topo {
+// event-timed operator apply (roofline measurement hook)
+__global__ void k_fill(long long n, double *x, double v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = v * (double)((i * 2654435761ull) % 1000) * 1e-3;
+}
+int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms) {
+    if (!le->design_ready) {
+        set_error("time_apply needs CompleteInitialState first");
+        return TOPO_ERR_STATE;
+    }
+    cudaStream_t s = le->stream;
+    Level &l0 = le->L[0];
+    Operator &op = le->ops[0];
+    long long nd = le->ndof;
+    k_fill<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sp, 1.0);
+    k_d2f<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sp, l0.fr);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto one = [&]() {
+        if (precision == 0) {
+            Weights<double> wt{l0.kfd, l0.mfd, nullptr, op.sK, op.sM};
+            PolResid<double> pr{l0.fixed, wt, le->sp, le->sb, le->sq, {}};
+            launch_tile<double>(l0.g, l0.Cd, pr, s);
+        } else {
+            Weights<float> wt{l0.kff, l0.mff, nullptr, (float)op.sK, (float)op.sM};
+            PolResid<float> pr{l0.fixed, wt, l0.fr, l0.fb, l0.fd, {}};
+            launch_tile<float>(l0.g, l0.Cf, pr, s);
+        }
+    };
+    for (int i = 0; i < warmup; i++) one();
+    CK(cudaEventRecord(e0, s));
+    for (int i = 0; i < reps; i++) one();
+    CK(cudaEventRecord(e1, s));
+    CK(cudaEventSynchronize(e1));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = (double)t / reps;
+    return TOPO_OK;
+}
+}  // namespace topo

@@ -1,0 +1,325 @@
+// policies.cuh -- fused epilogues for the matrix-free tile kernel (tile.cuh).
+//
+// Masking convention: the Dirichlet vector N of the reference
+// (LinearElasticity.cc:552-574) is stored as a per-node bitmask `fixed`
+// (bit c set <=> DOF 3n+c is clamped).  Every system operator is the
+// reference's  N A N + (I - N)  (MatDiagonalScale + MatDiagonalSet,
+// LinearElasticity.cc:1118-1122), applied as: zero clamped inputs, apply the
+// element operator, zero clamped outputs, add the identity on clamped DOFs.
+#pragma once
+#include "tile.cuh"
+
+namespace topo {
+
+template <class T>
+__device__ __forceinline__ void mask3(uint8_t f, T v[3]) {
+    if (f & 1) v[0] = T(0);
+    if (f & 2) v[1] = T(0);
+    if (f & 4) v[2] = T(0);
+}
+
+// scalars of one Krylov solve, resident in device memory
+struct SolveScalars {
+    double bb, rr, rho, rho_old, alpha, beta, pq, gam;
+    double tol2;      // rtol^2
+    int it, maxit;
+    int status;       // 0 running/converged, TOPO_ERR_* on failure
+    int done;         // 1 once converged / failed: later body kernels return
+    int zero_x;       // rhs was exactly zero: solution is zero
+    int total_it;     // accumulated iterations over all solves (diagnostics)
+};
+
+// ---------------------------------------------------------------------------
+// element weights: ck = sK * kf[e] (* P[e]), cm = sM * mf[e] (* P[e])
+// ---------------------------------------------------------------------------
+template <class T>
+struct Weights {
+    const T *kf, *mf;  // per-element density factors (may be null when s == 0)
+    const double *P;   // optional region mask
+    T sK, sM;
+    __device__ __forceinline__ void get(long long e, T &ck, T &cm) const {
+        T w = P ? (T)P[e] : T(1);
+        ck = kf ? sK * kf[e] * w : T(0);
+        cm = mf ? sM * mf[e] * w : T(0);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// FCG initial residual: r = b - (N A N + I - N) x0, reductions b.b and r.r
+// ---------------------------------------------------------------------------
+template <class T>
+struct PolInitResid {
+    static constexpr int NIN = 1, NRED = 2;
+    static constexpr bool HAS_K = true, HAS_M = true;
+    const uint8_t *fixed;
+    Weights<T> w;
+    const T *x, *b;
+    T *r;
+    float *r32;  // optional FP32 copy for the mixed-precision preconditioner
+    SolveScalars *S;
+    cudaGraphConditionalHandle cond;
+    int has_cond;
+    Partials<2> part;
+    __device__ void load(long long n, T v[1][3]) const {
+        v[0][0] = x[3 * n];
+        v[0][1] = x[3 * n + 1];
+        v[0][2] = x[3 * n + 2];
+        mask3(fixed[n], v[0]);
+    }
+    __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const T y[3], double red[2]) const {
+        uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) {
+            T xv = x[3 * n + c], bv = b[3 * n + c];
+            T ax = ((f >> c) & 1) ? xv : y[c];
+            T rv = bv - ax;
+            r[3 * n + c] = rv;
+            if (r32) r32[3 * n + c] = (float)rv;
+            red[0] += (double)bv * (double)bv;
+            red[1] += (double)rv * (double)rv;
+        }
+    }
+    __device__ void finish(const double t[2]) const {
+        S->bb = t[0];
+        S->rr = t[1];
+        S->it = 0;
+        S->status = 0;
+        S->zero_x = (t[0] == 0.0);
+        S->done = (t[0] == 0.0) || (t[1] <= S->tol2 * t[0]);
+        if (!isfinite(t[1])) {
+            S->status = TOPO_ERR_NAN;
+            S->done = 1;
+        }
+        if (has_cond) cudaGraphSetConditional(cond, S->done ? 0u : 1u);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// FCG operator product: q = (N A N + I - N) p, reduction p.q -> alpha
+// ---------------------------------------------------------------------------
+template <class T>
+struct PolPQ {
+    static constexpr int NIN = 1, NRED = 1;
+    static constexpr bool HAS_K = true, HAS_M = true;
+    const uint8_t *fixed;
+    Weights<T> w;
+    const T *p;
+    T *q;
+    SolveScalars *S;
+    Partials<1> part;
+    __device__ void load(long long n, T v[1][3]) const {
+        v[0][0] = p[3 * n];
+        v[0][1] = p[3 * n + 1];
+        v[0][2] = p[3 * n + 2];
+        mask3(fixed[n], v[0]);
+    }
+    __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const T y[3], double red[1]) const {
+        uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) {
+            T pv = p[3 * n + c];
+            T qv = ((f >> c) & 1) ? pv : y[c];
+            q[3 * n + c] = qv;
+            red[0] += (double)pv * (double)qv;
+        }
+    }
+    __device__ void finish(const double t[1]) const {
+        S->pq = t[0];
+        if (!(t[0] > 0.0) || !isfinite(t[0])) {
+            S->status = isfinite(t[0]) ? TOPO_ERR_BREAKDOWN : TOPO_ERR_NAN;
+            S->alpha = 0.0;
+            S->done = 1;
+        } else {
+            S->alpha = S->rho / t[0];
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Chebyshev-Jacobi smoothing step (one operator application):
+//   r = b - (N A N + I - N) x_in ;  d = c1 d + c2 Dinv r ;  x_out = x_in + d
+// Coefficients from the device-resident spectrum bounds [lo, hi] of Dinv A.
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void cheb_coeffs(const double *lohi, int k, T &c1, T &c2) {
+    double lo = lohi[0], hi = lohi[1];
+    double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    if (k == 0) {
+        c1 = T(0);
+        c2 = (T)(1.0 / theta);
+        return;
+    }
+    double rho_prev = 1.0 / sigma, rho = rho_prev;
+    for (int i = 1; i <= k; i++) {
+        rho_prev = rho;
+        rho = 1.0 / (2.0 * sigma - rho_prev);
+    }
+    c1 = (T)(rho * rho_prev);
+    c2 = (T)(2.0 * rho / delta);
+}
+
+template <class T>
+struct PolCheb {
+    static constexpr int NIN = 1, NRED = 0;
+    static constexpr bool HAS_K = true, HAS_M = true;
+    const uint8_t *fixed;
+    Weights<T> w;
+    const T *x_in, *b, *dinv;
+    T *x_out, *d;
+    const double *lohi;
+    int k;
+    Partials<1> part;
+    __device__ void load(long long n, T v[1][3]) const {
+        v[0][0] = x_in[3 * n];
+        v[0][1] = x_in[3 * n + 1];
+        v[0][2] = x_in[3 * n + 2];
+        mask3(fixed[n], v[0]);
+    }
+    __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const T y[3], double *) const {
+        T c1, c2;
+        cheb_coeffs<T>(lohi, k, c1, c2);
+        uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) {
+            T xv = x_in[3 * n + c];
+            T rv = b[3 * n + c] - (((f >> c) & 1) ? xv : y[c]);
+            T dv = (k == 0 ? T(0) : c1 * d[3 * n + c]) + c2 * dinv[3 * n + c] * rv;
+            d[3 * n + c] = dv;
+            x_out[3 * n + c] = xv + dv;
+        }
+    }
+    __device__ void finish(const double *) const {}
+};
+
+// residual only: r = b - (N A N + I - N) x   (before restriction)
+template <class T>
+struct PolResid {
+    static constexpr int NIN = 1, NRED = 0;
+    static constexpr bool HAS_K = true, HAS_M = true;
+    const uint8_t *fixed;
+    Weights<T> w;
+    const T *x, *b;
+    T *r;
+    Partials<1> part;
+    __device__ void load(long long n, T v[1][3]) const {
+        v[0][0] = x[3 * n];
+        v[0][1] = x[3 * n + 1];
+        v[0][2] = x[3 * n + 2];
+        mask3(fixed[n], v[0]);
+    }
+    __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const T y[3], double *) const {
+        uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) {
+            T xv = x[3 * n + c];
+            r[3 * n + c] = b[3 * n + c] - (((f >> c) & 1) ? xv : y[c]);
+        }
+    }
+    __device__ void finish(const double *) const {}
+};
+
+// plain weighted product y = sum_e (ck KE + cm ME) x_e, no masking
+template <class T, bool HK, bool HM>
+struct PolProduct {
+    static constexpr int NIN = 1, NRED = 0;
+    static constexpr bool HAS_K = HK, HAS_M = HM;
+    Weights<T> w;
+    const T *x;
+    T *y;
+    Partials<1> part;
+    __device__ void load(long long n, T v[1][3]) const {
+        v[0][0] = x[3 * n];
+        v[0][1] = x[3 * n + 1];
+        v[0][2] = x[3 * n + 2];
+    }
+    __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const T yv[3], double *) const {
+        y[3 * n] = yv[0];
+        y[3 * n + 1] = yv[1];
+        y[3 * n + 2] = yv[2];
+    }
+    __device__ void finish(const double *) const {}
+};
+
+// ---------------------------------------------------------------------------
+// Newmark right-hand side of one forward step (SolveStateBlock,
+// LinearElasticity.cc:1330-1356):
+//   b = N (f(t) + B1 u- + B2 du- + B3 ddu-),  B_i = N (cMi M + cKi K) N
+// staged as vK = sum cKi (u-,du-,ddu-)_i and vM = sum cMi (...)_i so that one
+// element pass gives K vK + M vM.  Also writes the Newmark predictor
+// u- + dt du- + (1/2 - beta) dt^2 ddu- as the Krylov initial guess.
+// ---------------------------------------------------------------------------
+struct StepCtx {   // device-resident time-stepping state
+    int block;     // checkpoint block c
+    int j;         // step within block
+    int tsc;
+    int pad;
+    double dt;
+    double fx;     // objective accumulator
+};
+
+__device__ __forceinline__ double load_signal(int which, double t) {
+    if (which == 1) return (t < 0.5) ? sin(2.0 * 3.14159265358979323846 * t) : 0.0;
+    // LinearElasticity.cc:597-606
+    const double t0 = 8.0, c = 1.1;
+    double s = t - t0;
+    return exp(-(s * s) / ((2 * c) * (2 * c))) * cos(4.0 * s) * cos(5.0 * s) * cos(6.0 * s) * cos(7.0 * s);
+}
+
+struct PolRhsFwd {
+    static constexpr int NIN = 2, NRED = 0;
+    static constexpr bool HAS_K = true, HAS_M = true;
+    const uint8_t *fixed;
+    Weights<double> w;
+    const double *cp;                   // checkpoints: block start state (j == 0)
+    const double *Uh, *DUh, *DDUh;      // block history [tsc][ndof]
+    long long ndof;
+    const double *rhs0;                 // RHSLocation (LoadLocation, LinearElasticity.cc:616-675)
+    double load_scale;                  // 1/(ny-1)
+    int loadsignal;
+    double cK[3], cM[3];                // combination coefficients of (u-, du-, ddu-)
+    double pred[3];                     // predictor coefficients
+    const StepCtx *st;
+    double *b, *x0;
+    Partials<1> part;
+    __device__ __forceinline__ void prev(const double *&u, const double *&du, const double *&ddu) const {
+        int j = st->j;
+        if (j == 0) {
+            const double *base = cp + (long long)st->block * 3 * ndof;
+            u = base;
+            du = base + ndof;
+            ddu = base + 2 * ndof;
+        } else {
+            u = Uh + (long long)(j - 1) * ndof;
+            du = DUh + (long long)(j - 1) * ndof;
+            ddu = DDUh + (long long)(j - 1) * ndof;
+        }
+    }
+    __device__ void load(long long n, double v[2][3]) const {
+        const double *u, *du, *ddu;
+        prev(u, du, ddu);
+        for (int c = 0; c < 3; c++) {
+            double a = u[3 * n + c], bb = du[3 * n + c], cc = ddu[3 * n + c];
+            v[0][c] = cK[0] * a + cK[1] * bb + cK[2] * cc;
+            v[1][c] = cM[0] * a + cM[1] * bb + cM[2] * cc;
+        }
+        mask3(fixed[n], v[0]);
+        mask3(fixed[n], v[1]);
+    }
+    __device__ void coef(long long e, double &ck, double &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const double y[3], double *) const {
+        const double *u, *du, *ddu;
+        prev(u, du, ddu);
+        int t = st->tsc * st->block + st->j + 1;
+        double s = load_signal(loadsignal, t * st->dt) * load_scale;
+        uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) {
+            bool fx = (f >> c) & 1;
+            b[3 * n + c] = fx ? 0.0 : (rhs0[3 * n + c] * s + y[c]);
+            x0[3 * n + c] = fx ? 0.0 : (pred[0] * u[3 * n + c] + pred[1] * du[3 * n + c] + pred[2] * ddu[3 * n + c]);
+        }
+    }
+    __device__ void finish(const double *) const {}
+};
+
+}  // namespace topo

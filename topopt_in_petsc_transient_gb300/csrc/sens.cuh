@@ -1,0 +1,288 @@
+// sens.cuh -- adjoint right-hand side and element sensitivity kernels.
+#pragma once
+#include "kernels.cuh"
+
+namespace topo {
+
+// ---------------------------------------------------------------------------
+// Adjoint step right-hand side, SolveLagrangen (LinearElasticity.cc:890-926):
+//   DL  = -(h_du  + B2 L+ - a0 DL+ + a3 DDL+)
+//   DDL = -(h_ddu + B3 L+ + a4 DDL+)
+//   R1  = N ( -(h_u + B1 L+ + a2 DL+ + a5 DDL+) + a2 DL + a5 DDL )
+// with B_i L+ = N (cMi M + cKi K) N L+.  The terminal step (:864-889) is the
+// same formula with L+ = DL+ = DDL+ = 0, which is how the sweep starts.
+// h_* (ComputeGradientObjectiveElementLoop, :2206-2356) come either from the
+// per-node region count (objectives 0-2: dt * sum_{e ni n} P_e * state) or
+// from weighted element products computed beforehand (objectives 3-6).
+// Values on clamped DOFs of DL/DDL never reach lambda or the sensitivities.
+// ---------------------------------------------------------------------------
+struct AdjCombine {
+    const uint8_t *fixed;
+    const double *KL, *ML;        // K L+ and M L+ (unmasked element sums, masked input)
+    const double *Lp1, *DLp1, *DDLp1;
+    const double *hK, *hM;        // product-form objective gradients (or null)
+    const float *cntP;            // per node sum of P over adjacent elements
+    const double *Ustate, *DUstate, *DDUstate;  // state at this step (base of history)
+    const double *cp;             // checkpoints (for j < 0: t = 0 state)
+    long long ndof;
+    int objective;
+    int t0mode;                   // 1: SolveLagrange0 right-hand side R3
+    double dt;
+    double a[6];
+    double cM[3], cK[3];          // B1..B3 coefficients
+    const StepCtx *st;
+    double *DL, *DDL, *b, *x0;
+};
+
+static __global__ void k_adj_combine(AdjCombine A) {
+    long long nn = A.ndof / 3;
+    const double *u, *du, *ddu;
+    if (A.t0mode) {
+        u = A.cp;
+        du = A.cp + A.ndof;
+        ddu = A.cp + 2 * A.ndof;
+    } else {
+        long long off = (long long)A.st->j * A.ndof;
+        u = A.Ustate + off;
+        du = A.DUstate + off;
+        ddu = A.DDUstate + off;
+    }
+    const double *a = A.a;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+        uint8_t f = A.fixed[n];
+        double cnt = A.cntP[n];
+        for (int c = 0; c < 3; c++) {
+            long long i = 3 * n + c;
+            double hu = 0.0, hdu = 0.0, hddu = 0.0;
+            switch (A.objective) {
+            case 0: hu = A.dt * cnt * u[i]; break;
+            case 1: hdu = A.dt * cnt * du[i]; break;
+            case 2: hddu = A.dt * cnt * ddu[i]; break;
+            case 3: hu = A.hK[i]; break;
+            case 4: hdu = A.hM[i]; break;
+            case 5:
+                hu = A.hK[i];
+                hdu = A.hM[i];
+                break;
+            default: hdu = A.hK[i]; break;
+            }
+            bool fx = (f >> c) & 1;
+            double kl = fx ? 0.0 : A.KL[i], ml = fx ? 0.0 : A.ML[i];
+            double B1 = A.cM[0] * ml + A.cK[0] * kl;
+            double B2 = A.cM[1] * ml + A.cK[1] * kl;
+            double B3 = A.cM[2] * ml + A.cK[2] * kl;
+            double dlp = A.DLp1[i], ddlp = A.DDLp1[i];
+            if (A.t0mode) {
+                // SolveLagrange0 R3 (LinearElasticity.cc:753-758)
+                double r3 = -(hddu + B3 - a[1] * dlp + a[4] * ddlp);
+                A.b[i] = fx ? 0.0 : r3;
+                A.x0[i] = fx ? 0.0 : 0.0;
+            } else {
+                double DL = -(hdu + B2 - a[0] * dlp + a[3] * ddlp);
+                double DDL = -(hddu + B3 + a[4] * ddlp);
+                double R1 = -(hu + B1 + a[2] * dlp + a[5] * ddlp) + a[2] * DL + a[5] * DDL;
+                A.DL[i] = DL;
+                A.DDL[i] = DDL;
+                A.b[i] = fx ? 0.0 : R1;
+                A.x0[i] = fx ? 0.0 : A.Lp1[i];
+            }
+        }
+    }
+}
+
+// per-node count of adjacent elements inside the objective region
+static __global__ void k_count_region(GridDesc g, const double *__restrict__ P, float *cnt) {
+    long long nn = g.nn();
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
+        double s = 0.0;
+        for (int c = 0; c < 8; c++) {
+            int ei = i - (c & 1), ej = j - ((c >> 1) & 1), ek = k - (c >> 2);
+            if (ei < 0 || ej < 0 || ek < 0 || ei >= g.ex || ej >= g.ey || ek >= g.ez) continue;
+            s += P[ei + (long long)g.ex * (ej + (long long)g.ey * ek)];
+        }
+        cnt[n] = (float)s;
+    }
+}
+
+// after the adjoint solve of step j: L+ <- lambda_j, DL+ <- DL_j, DDL+ <- DDL_j
+static __global__ void k_adj_advance(long long ndof, const double *__restrict__ lam, const double *__restrict__ DL,
+                              const double *__restrict__ DDL, double *Lp1, double *DLp1, double *DDLp1) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        Lp1[i] = lam[i];
+        DLp1[i] = DL[i];
+        DDLp1[i] = DDL[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Element sensitivities + objective, ComputeSensitivitiesElementLoopn
+// (LinearElasticity.cc:1911-2077), ComputeSensitivitiesElementLoop0
+// (:2080-2204) and ComputeObjectiveElementLoop (:2359-2452), fused.
+//
+// The 4 x 576 multiply-adds per element of the reference reduce to
+//   df_e += P_e dfx0_e + lam_e' (dkfac_e KE wK_e + dmfac_e ME wM_e)
+// with wK = sum aK_i s_i + bK_i p_i and wM likewise over the current state
+// s = (u, du, ddu) and the previous state p; evaluated in the mode basis as
+//   Lam' Khat WK  and  sum_m W_m Lam_m WM_m.
+// One thread per element; OBJ is the reference objective (EvaluateObjective,
+// :1416-1465, EvaluateObjectiveGradient :1469-1514).
+// ---------------------------------------------------------------------------
+struct SensArgs {
+    GridDesc g;
+    const double *lam;                       // adjoint (lambda_j, or DDL0)
+    const double *Uh, *DUh, *DDUh;           // history base (current = slot j)
+    const double *cp;                        // checkpoints (block start / t = 0 state)
+    const double *kf, *dkf, *mf, *dmf, *P;
+    double aK[3], bK[3], aM[3], bM[3];       // wK, wM combination coefficients
+    double dt, dalpha, dbeta;
+    int t0mode;                              // 1: state = t = 0, no previous state
+    int with_objective;                      // accumulate the objective of the current state
+    const StepCtx *st;
+    double *df;
+    double *fx;                              // device accumulator
+    Partials<1> part;
+};
+
+template <class T>
+__device__ __forceinline__ void gather8(const double *v, const long long nodes[8], T out[3][8]) {
+#pragma unroll
+    for (int L = 0; L < 8; L++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) out[c][L] = (T)v[3 * nodes[L] + c];
+}
+
+template <class T>
+__device__ __forceinline__ T quad_K(const ElemConst<T> &C, T A[3][8], T B[3][8]) {
+    // A, B already in mode space; returns A' Khat B
+    T Y[3][8];
+    mode_stiffness(C, B, Y);
+    T s = T(0);
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int m = 0; m < 8; m++) s += A[c][m] * Y[c][m];
+    return s;
+}
+template <class T>
+__device__ __forceinline__ T quad_M(const ElemConst<T> &C, T A[3][8], T B[3][8]) {
+    T s = T(0);
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int m = 0; m < 8; m++) s += C.W[m] * A[c][m] * B[c][m];
+    return s;
+}
+
+template <int OBJ, class T>
+static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const ElemConst<T> C) {
+    const GridDesc g = A.g;
+    const long long nel = g.nel(), ndof = 3 * g.nn();
+    const double *u, *du, *ddu, *up = nullptr, *dup = nullptr, *ddup = nullptr;
+    if (A.t0mode) {
+        u = A.cp;
+        du = A.cp + ndof;
+        ddu = A.cp + 2 * ndof;
+    } else {
+        int j = A.st->j;
+        u = A.Uh + (long long)j * ndof;
+        du = A.DUh + (long long)j * ndof;
+        ddu = A.DDUh + (long long)j * ndof;
+        if (j == 0) {
+            const double *base = A.cp + (long long)A.st->block * 3 * ndof;
+            up = base;
+            dup = base + ndof;
+            ddup = base + 2 * ndof;
+        } else {
+            up = A.Uh + (long long)(j - 1) * ndof;
+            dup = A.DUh + (long long)(j - 1) * ndof;
+            ddup = A.DDUh + (long long)(j - 1) * ndof;
+        }
+    }
+    double fxv[1] = {0.0};
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(e % g.ex), jj = (int)((e / g.ex) % g.ey), k = (int)(e / ((long long)g.ex * g.ey));
+        long long nodes[8];
+#pragma unroll
+        for (int L = 0; L < 8; L++)
+            nodes[L] = (i + (L & 1)) + (long long)g.nx * ((jj + ((L >> 1) & 1)) + (long long)g.ny * (k + (L >> 2)));
+        T Lm[3][8], WK[3][8], WM[3][8];
+        gather8<T>(A.lam, nodes, Lm);
+        // combination vectors (nodal), then transform
+#pragma unroll
+        for (int L = 0; L < 8; L++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                long long q = 3 * nodes[L] + c;
+                double s0 = u[q], s1 = du[q], s2 = ddu[q];
+                double wk = A.aK[0] * s0 + A.aK[1] * s1 + A.aK[2] * s2;
+                double wm = A.aM[0] * s0 + A.aM[1] * s1 + A.aM[2] * s2;
+                if (!A.t0mode) {
+                    double p0 = up[q], p1 = dup[q], p2 = ddup[q];
+                    wk += A.bK[0] * p0 + A.bK[1] * p1 + A.bK[2] * p2;
+                    wm += A.bM[0] * p0 + A.bM[1] * p1 + A.bM[2] * p2;
+                }
+                WK[c][L] = (T)wk;
+                WM[c][L] = (T)wm;
+            }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            mode_fwd(Lm[c]);
+            mode_fwd(WK[c]);
+            mode_fwd(WM[c]);
+        }
+        double dkfe = A.dkf[e], dmfe = A.dmf[e], kfe = A.kf[e], mfe = A.mf[e], Pe = A.P[e];
+        double t3 = dkfe * (double)quad_K(C, Lm, WK) + dmfe * (double)quad_M(C, Lm, WM);
+        // objective value h0 and its explicit density derivative dfx0
+        double h0 = 0.0, dfx0 = 0.0;
+        if (OBJ == 0 || OBJ == 1 || OBJ == 2) {
+            if (A.with_objective) {
+                const double *s = (OBJ == 0) ? u : (OBJ == 1 ? du : ddu);
+                double acc = 0.0;
+#pragma unroll
+                for (int L = 0; L < 8; L++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        double v = s[3 * nodes[L] + c];
+                        acc += v * v;
+                    }
+                h0 = A.dt * 0.5 * acc;
+            }
+        } else {
+            T S0[3][8];
+            const double *s = (OBJ == 3) ? u : du;
+            gather8<T>(s, nodes, S0);
+#pragma unroll
+            for (int c = 0; c < 3; c++) mode_fwd(S0[c]);
+            if (OBJ == 3) {
+                double uKu = (double)quad_K(C, S0, S0);
+                h0 = A.dt * 0.5 * kfe * uKu;
+                dfx0 = A.dt * 0.5 * dkfe * uKu;
+            } else if (OBJ == 4) {
+                double vMv = (double)quad_M(C, S0, S0);
+                h0 = A.dt * 0.5 * mfe * vMv;
+                dfx0 = A.dt * 0.5 * dmfe * vMv;
+            } else if (OBJ == 5) {
+                T S1[3][8];
+                gather8<T>(u, nodes, S1);
+#pragma unroll
+                for (int c = 0; c < 3; c++) mode_fwd(S1[c]);
+                double uKu = (double)quad_K(C, S1, S1);
+                double vMv = (double)quad_M(C, S0, S0);
+                h0 = A.dt * 0.5 * (kfe * uKu + mfe * vMv);
+                dfx0 = A.dt * 0.5 * (dkfe * uKu + dmfe * vMv);
+            } else {  // 6: dissipated energy with interpolated damping
+                double vKv = (double)quad_K(C, S0, S0);
+                double vMv = (double)quad_M(C, S0, S0);
+                h0 = A.dt * 0.5 * (A.dalpha * mfe * vMv + A.dbeta * kfe * vKv);
+                dfx0 = A.dt * 0.5 * (A.dalpha * dmfe * vMv + A.dbeta * dkfe * vKv);
+            }
+        }
+        A.df[e] += Pe * dfx0 + t3;
+        if (A.with_objective) fxv[0] += Pe * h0;
+    }
+    double tot[1];
+    if (grid_reduce<EW, 1>(fxv, A.part, tot)) *A.fx += tot[0];
+}
+
+}  // namespace topo

@@ -1,0 +1,177 @@
+// tile.cuh -- the matrix-free hex8 operator kernel.
+//
+// One CTA of 512 threads owns a 7x7x7 brick of output nodes.  It stages the
+// 9x9x9 input nodes (brick + one-node halo) in shared memory, lets each thread
+// apply the element operator of one of the 8x8x8 elements touching the brick
+// (mode-basis form, common.cuh), parks the 24 element outputs in shared memory
+// and finally lets each output node gather its 8 element contributions.  No
+// atomics: every output is written once, so results are bitwise reproducible.
+// Element work on the brick faces is recomputed by the neighbour CTA
+// (512/343 = 1.49x redundancy), traded for determinism and zero global
+// scatter traffic.
+//
+// What is staged, how element weights are formed and what happens to the
+// assembled value (masking, fused vector updates, dot products) is supplied by
+// a policy type; see le.cu for the policies used by the solver.
+#pragma once
+#include "common.cuh"
+
+namespace topo {
+
+constexpr int TILE = 7;               // output nodes per CTA edge
+constexpr int TILE_E = TILE + 1;      // elements per CTA edge
+constexpr int TILE_N = TILE + 2;      // staged nodes per CTA edge
+constexpr int TILE_THREADS = 512;     // == TILE_E^3
+constexpr int TILE_STAGED = TILE_N * TILE_N * TILE_N;  // 729
+constexpr int TILE_OUT = TILE * TILE * TILE;            // 343
+constexpr int EL_STRIDE = 25;         // padded element-output row (bank spread)
+
+template <class T, class Pol>
+constexpr size_t tile_smem_bytes() {
+    return sizeof(T) * ((size_t)Pol::NIN * TILE_STAGED * 3 + (size_t)TILE_THREADS * EL_STRIDE);
+}
+
+__host__ inline dim3 tile_grid(const GridDesc &g) {
+    return dim3((g.nx + TILE - 1) / TILE, (g.ny + TILE - 1) / TILE, (g.nz + TILE - 1) / TILE);
+}
+
+// Policy interface:
+//   static constexpr int NIN;      staged 3-vectors per node (1: K and M act on
+//                                  input 0; 2: K on input 0, M on input 1)
+//   static constexpr bool HAS_K, HAS_M;
+//   static constexpr int NRED;     grid-reduced doubles (0..4)
+//   __device__ void load(long long n, T v[NIN][3]) const;
+//   __device__ void coef(long long e, T &ck, T &cm) const;
+//   __device__ void epilogue(long long n, int i, int j, int k, const T y[3], double red[]) const;
+//   __device__ void finish(const double tot[]) const;   (thread 0 of last CTA)
+//   Partials<NRED> part;  (when NRED > 0)
+template <class T, class Pol>
+__global__ void __launch_bounds__(TILE_THREADS, 1) k_tile(const GridDesc g, const ElemConst<T> C, const Pol pol) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sIn = reinterpret_cast<T *>(smem_raw);
+    T *sEl = sIn + Pol::NIN * TILE_STAGED * 3;
+    const int tid = threadIdx.x;
+    const int i0 = blockIdx.x * TILE, j0 = blockIdx.y * TILE, k0 = blockIdx.z * TILE;
+
+    // ---- stage inputs (brick + halo), zero outside the domain ----
+    for (int s = tid; s < TILE_STAGED; s += TILE_THREADS) {
+        int lx = s % TILE_N, ly = (s / TILE_N) % TILE_N, lz = s / (TILE_N * TILE_N);
+        int gi = i0 - 1 + lx, gj = j0 - 1 + ly, gk = k0 - 1 + lz;
+        T v[Pol::NIN][3];
+        if (gi >= 0 && gi < g.nx && gj >= 0 && gj < g.ny && gk >= 0 && gk < g.nz) {
+            long long n = gi + (long long)g.nx * (gj + (long long)g.ny * gk);
+            pol.load(n, v);
+        } else {
+#pragma unroll
+            for (int f = 0; f < Pol::NIN; f++) v[f][0] = v[f][1] = v[f][2] = T(0);
+        }
+#pragma unroll
+        for (int f = 0; f < Pol::NIN; f++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) sIn[(f * TILE_STAGED + s) * 3 + c] = v[f][c];
+    }
+    __syncthreads();
+
+    // ---- one element per thread ----
+    {
+        const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;
+        const int ei = i0 - 1 + lx, ej = j0 - 1 + ly, ek = k0 - 1 + lz;
+        T *out = sEl + tid * EL_STRIDE;
+        if (ei >= 0 && ei < g.ex && ej >= 0 && ej < g.ey && ek >= 0 && ek < g.ez) {
+            long long e = ei + (long long)g.ex * (ej + (long long)g.ey * ek);
+            T ck, cm;
+            pol.coef(e, ck, cm);
+            T U[3][8];
+#pragma unroll
+            for (int L = 0; L < 8; L++) {
+                int s = (lx + (L & 1)) + TILE_N * ((ly + ((L >> 1) & 1)) + TILE_N * (lz + (L >> 2)));
+#pragma unroll
+                for (int c = 0; c < 3; c++) U[c][L] = sIn[s * 3 + c];
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) mode_fwd(U[c]);
+            T D[8];
+            if (Pol::HAS_K) {
+#pragma unroll
+                for (int m = 0; m < 8; m++) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+                        if (!(m & (1 << a))) acc += C.g[a] * U[a][m | (1 << a)];
+                    D[m] = acc;
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                T Y[8];
+#pragma unroll
+                for (int m = 0; m < 8; m++) Y[m] = T(0);
+                if (Pol::HAS_K) {
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+#pragma unroll
+                        for (int m = 0; m < 8; m++) {
+                            if (m & (1 << a)) continue;
+                            T sym = C.g[a] * U[b][m | (1 << a)];
+                            if (!(m & (1 << b))) sym += C.g[b] * U[a][m | (1 << b)];
+                            T S = C.mu * sym;
+                            if (a == b) S += C.lam * D[m];
+                            Y[m | (1 << a)] += (C.g[a] * C.W[m]) * S;
+                        }
+#pragma unroll
+                    for (int m = 0; m < 8; m++) Y[m] *= ck;
+                }
+                if (Pol::HAS_M) {
+                    T V[8];
+                    if (Pol::NIN == 2) {
+#pragma unroll
+                        for (int L = 0; L < 8; L++) {
+                            int s = (lx + (L & 1)) + TILE_N * ((ly + ((L >> 1) & 1)) + TILE_N * (lz + (L >> 2)));
+                            V[L] = sIn[((Pol::NIN - 1) * TILE_STAGED + s) * 3 + b];
+                        }
+                        mode_fwd(V);
+                    } else {
+#pragma unroll
+                        for (int m = 0; m < 8; m++) V[m] = U[b][m];
+                    }
+#pragma unroll
+                    for (int m = 0; m < 8; m++) Y[m] += (cm * C.W[m]) * V[m];
+                }
+                mode_bwd(Y);
+#pragma unroll
+                for (int L = 0; L < 8; L++) out[L * 3 + b] = Y[L];
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 24; q++) out[q] = T(0);
+        }
+    }
+    __syncthreads();
+
+    // ---- gather + policy epilogue ----
+    double red[Pol::NRED > 0 ? Pol::NRED : 1];
+#pragma unroll
+    for (int r = 0; r < (Pol::NRED > 0 ? Pol::NRED : 1); r++) red[r] = 0.0;
+    if (tid < TILE_OUT) {
+        const int tx = tid % TILE, ty = (tid / TILE) % TILE, tz = tid / (TILE * TILE);
+        const int gi = i0 + tx, gj = j0 + ty, gk = k0 + tz;
+        if (gi < g.nx && gj < g.ny && gk < g.nz) {
+            T y[3] = {T(0), T(0), T(0)};
+#pragma unroll
+            for (int L = 0; L < 8; L++) {
+                int ax = L & 1, ay = (L >> 1) & 1, az = L >> 2;
+                int le = (tx + 1 - ax) + TILE_E * ((ty + 1 - ay) + TILE_E * (tz + 1 - az));
+#pragma unroll
+                for (int c = 0; c < 3; c++) y[c] += sEl[le * EL_STRIDE + L * 3 + c];
+            }
+            long long n = gi + (long long)g.nx * (gj + (long long)g.ny * gk);
+            pol.epilogue(n, gi, gj, gk, y, red);
+        }
+    }
+    if constexpr (Pol::NRED > 0) {
+        double tot[Pol::NRED];
+        if (grid_reduce<TILE_THREADS, Pol::NRED>(red, pol.part, tot)) pol.finish(tot);
+    }
+}
+
+}  // namespace topo

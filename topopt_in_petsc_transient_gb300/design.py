@@ -1,0 +1,137 @@
+"""TopOpt-style configuration and the main.cc design iteration on the GPU path.
+
+`TopOpt` holds the parameters TopOpt::SetUp/SetUpOPT read from the PETSc
+options database (TopOpt.cc:71-518) and the design vectors as device tensors.
+`design_iteration` performs one pass of the optimisation loop of main.cc:82-154
+with the same call order: CompleteInitialState, GenerateCheckPoints,
+ComputeObjectiveSensitivities, VolumeConstraint, Filter::Gradients, objective
+scaling, SetOuterMovelimit, MMA::Update, DesignChange, IncreaseBeta,
+Filter::FilterProject.
+"""
+from dataclasses import dataclass, field
+
+
+@dataclass
+class TopOpt:
+    nelx: int = 64
+    nely: int = 32
+    nelz: int = 32
+    h: tuple = (1.0, 1.0, 1.0)
+    nu: float = 0.3
+    nlvls: int = 4
+    volfrac: float = 0.3
+    V0: float = None
+    maxItr: int = 10
+    rmin: float = 1.5
+    penalK: float = 3.0
+    penalM: float = 1.0
+    Emax: float = 1e3
+    Ef: float = 1e-9
+    Rmax: float = 4.16666666667e-4
+    Rf: float = 1e-3
+    filter: int = 2
+    sInt: int = 1
+    mInt: int = 0
+    Xmin: float = 0.0
+    Xmax: float = 1.0
+    movlim: float = 0.2
+    ti: int = 1
+    t1: float = 50.0
+    ncp: int = 2
+    tsc: int = 25
+    dalpha: float = 1e-4
+    dbeta: float = 1e-4
+    objective: int = 0
+    minmax: int = -1
+    boundaries: int = 1
+    loadloc: int = 1
+    optimizationRegion: int = 2
+    projectionFilter: bool = True
+    beta: float = 0.1
+    betaFinal: float = 48.0
+    eta: float = 0.15
+    loadsignal: int = 0
+    m: int = 1
+    # GB300 solver controls
+    mixed: bool = True
+    rtol: float = 1e-10
+    filter_rtol: float = 1e-10
+    smooth: int = 3
+    cheb_ratio: float = 30.0
+    use_graphs: bool = True
+    # state
+    fscale: float = 1.0
+    itr: int = 0
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def Emin(self):
+        return self.Ef * self.Emax  # TopOpt.cc:472
+
+    @property
+    def Rmin(self):
+        return self.Rf * self.Rmax  # TopOpt.cc:474
+
+    @property
+    def nel(self):
+        return self.nelx * self.nely * self.nelz
+
+    def setup(self, device="cuda"):
+        """Allocates design vectors (TopOpt::SetUpOPT, TopOpt.cc:495-515) and
+        the physics, filter and MMA objects (main.cc:35-58)."""
+        import torch
+
+        from .topopt import MMA, Filter, LinearElasticity
+        V0 = self.volfrac if self.V0 is None else self.V0
+        n = self.nel
+        f64 = dict(dtype=torch.float64, device=device)
+        self.x = torch.full((n,), V0, **f64)
+        self.xTilde = torch.full((n,), V0, **f64)
+        self.xPhys = torch.full((n,), V0, **f64)
+        self.xold = torch.full((n,), V0, **f64)
+        self.dfdx = torch.zeros(n, **f64)
+        self.dgdx = torch.zeros(self.m * n, **f64)
+        self.xmin = torch.zeros(n, **f64)
+        self.xmax = torch.zeros(n, **f64)
+        self.physics = LinearElasticity(
+            self.nelx, self.nely, self.nelz, nu=self.nu, nlvls=self.nlvls, ncp=self.ncp, tsc=self.tsc, t1=self.t1,
+            ti=self.ti, objective=self.objective, stiffnessInterpolation=self.sInt, massInterpolation=self.mInt,
+            boundaries=self.boundaries, loadloc=self.loadloc, dalpha=self.dalpha, dbeta=self.dbeta,
+            optimizationRegion=self.optimizationRegion, h=self.h, loadsignal=self.loadsignal, mixed=self.mixed,
+            rtol=self.rtol, smooth=self.smooth, cheb_ratio=self.cheb_ratio, use_graphs=self.use_graphs)
+        self.filt = Filter(self.nelx, self.nely, self.nelz, self.filter, self.rmin, h=self.h, rtol=self.filter_rtol)
+        self.mma = MMA(n, self.m, self.x)
+        self.mma.SetAsymptotes(0.1, 0.6, 1.05)  # main.cc:58
+        self.filt.FilterProject(self.x, self.xTilde, self.xPhys, self.projectionFilter, self.beta, self.eta)
+        return self
+
+
+def design_iteration(opt: TopOpt):
+    """One iteration of the main.cc optimisation loop (main.cc:76-160);
+    returns (fx_true, gx0, ch, mnd)."""
+    opt.itr += 1
+    ph = opt.physics
+    ph.CompleteInitialState(opt.xPhys, opt.Emin, opt.Emax, opt.Rmin, opt.Rmax, opt.penalK, opt.penalM)
+    if opt.ncp > 1:
+        ph.GenerateCheckPoints()
+    fx = ph.ComputeObjectiveSensitivities(opt.dfdx)
+    gx0 = ph.VolumeConstraint(opt.dgdx, opt.xPhys, opt.volfrac)
+    opt.filt.Gradients(opt.x, opt.xTilde, opt.dfdx, opt.m, opt.dgdx, opt.projectionFilter, opt.beta, opt.eta)
+    mnd = opt.filt.GetMND(opt.xPhys)
+    if opt.itr == 1:
+        opt.fscale = 1.0 / fx
+    fxs = fx * opt.fscale
+    opt.dfdx.mul_(opt.fscale)
+    opt.mma.SetOuterMovelimit(opt.Xmin, opt.Xmax, opt.movlim, opt.x, opt.xmin, opt.xmax)
+    if opt.minmax == 1:
+        opt.dfdx.mul_(-1.0)
+    opt.mma.Update(opt.x, opt.dfdx, [gx0], opt.dgdx, opt.xmin, opt.xmax)
+    ch = opt.mma.DesignChange(opt.x, opt.xold)
+    if opt.projectionFilter and (opt.itr >= 200 or ch < 0.01):
+        changed, opt.beta = opt.filt.IncreaseBeta(opt.beta, opt.betaFinal, gx0, opt.itr, ch)
+        if changed:
+            ch = 1.0
+    if gx0 > 0:
+        ch = 1.0
+    opt.filt.FilterProject(opt.x, opt.xTilde, opt.xPhys, opt.projectionFilter, opt.beta, opt.eta)
+    return fx, fxs, gx0, ch, mnd

@@ -1,0 +1,292 @@
+"""Host-side mirror of the reference classes on the transient hot path.
+
+Same class names, method names, argument meaning and call order as
+TopOpt_in_PETSc_Transient's C++ (LinearElasticity.h, PDEFilter.h, Filter.h,
+MMA.h, TopOpt.h); a non-zero status raises TopoError instead of returning a
+PetscErrorCode.  Arrays are either host numpy float64 arrays (VecGetArray
+semantics: DMDA natural order) or CUDA float64 torch tensors (device
+pointers, no copies).  All arithmetic happens in libtopopt_gb300.so.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import LEParams, LEStats, TopoError, check
+
+
+def _is_dev(a):
+    return hasattr(a, "is_cuda") and a.is_cuda
+
+
+def _addr(a, n=None, name="array"):
+    """(is_device, address) of a float64 contiguous buffer."""
+    if _is_dev(a):
+        import torch
+        if a.dtype != torch.float64 or not a.is_contiguous():
+            raise TypeError("%s must be a contiguous float64 CUDA tensor" % name)
+        if n is not None and a.numel() < n:
+            raise ValueError("%s has %d values, %d required" % (name, a.numel(), n))
+        return True, a.data_ptr()
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("%s must be a C-contiguous float64 numpy array or CUDA tensor" % name)
+    if n is not None and a.size < n:
+        raise ValueError("%s has %d values, %d required" % (name, a.size, n))
+    return False, a.ctypes.data
+
+
+class LinearElasticity:
+    """LinearElasticity (LinearElasticity.h:23-240) on the GPU.
+
+    Constructor arguments follow LinearElasticity::LinearElasticity
+    (LinearElasticity.h:29) with the DMDA replaced by its node counts and
+    element size; `mixed`, `rtol`, `maxit`, `smooth`, `cheb_ratio`,
+    `use_graphs` control the GB300 solver.
+    """
+
+    def __init__(self, nelx, nely, nelz, nu=0.3, nlvls=4, ncp=2, tsc=25, t1=50.0, ti=1, objective=0,
+                 stiffnessInterpolation=1, massInterpolation=0, t0=0.0, boundaries=1, loadloc=1, reduction=False,
+                 basis=5, dalpha=1e-4, dbeta=1e-4, omega0=1.0, optimizationRegion=2, V0=None, h=(1.0, 1.0, 1.0),
+                 loadsignal=0, mixed=True, rtol=1e-10, maxit=500, smooth=3, cheb_ratio=30.0, use_graphs=True):
+        if reduction:
+            raise TopoError(1, "LinearElasticity", "the SOMMG reduced-order path is not part of this build")
+        L = _lib.load()
+        p = LEParams()
+        L.topo_le_default_params(C.byref(p), nelx, nely, nelz)
+        p.hx, p.hy, p.hz = h
+        p.nu = nu
+        p.nlvls, p.ncp, p.tsc, p.t1, p.ti = nlvls, ncp, tsc, t1, ti
+        p.objective, p.sInt, p.mInt = objective, stiffnessInterpolation, massInterpolation
+        p.boundaries, p.loadloc, p.optregion, p.loadsignal = boundaries, loadloc, optimizationRegion, loadsignal
+        p.dalpha, p.dbeta = dalpha, dbeta
+        p.mixed, p.rtol, p.maxit, p.smooth = int(bool(mixed)), rtol, maxit, smooth
+        p.cheb_ratio, p.use_graphs = cheb_ratio, int(bool(use_graphs))
+        self.params = p
+        self.nelx, self.nely, self.nelz = nelx, nely, nelz
+        self.nel = nelx * nely * nelz
+        self.nn = (nelx + 1) * (nely + 1) * (nelz + 1)
+        self.ndof = 3 * self.nn
+        self.Ts = ncp * tsc + 1
+        self.dt = t1 / (self.Ts - 1)
+        h_ = C.c_void_p()
+        check(L.topo_le_create(C.byref(h_), C.byref(p)), "LinearElasticity")
+        self._h = h_
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().topo_le_destroy(h)
+            self._h = None
+
+    def CompleteInitialState(self, xPhys, Emin, Emax, Rmin, Rmax, penalK, penalM, dalpha=None, dbeta=None,
+                             write=False, output=None):
+        """LinearElasticity::CompleteInitialState (LinearElasticity.cc:956-1206)."""
+        L = _lib.load()
+        dev, a = _addr(xPhys, self.nel, "xPhys")
+        f = L.topo_le_complete_initial_state_dev if dev else L.topo_le_complete_initial_state
+        check(f(self._h, a, Emin, Emax, Rmin, Rmax, penalK, penalM), "CompleteInitialState")
+        return 0
+
+    def GenerateCheckPoints(self, write=False, xPhys=None, output=None):
+        """LinearElasticity::GenerateCheckPoints (LinearElasticity.cc:1208-1280)."""
+        check(_lib.load().topo_le_generate_checkpoints(self._h), "GenerateCheckPoints")
+        return 0
+
+    def ComputeObjectiveSensitivities(self, dfdx, *args, **kw):
+        """LinearElasticity::ComputeObjectiveSensitivities (LinearElasticity.cc:1625-1908).
+
+        Overwrites dfdx and returns fx (the reference writes *fx)."""
+        L = _lib.load()
+        dev, a = _addr(dfdx, self.nel, "dfdx")
+        fx = C.c_double()
+        f = L.topo_le_compute_objective_sensitivities_dev if dev else L.topo_le_compute_objective_sensitivities
+        check(f(self._h, C.byref(fx), a), "ComputeObjectiveSensitivities")
+        return fx.value
+
+    def VolumeConstraint(self, dgdx, xPhys, volfrac):
+        """LinearElasticity::VolumeConstraint (LinearElasticity.cc:1283-1296); returns gx[0]."""
+        L = _lib.load()
+        dev1, a = _addr(dgdx, self.nel, "dgdx")
+        dev2, b = _addr(xPhys, self.nel, "xPhys")
+        if dev1 != dev2:
+            raise TypeError("dgdx and xPhys must both be host or both be device arrays")
+        gx = C.c_double()
+        f = L.topo_le_volume_constraint_dev if dev1 else L.topo_le_volume_constraint
+        check(f(self._h, C.byref(gx), a, b, volfrac), "VolumeConstraint")
+        return gx.value
+
+    # -- inspection --------------------------------------------------------
+    def state(self, which, j):
+        out = np.zeros(self.ndof)
+        check(_lib.load().topo_le_get_state(self._h, which, j, out.ctypes.data), "get_state")
+        return out
+
+    def apply_km(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        K = np.zeros(self.ndof)
+        M = np.zeros(self.ndof)
+        check(_lib.load().topo_le_apply_km(self._h, x.ctypes.data, K.ctypes.data, M.ctypes.data), "apply_km")
+        return K, M
+
+    def stats(self):
+        s = LEStats()
+        check(_lib.load().topo_le_get_stats(self._h, C.byref(s)), "get_stats")
+        return {"cg_iterations": s.cg_iterations, "solves": s.solves, "device_bytes": s.device_bytes,
+                "last_fx": s.last_fx}
+
+
+class PDEFilt:
+    """PDEFilt (PDEFilter.h:29-74): Helmholtz filter on the nodal grid."""
+
+    def __init__(self, nelx, nely, nelz, rmin, h=(1.0, 1.0, 1.0), rtol=1e-10, maxit=5000):
+        L = _lib.load()
+        h_ = C.c_void_p()
+        check(L.topo_pdefilt_create(C.byref(h_), nelx + 1, nely + 1, nelz + 1, h[0], h[1], h[2], rmin, rtol, maxit),
+              "PDEFilt")
+        self._h = h_
+        self.nel = nelx * nely * nelz
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().topo_pdefilt_destroy(h)
+            self._h = None
+
+    def FilterProject(self, OX, FX):
+        """PDEFilt::FilterProject (PDEFilter.cc:193-222)."""
+        L = _lib.load()
+        d1, a = _addr(OX, self.nel, "OX")
+        d2, b = _addr(FX, self.nel, "FX")
+        if d1 != d2:
+            raise TypeError("OX and FX must both be host or both be device arrays")
+        f = L.topo_pdefilt_filter_project_dev if d1 else L.topo_pdefilt_filter_project
+        check(f(self._h, a, b), "PDEFilt::FilterProject")
+        return 0
+
+    def Gradients(self, OS, FS):
+        """PDEFilt::Gradients (PDEFilter.cc:224): the same symmetric operator."""
+        return self.FilterProject(OS, FS)
+
+
+class Filter:
+    """Filter (Filter.h:34-92) for filterType 2 (PDE filter) with the smoothed
+    Heaviside projection; filter types 0/1 are not part of this build."""
+
+    def __init__(self, nelx, nely, nelz, filterT, Rin, h=(1.0, 1.0, 1.0), rtol=1e-10, maxit=5000):
+        if filterT != 2:
+            raise TopoError(1, "Filter", "only the PDE filter (filter = 2) is built for the GPU path")
+        self.pdef = PDEFilt(nelx, nely, nelz, Rin, h=h, rtol=rtol, maxit=maxit)
+        self.nel = self.pdef.nel
+
+    def FilterProject(self, x, xTilde, xPhys, projectionFilter, beta, eta):
+        """Filter::FilterProject (Filter.cc:60-119)."""
+        L = _lib.load()
+        d = [_addr(v, self.nel, n) for v, n in ((x, "x"), (xTilde, "xTilde"), (xPhys, "xPhys"))]
+        if len({t[0] for t in d}) != 1:
+            raise TypeError("x, xTilde, xPhys must all be host or all be device arrays")
+        f = L.topo_filter_project_dev if d[0][0] else L.topo_filter_project
+        check(f(self.pdef._h, d[0][1], d[1][1], d[2][1], int(bool(projectionFilter)), beta, eta),
+              "Filter::FilterProject")
+        return 0
+
+    def Gradients(self, x, xTilde, dfdx, m, dgdx, projectionFilter, beta, eta):
+        """Filter::Gradients (Filter.cc:122-206); dfdx and dgdx (m x nel) in place."""
+        L = _lib.load()
+        d = [_addr(v, n_, nm) for v, n_, nm in ((xTilde, self.nel, "xTilde"), (dfdx, self.nel, "dfdx"),
+                                                 (dgdx, self.nel * m, "dgdx"))]
+        if len({t[0] for t in d}) != 1:
+            raise TypeError("xTilde, dfdx, dgdx must all be host or all be device arrays")
+        f = L.topo_filter_gradients_dev if d[0][0] else L.topo_filter_gradients
+        check(f(self.pdef._h, d[0][1], d[1][1], m, d[2][1], int(bool(projectionFilter)), beta, eta),
+              "Filter::Gradients")
+        return 0
+
+    def GetMND(self, x):
+        """Filter::GetMND (Filter.cc:208-227)."""
+        L = _lib.load()
+        dev, a = _addr(x, self.nel, "x")
+        out = C.c_double()
+        f = L.topo_filter_mnd_dev if dev else L.topo_filter_mnd
+        check(f(self.pdef._h, a, C.byref(out)), "Filter::GetMND")
+        return out.value
+
+    @staticmethod
+    def IncreaseBeta(beta, betaFinal, gx, itr, ch):
+        """Filter::IncreaseBeta (Filter.cc:274-300): scalar continuation logic;
+        returns (changeBeta, beta)."""
+        change = False
+        if (ch < 0.01 or itr % 10 == 0) and beta < betaFinal and gx <= 0.0:
+            change = True
+            beta = beta + 1 if beta < 7 else beta * 1.2
+            if beta > betaFinal:
+                beta = betaFinal
+                change = False
+        return change, beta
+
+
+class MMA:
+    """MMA (MMA.h:9-120) with design vectors on the device."""
+
+    def __init__(self, n, m, x=None, a=None, c=None, d=None):
+        L = _lib.load()
+        a = np.zeros(m) if a is None else np.ascontiguousarray(a, dtype=np.float64)
+        c = np.full(m, 1000.0) if c is None else np.ascontiguousarray(c, dtype=np.float64)
+        d = np.zeros(m) if d is None else np.ascontiguousarray(d, dtype=np.float64)
+        h_ = C.c_void_p()
+        check(L.topo_mma_create(C.byref(h_), n, m, a.ctypes.data, c.ctypes.data, d.ctypes.data), "MMA")
+        self._h = h_
+        self.n, self.m = n, m
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().topo_mma_destroy(h)
+            self._h = None
+
+    def SetAsymptotes(self, init, decrease, increase):
+        check(_lib.load().topo_mma_set_asymptotes(self._h, init, decrease, increase), "MMA::SetAsymptotes")
+        return 0
+
+    def SetOuterMovelimit(self, Xmin, Xmax, movlim, x, xmin, xmax):
+        """MMA::SetOuterMovelimit (MMA.cc:374-393); device arrays."""
+        d = [_addr(v, self.n, n) for v, n in ((x, "x"), (xmin, "xmin"), (xmax, "xmax"))]
+        if not all(t[0] for t in d):
+            raise TypeError("SetOuterMovelimit takes device (CUDA tensor) arrays")
+        check(_lib.load().topo_mma_set_outer_movelimit_dev(self._h, Xmin, Xmax, movlim, d[0][1], d[1][1], d[2][1]),
+              "MMA::SetOuterMovelimit")
+        return 0
+
+    def Update(self, xval, dfdx, gx, dgdx, xmin, xmax):
+        """MMA::Update (MMA.cc:487-507): xval updated in place."""
+        L = _lib.load()
+        g = np.ascontiguousarray(np.atleast_1d(np.asarray(gx, dtype=np.float64)))
+        d = [_addr(v, n_, nm) for v, n_, nm in ((xval, self.n, "xval"), (dfdx, self.n, "dfdx"),
+                                                 (dgdx, self.n * self.m, "dgdx"), (xmin, self.n, "xmin"),
+                                                 (xmax, self.n, "xmax"))]
+        if len({t[0] for t in d}) != 1:
+            raise TypeError("MMA::Update arrays must all be host or all be device arrays")
+        f = L.topo_mma_update_dev if d[0][0] else L.topo_mma_update
+        check(f(self._h, d[0][1], d[1][1], g.ctypes.data, d[2][1], d[3][1], d[4][1]), "MMA::Update")
+        return 0
+
+    def DesignChange(self, x, xold):
+        """MMA::DesignChange (MMA.cc:395-414): returns the inf-norm change, xold <- x."""
+        d = [_addr(v, self.n, n) for v, n in ((x, "x"), (xold, "xold"))]
+        if not all(t[0] for t in d):
+            raise TypeError("DesignChange takes device (CUDA tensor) arrays")
+        ch = C.c_double()
+        check(_lib.load().topo_mma_design_change_dev(self._h, d[0][1], d[1][1], C.byref(ch)), "MMA::DesignChange")
+        return ch.value
+
+    def KKTresidual(self, x, dfdx, fx, dgdx, xmin, xmax):
+        """MMA::KKTresidual (MMA.cc:416-484); device arrays; returns (norm2, normInf)."""
+        fxa = np.ascontiguousarray(np.atleast_1d(np.asarray(fx, dtype=np.float64)))
+        d = [_addr(v, n_, nm) for v, n_, nm in ((x, self.n, "x"), (dfdx, self.n, "dfdx"),
+                                                 (dgdx, self.n * self.m, "dgdx"), (xmin, self.n, "xmin"),
+                                                 (xmax, self.n, "xmax"))]
+        if not all(t[0] for t in d):
+            raise TypeError("KKTresidual takes device arrays")
+        n2, ni = C.c_double(), C.c_double()
+        check(_lib.load().topo_mma_kkt_residual_dev(self._h, d[0][1], d[1][1], fxa.ctypes.data, d[2][1], d[3][1],
+                                                     d[4][1], C.byref(n2), C.byref(ni)), "MMA::KKTresidual")
+        return n2.value, ni.value
