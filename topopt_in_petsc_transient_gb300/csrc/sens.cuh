@@ -83,7 +83,9 @@ static __global__ void k_adj_combine(AdjCombine A) {
                 double R1 = -(hu + B1 + a[2] * dlp + a[5] * ddlp) + a[2] * DL + a[5] * DDL;
                 A.DL[i] = DL;
                 A.DDL[i] = DDL;
-                A.b[i] = fx ? 0.0 : R1;
+                // the reference solves (N A N + I - N) L = R1 with A = -Keff
+                // (LinearElasticity.cc:1022-1026, :924): Keff L = -R1 on free DOFs
+                A.b[i] = fx ? 0.0 : -R1;
                 A.x0[i] = fx ? 0.0 : A.Lp1[i];
             }
         }
