@@ -58,6 +58,15 @@ typedef struct topo_le_params {
     int smooth;              /* Chebyshev degree of pre/post smoothing              */
     double cheb_ratio;       /* Chebyshev lower bound = max(lo_bound, hi/ratio)     */
     int use_graphs;          /* 1: CUDA graphs with device-side loop control        */
+    int coarse_dense_max;    /* coarsest level solved by a dense FP64-factored
+                                inverse when it has at most this many DOFs,
+                                otherwise by Chebyshev-Jacobi smoothing           */
+    int coarse_smooth;       /* Chebyshev degree of the iterative coarse solve      */
+    int sens_fp32;           /* mixed mode: FP32 element math in the sensitivity
+                                kernel (state combinations still formed in FP64)  */
+    double inner_tol;        /* mixed mode: FP32 recurrence residual reduction
+                                between FP64 residual replacements                */
+    int inner_maxit;         /* mixed mode: FP32 iterations between replacements    */
 } topo_le_params;
 
 typedef struct topo_le_stats {
@@ -65,6 +74,7 @@ typedef struct topo_le_stats {
     long long solves;         /* linear solves since creation           */
     double device_bytes;      /* HBM held by the object                 */
     double last_fx;           /* last objective                         */
+    long long graph_body_launches; /* kernels run inside device-side Krylov loops */
 } topo_le_stats;
 
 /* fills p with the reference defaults for a cantilever of nelx x nely x nelz
@@ -138,6 +148,8 @@ int topo_mma_create(topo_mma **out, int n, int m, const double *a, const double 
 void topo_mma_destroy(topo_mma *mma);
 int topo_mma_set_asymptotes(topo_mma *mma, double init, double decrease, double increase);
 /* MMA::SetOuterMovelimit (MMA.cc:374-393) */
+int topo_mma_set_outer_movelimit(topo_mma *mma, double Xmin, double Xmax, double movlim, const double *x,
+                                 double *xmin, double *xmax);
 int topo_mma_set_outer_movelimit_dev(topo_mma *mma, double Xmin, double Xmax, double movlim, const double *x_dev,
                                      double *xmin_dev, double *xmax_dev);
 /* MMA::Update (MMA.cc:487-507): xval updated in place; gx has m host values */
@@ -146,11 +158,17 @@ int topo_mma_update(topo_mma *mma, double *xval, const double *dfdx, const doubl
 int topo_mma_update_dev(topo_mma *mma, double *xval_dev, const double *dfdx_dev, const double *gx,
                         const double *dgdx_dev, const double *xmin_dev, const double *xmax_dev);
 /* MMA::DesignChange (MMA.cc:395-414): inf-norm change, xold <- x */
+int topo_mma_design_change(topo_mma *mma, const double *x, double *xold, double *ch);
 int topo_mma_design_change_dev(topo_mma *mma, const double *x_dev, double *xold_dev, double *ch);
 /* MMA::KKTresidual (MMA.cc:416-484) */
 int topo_mma_kkt_residual_dev(topo_mma *mma, const double *x_dev, const double *dfdx_dev, const double *fx,
                               const double *dgdx_dev, const double *xmin_dev, const double *xmax_dev, double *norm2,
                               double *normInf);
+
+/* kernels launched by this library so far (direct launches and graph
+ * replays; kernels inside device-side Krylov loops are reported per object by
+ * topo_le_stats.graph_body_launches) */
+long long topo_kernel_launches(void);
 
 /* last error message of the calling thread, and a name for a status code */
 const char *topo_last_error(void);

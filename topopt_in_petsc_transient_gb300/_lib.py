@@ -37,12 +37,14 @@ class LEParams(C.Structure):
         ("dalpha", C.c_double), ("dbeta", C.c_double),
         ("mixed", C.c_int), ("rtol", C.c_double), ("maxit", C.c_int), ("smooth", C.c_int),
         ("cheb_ratio", C.c_double), ("use_graphs", C.c_int),
+        ("coarse_dense_max", C.c_int), ("coarse_smooth", C.c_int), ("sens_fp32", C.c_int),
+        ("inner_tol", C.c_double), ("inner_maxit", C.c_int),
     ]
 
 
 class LEStats(C.Structure):
     _fields_ = [("cg_iterations", C.c_longlong), ("solves", C.c_longlong), ("device_bytes", C.c_double),
-                ("last_fx", C.c_double)]
+                ("last_fx", C.c_double), ("graph_body_launches", C.c_longlong)]
 
 
 EXPORTS = [
@@ -56,9 +58,10 @@ EXPORTS = [
     "topo_pdefilt_create", "topo_pdefilt_destroy", "topo_pdefilt_filter_project", "topo_pdefilt_filter_project_dev",
     "topo_filter_project", "topo_filter_project_dev", "topo_filter_gradients", "topo_filter_gradients_dev",
     "topo_filter_mnd", "topo_filter_mnd_dev",
-    "topo_mma_create", "topo_mma_destroy", "topo_mma_set_asymptotes", "topo_mma_set_outer_movelimit_dev",
+    "topo_mma_create", "topo_mma_destroy", "topo_mma_set_asymptotes", "topo_mma_set_outer_movelimit",
+    "topo_mma_set_outer_movelimit_dev", "topo_mma_design_change",
     "topo_mma_update", "topo_mma_update_dev", "topo_mma_design_change_dev", "topo_mma_kkt_residual_dev",
-    "topo_last_error", "topo_status_str",
+    "topo_kernel_launches", "topo_last_error", "topo_status_str",
 ]
 
 _lib = None
@@ -106,11 +109,14 @@ def load(path=None):
         "topo_mma_create": (ip, [pp, ip, ip, vp, vp, vp]),
         "topo_mma_destroy": (None, [vp]),
         "topo_mma_set_asymptotes": (ip, [vp, d, d, d]),
+        "topo_mma_set_outer_movelimit": (ip, [vp, d, d, d, vp, vp, vp]),
         "topo_mma_set_outer_movelimit_dev": (ip, [vp, d, d, d, vp, vp, vp]),
+        "topo_mma_design_change": (ip, [vp, vp, vp, dp]),
         "topo_mma_update": (ip, [vp, vp, vp, vp, vp, vp, vp]),
         "topo_mma_update_dev": (ip, [vp, vp, vp, vp, vp, vp, vp]),
         "topo_mma_design_change_dev": (ip, [vp, vp, vp, dp]),
         "topo_mma_kkt_residual_dev": (ip, [vp, vp, vp, vp, vp, vp, vp, dp, dp]),
+        "topo_kernel_launches": (C.c_longlong, []),
         "topo_last_error": (C.c_char_p, []),
         "topo_status_str": (C.c_char_p, [ip]),
     }

@@ -95,6 +95,11 @@ void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz) {
     p->smooth = 3;
     p->cheb_ratio = 30.0;
     p->use_graphs = 1;
+    p->coarse_dense_max = 4096;
+    p->coarse_smooth = 8;
+    p->sens_fp32 = 0;
+    p->inner_tol = 1e-4;
+    p->inner_maxit = 40;
 }
 
 int topo_le_create(topo_le **out, const topo_le_params *p) {
@@ -169,6 +174,7 @@ int topo_le_compute_objective_sensitivities(topo_le *le, double *fx, double *dfd
 int topo_le_volume_constraint_dev(topo_le *le, double *gx, double *dgdx_dev, const double *xPhys_dev, double volfrac) {
     if (!le || !gx || !dgdx_dev || !xPhys_dev) return TOPO_ERR_ARG;
     double *gd = le->part + 65535;
+    count_launch();
     k_volume<<<ew_blocks(le->nel), EW>>>(le->nel, xPhys_dev, volfrac, dgdx_dev, Partials<1>{le->part, le->counter}, gd);
     ACK(cudaMemcpy(gx, gd, sizeof(double), cudaMemcpyDeviceToHost));
     return TOPO_OK;
@@ -381,6 +387,29 @@ int topo_mma_set_outer_movelimit_dev(topo_mma *mma, double Xmin, double Xmax, do
     return mma_movelimit_dev(mma->impl, Xmin, Xmax, movlim, x_dev, xmin_dev, xmax_dev);
 }
 
+int topo_mma_set_outer_movelimit(topo_mma *mma, double Xmin, double Xmax, double movlim, const double *x,
+                                 double *xmin, double *xmax) {
+    if (!mma || !x || !xmin || !xmax) return TOPO_ERR_ARG;
+    size_t b = sizeof(double) * (size_t)mma->n;
+    ACK(cudaMemcpy(mma->d_x, x, b, cudaMemcpyHostToDevice));
+    int rc = mma_movelimit_dev(mma->impl, Xmin, Xmax, movlim, mma->d_x, mma->d_lo, mma->d_hi);
+    if (rc) return rc;
+    ACK(cudaMemcpy(xmin, mma->d_lo, b, cudaMemcpyDeviceToHost));
+    ACK(cudaMemcpy(xmax, mma->d_hi, b, cudaMemcpyDeviceToHost));
+    return TOPO_OK;
+}
+
+int topo_mma_design_change(topo_mma *mma, const double *x, double *xold, double *ch) {
+    if (!mma || !x || !xold || !ch) return TOPO_ERR_ARG;
+    size_t b = sizeof(double) * (size_t)mma->n;
+    ACK(cudaMemcpy(mma->d_x, x, b, cudaMemcpyHostToDevice));
+    ACK(cudaMemcpy(mma->d_df, xold, b, cudaMemcpyHostToDevice));
+    int rc = mma_design_change_dev(mma->impl, mma->d_x, mma->d_df, ch);
+    if (rc) return rc;
+    ACK(cudaMemcpy(xold, mma->d_df, b, cudaMemcpyDeviceToHost));
+    return TOPO_OK;
+}
+
 int topo_mma_update_dev(topo_mma *mma, double *xval_dev, const double *dfdx_dev, const double *gx,
                         const double *dgdx_dev, const double *xmin_dev, const double *xmax_dev) {
     if (!mma || !xval_dev || !dfdx_dev || !gx || !dgdx_dev || !xmin_dev || !xmax_dev) return TOPO_ERR_ARG;
@@ -414,6 +443,8 @@ int topo_mma_kkt_residual_dev(topo_mma *mma, const double *x_dev, const double *
         return TOPO_ERR_ARG;
     return mma_kkt_dev(mma->impl, x_dev, dfdx_dev, fx, dgdx_dev, xmin_dev, xmax_dev, norm2, normInf);
 }
+
+long long topo_kernel_launches(void) { return launch_counter(); }
 
 const char *topo_last_error(void) { return last_error(); }
 

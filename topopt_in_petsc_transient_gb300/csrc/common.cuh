@@ -17,6 +17,14 @@
 namespace topo {
 
 // status codes TOPO_OK / TOPO_ERR_* come from the C ABI header
+
+// host-side count of kernel launches issued by this library (one program-wide
+// counter; graph replays are added from their captured kernel counts)
+inline long long &launch_counter() {
+    static long long c = 0;
+    return c;
+}
+inline void count_launch(long long n = 1) { launch_counter() += n; }
 // ---------------------------------------------------------------------------
 // one level of the structured node/element grid
 // ---------------------------------------------------------------------------

@@ -308,6 +308,7 @@ int pdefilt_create(TopoPDEFilt **out, int nx, int ny, int nz, double hx, double 
     }
     KFMat K;
     memcpy(K.v, f->KF, sizeof(K.v));
+    count_launch();
     k_filt_dinv<<<ew_blocks(nn), EW, 0, f->stream>>>(f->g, K, f->dinv);
     e = cudaStreamSynchronize(f->stream);
     if (e != cudaSuccess) {
@@ -337,14 +338,20 @@ static int helmholtz_solve(TopoPDEFilt *f, const double *x_dev) {
     Partials<2> p2{f->part, f->counter};
     KFMat K;
     memcpy(K.v, f->KF, sizeof(K.v));
+    count_launch();
     k_T<<<ew_blocks(nn), EW, 0, s>>>(f->g, f->vol, x_dev, f->rhs);
+    count_launch();
     k_fprime<<<1, 1, 0, s>>>(f->S, f->rtol * f->rtol, f->maxit);
+    count_launch();
     k_fpcg_init<<<ew_blocks(nn), EW, 0, s>>>(nn, f->rhs, f->dinv, f->u, f->r, f->p, f->S, p2);
     FiltScalars h;
     for (int outer = 0; outer < 1000000; outer++) {
         for (int it = 0; it < 8; it++) {
+            count_launch();
             k_filt_apply<<<ew_blocks(nn), EW, 0, s>>>(f->g, K, f->p, f->q, p1, f->S, 1);
+            count_launch();
             k_fpcg_update<<<ew_blocks(nn), EW, 0, s>>>(nn, f->dinv, f->u, f->r, f->p, f->q, f->S, p2);
+            count_launch();
             k_fpcg_p<<<ew_blocks(nn), EW, 0, s>>>(nn, f->dinv, f->r, f->p, f->S);
         }
         FCK(cudaMemcpyAsync(&h, f->S, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -361,6 +368,7 @@ static int helmholtz_solve(TopoPDEFilt *f, const double *x_dev) {
 int pdefilt_apply_dev(TopoPDEFilt *f, const double *x_dev, double *xout_dev) {
     int rc = helmholtz_solve(f, x_dev);
     if (rc) return rc;
+    count_launch();
     k_Tt<<<ew_blocks(f->g.nel()), EW, 0, f->stream>>>(f->g, f->u, xout_dev, nullptr, 0, 0, 0.0, 0.0);
     FCK(cudaStreamSynchronize(f->stream));
     return TOPO_OK;
@@ -370,6 +378,7 @@ int filter_project_dev(TopoPDEFilt *f, const double *x_dev, double *xTilde_dev, 
                        double beta, double eta) {
     int rc = helmholtz_solve(f, x_dev);
     if (rc) return rc;
+    count_launch();
     k_Tt<<<ew_blocks(f->g.nel()), EW, 0, f->stream>>>(f->g, f->u, xTilde_dev, xPhys_dev, 1, projection, beta, eta);
     FCK(cudaStreamSynchronize(f->stream));
     return TOPO_OK;
@@ -378,8 +387,10 @@ int filter_project_dev(TopoPDEFilt *f, const double *x_dev, double *xTilde_dev, 
 int filter_gradients_dev(TopoPDEFilt *f, const double *xTilde_dev, double *dfdx_dev, int m, double *dgdx_dev,
                          int projection, double beta, double eta) {
     long long nel = f->g.nel();
-    if (projection)
+    if (projection) {
+        count_launch();
         k_chain<<<ew_blocks(nel), EW, 0, f->stream>>>(nel, xTilde_dev, dfdx_dev, m, dgdx_dev, beta, eta);
+    }
     // PDEFilt::Gradients == FilterProject (PDEFilter.cc:224); in place via scratch
     FCK(cudaMemcpyAsync(f->e1, dfdx_dev, sizeof(double) * nel, cudaMemcpyDeviceToDevice, f->stream));
     int rc = pdefilt_apply_dev(f, f->e1, dfdx_dev);
@@ -396,6 +407,7 @@ int filter_gradients_dev(TopoPDEFilt *f, const double *xTilde_dev, double *dfdx_
 int filter_mnd_dev(TopoPDEFilt *f, const double *x_dev, double *mnd) {
     long long nel = f->g.nel();
     Partials<1> p1{f->part, f->counter};
+    count_launch();
     k_mnd<<<ew_blocks(nel), EW, 0, f->stream>>>(nel, x_dev, p1, f->e2);
     FCK(cudaMemcpyAsync(mnd, f->e2, sizeof(double), cudaMemcpyDeviceToHost, f->stream));
     FCK(cudaStreamSynchronize(f->stream));

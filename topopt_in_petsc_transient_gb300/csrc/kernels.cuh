@@ -360,6 +360,52 @@ static __global__ void k_fcg_update(long long ndof, double *x, double *r, float 
     }
 }
 
+// mixed-precision FCG pieces (FP32 vectors, FP64 scalars and iterate)
+static __global__ void k_mfcg_dot(long long ndof, const float *__restrict__ z, const float *__restrict__ r32,
+                                  const float *__restrict__ q32, SolveScalars *S, Partials<2> part) {
+    double v[2] = {0.0, 0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        double zi = (double)z[i];
+        v[0] += zi * (double)r32[i];
+        v[1] += zi * (double)q32[i];
+    }
+    double tot[2];
+    if (grid_reduce<EW, 2>(v, part, tot)) {
+        S->rho = tot[0];
+        S->gam = tot[1];
+        S->beta = S->restart ? 0.0 : -tot[1] / S->pq;
+        if (!isfinite(S->beta)) S->beta = 0.0;
+    }
+}
+
+static __global__ void k_mfcg_p(long long ndof, const float *__restrict__ z, float *p, const SolveScalars *S) {
+    float beta = (float)S->beta;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)
+        p[i] = (beta == 0.0f) ? z[i] : z[i] + beta * p[i];
+}
+
+static __global__ void k_mfcg_update(long long ndof, double *x, float *r32, const float *__restrict__ p,
+                                     const float *__restrict__ q, SolveScalars *S, Partials<1> part) {
+    double alpha = S->alpha;
+    float af = (float)alpha;
+    double v[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        x[i] += alpha * (double)p[i];
+        float rv = r32[i] - af * q[i];
+        r32[i] = rv;
+        v[0] += (double)rv * (double)rv;
+    }
+    double tot[1];
+    if (grid_reduce<EW, 1>(v, part, tot)) {
+        S->it += 1;
+        S->total_it += 1;
+        S->inner_it += 1;
+        S->restart = 0;
+        if (!isfinite(tot[0]) || tot[0] <= S->tau2 * S->rr_ref || S->inner_it >= S->kmax || S->it >= S->maxit)
+            S->need_replace = 1;
+    }
+}
+
 static __global__ void k_fcg_zero_x(long long ndof, double *x, const SolveScalars *S) {
     if (!S->zero_x) return;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)

@@ -131,6 +131,7 @@ static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol
         cudaFuncSetAttribute(k_tile<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         attr = true;
     }
+    count_launch();
     k_tile<T, Pol><<<tile_grid(g), TILE_THREADS, sm, s>>>(g, C, pol);
 }
 
@@ -189,7 +190,8 @@ struct TopoLE {
     double *df = nullptr;
     // solver vectors
     double *sx = nullptr, *sb = nullptr, *sr = nullptr, *sp = nullptr, *sq = nullptr, *sz = nullptr;
-    float *sr32 = nullptr;
+    float *sr32 = nullptr, *sp32 = nullptr, *sq32 = nullptr;
+    int coarse_dense = 1;
     // coarse assembly scratch
     double *KEc = nullptr, *MEc = nullptr, *Acoarse = nullptr, *gj_row = nullptr, *gj_col = nullptr;
     int ncoarse = 0;
@@ -201,6 +203,7 @@ struct TopoLE {
     unsigned long long *bbits = nullptr;
     int *err = nullptr;
     long long nsolves = 0;
+    long long step_kernels[2] = {0, 0}, body_kernels = 0, direct_iters = 0;
     // graphs
     cudaGraphExec_t gx_fwd = nullptr, gx_adj = nullptr;
     int graphs_ok = 0;
@@ -293,6 +296,8 @@ int le_alloc(TopoLE *le) {
     AG(le->sq, nd);
     AG(le->sz, nd);
     AG(le->sr32, nd);
+    AG(le->sp32, nd);
+    AG(le->sq32, nd);
     AG(le->S, 1);
     AG(le->st, 1);
     AG(le->part, 4 * 65536);
@@ -348,6 +353,7 @@ int le_alloc(TopoLE *le) {
     }
     CK(cudaMemcpy(le->rhs0, rhs0.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(le->P, P.data(), sizeof(double) * ne, cudaMemcpyHostToDevice));
+    count_launch();
     k_count_region<<<ew_blocks(nn), EW, 0, le->stream>>>(le->g, le->P, le->cntP);
 
     // ---- multigrid levels ----
@@ -395,10 +401,9 @@ int le_alloc(TopoLE *le) {
         AG(lv.dr, lnd);
         if (l == le->nlev - 1) {
             le->ncoarse = (int)lnd;
-            if (le->ncoarse > 12288) {
-                set_error("coarsest multigrid level too large for the dense solve; increase nlvls");
-                return TOPO_ERR_ARG;
-            }
+            le->coarse_dense = (lnd <= (long long)p.coarse_dense_max) && lnd <= 12288;
+        }
+        if (l == le->nlev - 1 && le->coarse_dense) {
             AG(le->KEc, 576);
             AG(le->MEc, 576);
             CK(cudaMemcpy(le->KEc, KE, sizeof(KE), cudaMemcpyHostToDevice));
@@ -429,8 +434,10 @@ int le_alloc(TopoLE *le) {
             AG(op.lv[l].dinvf, lnd);
             AG(op.lv[l].lohi, 2);
         }
-        AG(op.Ainv_d, (size_t)le->ncoarse * le->ncoarse);
-        AG(op.Ainv_f, (size_t)le->ncoarse * le->ncoarse);
+        if (le->coarse_dense) {
+            AG(op.Ainv_d, (size_t)le->ncoarse * le->ncoarse);
+            AG(op.Ainv_f, (size_t)le->ncoarse * le->ncoarse);
+        }
     }
     CK(cudaStreamSynchronize(le->stream));
     le->stats.device_bytes = (double)arena.bytes;
@@ -455,23 +462,35 @@ static int setup_operator(TopoLE *le, int o) {
     for (int l = 0; l < le->nlev; l++) {
         Level &lv = le->L[l];
         const double *kfp = (op.sK != 0.0) ? lv.kfd : nullptr;
+        count_launch();
         k_dinv<<<ew_blocks(lv.g.nn()), EW, 0, s>>>(lv.g, lv.fixed, kfp, lv.mfd, op.sK, op.sM, lv.dK[0], lv.dK[1],
                                                    lv.dK[2], lv.dM, op.lv[l].dinvd, op.lv[l].dinvf);
+        count_launch();
         k_bounds_init<<<1, 1, 0, s>>>(le->bbits);
+        count_launch();
         k_bounds<<<ew_blocks(lv.g.nel()), EW, 0, s>>>(lv.g.nel(), kfp, lv.mfd, op.sK, op.sM, lv.dK[0], lv.dK[1],
                                                       lv.dK[2], lv.dM, lv.lamK, 0.125, 3.375, le->bbits);
+        count_launch();
         k_bounds_final<<<1, 1, 0, s>>>(le->bbits, le->p.cheb_ratio, op.lv[l].lohi);
     }
     // dense coarsest operator and its inverse (FP64 Gauss-Jordan)
+    if (!le->coarse_dense) {
+        CK(cudaGetLastError());
+        return TOPO_OK;
+    }
     Level &lc = le->L[le->nlev - 1];
     int n = le->ncoarse;
     const double *kfp = (op.sK != 0.0) ? lc.kfd : nullptr;
+    count_launch();
     k_coarse_assemble<<<ew_blocks((long long)n * n), EW, 0, s>>>(lc.g, lc.fixed, kfp, lc.mfd, op.sK, op.sM, le->KEc,
                                                                  le->MEc, op.Ainv_d);
     for (int k = 0; k < n; k++) {
+        count_launch();
         k_gj_save<<<(n + EW - 1) / EW, EW, 0, s>>>(op.Ainv_d, n, k, le->gj_row, le->gj_col);
+        count_launch();
         k_gj_update<<<ew_blocks((long long)n * n), EW, 0, s>>>(op.Ainv_d, n, k, le->gj_row, le->gj_col);
     }
+    count_launch();
     k_d2f<<<ew_blocks((long long)n * n), EW, 0, s>>>((long long)n * n, op.Ainv_d, op.Ainv_f);
     CK(cudaGetLastError());
     return TOPO_OK;
@@ -513,15 +532,30 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b) {
     VW<T> w = vw<T>(le, o, l);
     Operator &op = le->ops[o];
     long long nd = 3 * lv.g.nn();
-    if (l == le->nlev - 1) {
-        int n = le->ncoarse;
-        k_gemv<T><<<(n * 32 + 255) / 256, 256, 0, s>>>(n, ainv<T>(le, o), b, w.xa);
-        return w.xa;
-    }
     Weights<T> wt{op.sK != 0.0 ? w.kf : nullptr, w.mf, nullptr, (T)op.sK, (T)op.sM};
     const double *lohi = op.lv[l].lohi;
-    const int nu = le->p.smooth;
     T *x = w.xa, *xo = w.xb;
+    if (l == le->nlev - 1) {
+        if (le->coarse_dense) {
+            int n = le->ncoarse;
+            count_launch();
+            k_gemv<T><<<(n * 32 + 255) / 256, 256, 0, s>>>(n, ainv<T>(le, o), b, w.xa);
+            return w.xa;
+        }
+        // iterative coarse solve: Chebyshev-Jacobi polynomial from zero
+        count_launch();
+        k_cheb0<T><<<ew_blocks(nd), EW, 0, s>>>(nd, b, w.dinv, lohi, x, w.d);
+        for (int k = 1; k < le->p.coarse_smooth; k++) {
+            PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, lohi, k, {}};
+            launch_tile<T>(lv.g, *w.C, pc, s);
+            T *t = x;
+            x = xo;
+            xo = t;
+        }
+        return x;
+    }
+    const int nu = le->p.smooth;
+    count_launch();
     k_cheb0<T><<<ew_blocks(nd), EW, 0, s>>>(nd, b, w.dinv, lohi, x, w.d);
     for (int k = 1; k < nu; k++) {
         PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, lohi, k, {}};
@@ -534,8 +568,10 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b) {
     launch_tile<T>(lv.g, *w.C, pr, s);
     Level &lc = le->L[l + 1];
     VW<T> wc = vw<T>(le, o, l + 1);
+    count_launch();
     k_restrict<T><<<ew_blocks(lc.g.nn()), EW, 0, s>>>(lv.g, lc.g, lc.fixed, w.r, wc.b);
     T *xc = vcycle<T>(le, o, l + 1, wc.b);
+    count_launch();
     k_prolong<T><<<ew_blocks(lv.g.nn()), EW, 0, s>>>(lv.g, lc.g, lv.fixed, xc, x);
     for (int k = 0; k < nu; k++) {
         PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, lohi, k, {}};
@@ -550,9 +586,11 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b) {
 // ---------------------------------------------------------------------------
 // flexible CG:  (N A N + I - N) x = b for operator o; sx holds the initial guess
 // ---------------------------------------------------------------------------
-__global__ void k_solve_prime(SolveScalars *S, double tol2, int maxit) {
+__global__ void k_solve_prime(SolveScalars *S, double tol2, int maxit, double tau2, int kmax) {
     S->tol2 = tol2;
     S->maxit = maxit;
+    S->tau2 = tau2;
+    S->kmax = kmax;
     S->done = 0;
     S->status = 0;
     S->it = 0;
@@ -561,13 +599,22 @@ __global__ void k_solve_check(const SolveScalars *S, int *err) {
     if (S->status != 0 && *err == 0) *err = S->status;
 }
 
+static const double *&cur_b(TopoLE *le);
 static void solve_init(TopoLE *le, int o, const double *b, cudaGraphConditionalHandle cond, int has_cond) {
+    cur_b(le) = b;
     Level &l0 = le->L[0];
     Operator &op = le->ops[o];
     Weights<double> wt{op.sK != 0.0 ? l0.kfd : nullptr, l0.mfd, nullptr, op.sK, op.sM};
     PolInitResid<double> pi{l0.fixed, wt, le->sx, b, le->sr, le->p.mixed ? le->sr32 : nullptr,
                             le->S, cond, has_cond, P2(le)};
     launch_tile<double>(l0.g, l0.Cd, pi, le->stream);
+}
+
+// right-hand side of the solve in flight (set by solve_init)
+static const double *&cur_b(TopoLE *le) {
+    static thread_local const double *b = nullptr;
+    (void)le;
+    return b;
 }
 
 static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, int has_cond) {
@@ -577,24 +624,41 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
     long long nd = le->ndof;
     unsigned nb = ew_blocks(nd);
     if (le->p.mixed) {
+        // reliable-update mixed precision: FP32 recurrence, FP64 replacements
         float *z = vcycle<float>(le, o, 0, le->sr32);
-        k_fcg_dot<float><<<nb, EW, 0, s>>>(nd, z, le->sr, le->sq, le->S, P2(le));
-        k_fcg_p<float><<<nb, EW, 0, s>>>(nd, z, le->sp, le->S);
+        count_launch();
+        k_mfcg_dot<<<nb, EW, 0, s>>>(nd, z, le->sr32, le->sq32, le->S, P2(le));
+        count_launch();
+        k_mfcg_p<<<nb, EW, 0, s>>>(nd, z, le->sp32, le->S);
+        Weights<float> wf{op.sK != 0.0 ? l0.kff : nullptr, l0.mff, nullptr, (float)op.sK, (float)op.sM};
+        PolPQ32 pq32{l0.fixed, wf, le->sp32, le->sq32, le->S, P1(le)};
+        launch_tile<float>(l0.g, l0.Cf, pq32, s);
+        count_launch();
+        k_mfcg_update<<<nb, EW, 0, s>>>(nd, le->sx, le->sr32, le->sp32, le->sq32, le->S, P1(le));
+        Weights<double> wd{op.sK != 0.0 ? l0.kfd : nullptr, l0.mfd, nullptr, op.sK, op.sM};
+        PolReplace rp{l0.fixed, wd, le->sx, cur_b(le), le->sr, le->sr32, le->S, cond, has_cond, P1(le)};
+        launch_tile<double>(l0.g, l0.Cd, rp, s);
+        return;
     } else {
         double *z = vcycle<double>(le, o, 0, le->sr);
+        count_launch();
         k_fcg_dot<double><<<nb, EW, 0, s>>>(nd, z, le->sr, le->sq, le->S, P2(le));
+        count_launch();
         k_fcg_p<double><<<nb, EW, 0, s>>>(nd, z, le->sp, le->S);
     }
     Weights<double> wt{op.sK != 0.0 ? l0.kfd : nullptr, l0.mfd, nullptr, op.sK, op.sM};
     PolPQ<double> pq{l0.fixed, wt, le->sp, le->sq, le->S, P1(le)};
     launch_tile<double>(l0.g, l0.Cd, pq, s);
+    count_launch();
     k_fcg_update<<<nb, EW, 0, s>>>(nd, le->sx, le->sr, le->p.mixed ? le->sr32 : nullptr, le->sp, le->sq, le->S,
                                    P1(le), cond, has_cond);
 }
 
 // direct launches, host checks convergence after every iteration
 static int solve_direct(TopoLE *le, int o, const double *b) {
-    k_solve_prime<<<1, 1, 0, le->stream>>>(le->S, le->p.rtol * le->p.rtol, le->p.maxit);
+    count_launch();
+    k_solve_prime<<<1, 1, 0, le->stream>>>(le->S, le->p.rtol * le->p.rtol, le->p.maxit,
+                                              le->p.inner_tol * le->p.inner_tol, le->p.inner_maxit);
     solve_init(le, o, b, 0, 0);
     SolveScalars h;
     for (;;) {
@@ -602,8 +666,11 @@ static int solve_direct(TopoLE *le, int o, const double *b) {
         CK(cudaStreamSynchronize(le->stream));
         if (h.done) break;
         solve_iteration(le, o, 0, 0);
+        le->direct_iters++;
     }
+    count_launch();
     k_fcg_zero_x<<<ew_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, le->sx, le->S);
+    count_launch();
     k_solve_check<<<1, 1, 0, le->stream>>>(le->S, le->err);
     le->nsolves++;
     CK(cudaGetLastError());
@@ -614,7 +681,9 @@ static int solve_direct(TopoLE *le, int o, const double *b) {
 // body is the iteration; the device sets the condition after each iteration
 static int solve_captured(TopoLE *le, int o, const double *b) {
     cudaStream_t s = le->stream;
-    k_solve_prime<<<1, 1, 0, s>>>(le->S, le->p.rtol * le->p.rtol, le->p.maxit);
+    count_launch();
+    k_solve_prime<<<1, 1, 0, s>>>(le->S, le->p.rtol * le->p.rtol, le->p.maxit, le->p.inner_tol * le->p.inner_tol,
+                                  le->p.inner_maxit);
     cudaStreamCaptureStatus cs;
     cudaGraph_t graph;
     const cudaGraphNode_t *deps = nullptr;
@@ -637,13 +706,17 @@ static int solve_captured(TopoLE *le, int o, const double *b) {
     CK(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
     CK(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     le->stream = bs;
+    long long c0 = launch_counter();
     solve_iteration(le, o, h, 1);
+    le->body_kernels = launch_counter() - c0;
     le->stream = s;
     cudaGraph_t outg;
     cudaError_t e1 = cudaStreamEndCapture(bs, &outg);
     cudaStreamDestroy(bs);
     CK(e1);
+    count_launch();
     k_fcg_zero_x<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->S);
+    count_launch();
     k_solve_check<<<1, 1, 0, s>>>(le->S, le->err);
     return TOPO_OK;
 }
@@ -696,7 +769,9 @@ static int fwd_step(TopoLE *le, bool capturing) {
     if (rc) return rc;
     Newmark nm;
     memcpy(nm.a, le->a, sizeof(nm.a));
+    count_launch();
     k_newmark<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh, le->DUh, le->DDUh, nm);
+    count_launch();
     k_step_add<<<1, 1, 0, s>>>(le->st, +1);
     return TOPO_OK;
 }
@@ -735,6 +810,7 @@ static void objective_products(TopoLE *le, int t0mode) {
     double dt = le->dt;
     // stage the needed state vectors into the solver scratch (sp, sq are free here)
     bool needU = (obj == 3 || obj == 5), needDU = (obj >= 4);
+    count_launch();
     k_select_state<<<ew_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, le->st, le->Uh, le->DUh, t0mode, le->cp,
                                                                  needU ? le->sp : nullptr, needDU ? le->sq : nullptr);
     if (obj == 3) product<true, false>(le, le->sp, le->hK, le->P, dt, 0.0);
@@ -833,7 +909,11 @@ static SensArgs sens_args(TopoLE *le, int t0mode) {
 
 template <int OBJ>
 static void launch_sens_obj(TopoLE *le, const SensArgs &S) {
-    k_sens<OBJ, double><<<ew_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cd);
+    count_launch();
+    if (le->p.mixed && le->p.sens_fp32)
+        k_sens<OBJ, float><<<ew_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cf);
+    else
+        k_sens<OBJ, double><<<ew_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cd);
 }
 static void launch_sens(TopoLE *le, int t0mode) {
     SensArgs S = sens_args(le, t0mode);
@@ -854,11 +934,14 @@ static int adj_step(TopoLE *le, bool capturing) {
     product<true, false>(le, le->Lp1, le->KL, nullptr, 1.0, 0.0);
     product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
     objective_products(le, 0);
+    count_launch();
     k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 0));
     int rc = solve(le, 0, le->sb, capturing);
     if (rc) return rc;
     launch_sens(le, 0);
+    count_launch();
     k_adj_advance<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->DLc, le->DDLc, le->Lp1, le->DLp1, le->DDLp1);
+    count_launch();
     k_step_add<<<1, 1, 0, s>>>(le->st, -1);
     return TOPO_OK;
 }
@@ -868,10 +951,12 @@ static int lagrange0(TopoLE *le) {
     product<true, false>(le, le->Lp1, le->KL, nullptr, 1.0, 0.0);
     product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
     objective_products(le, 1);
+    count_launch();
     k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 1));
     int rc = solve(le, 1, le->sb, false);
     if (rc) return rc;
     launch_sens(le, 1);
+    count_launch();
     k_copy<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->DDL0);
     return TOPO_OK;
 }
@@ -881,7 +966,11 @@ static int get_graph(TopoLE *le, int adjoint, cudaGraphExec_t *out) {
     cudaGraphExec_t &gx = adjoint ? le->gx_adj : le->gx_fwd;
     if (!gx) {
         CK(cudaStreamBeginCapture(le->stream, cudaStreamCaptureModeRelaxed));
+        long long c0 = launch_counter();
         int rc = adjoint ? adj_step(le, true) : fwd_step(le, true);
+        long long captured = launch_counter() - c0;
+        launch_counter() -= captured;  // capturing is not launching: counted per replay
+        le->step_kernels[adjoint] = captured - le->body_kernels;
         cudaGraph_t g;
         cudaError_t e = cudaStreamEndCapture(le->stream, &g);
         if (rc) return rc;
@@ -896,6 +985,7 @@ static int get_graph(TopoLE *le, int adjoint, cudaGraphExec_t *out) {
 
 static int run_block(TopoLE *le, int c, int adjoint) {
     const int tsc = le->p.tsc;
+    count_launch();
     k_step_set<<<1, 1, 0, le->stream>>>(le->st, c, adjoint ? tsc - 1 : 0);
     if (le->p.use_graphs) {
         cudaGraphExec_t gx;
@@ -903,6 +993,7 @@ static int run_block(TopoLE *le, int c, int adjoint) {
         if (rc) return rc;
         for (int j = 0; j < tsc; j++) CK(cudaGraphLaunch(gx, le->stream));
         le->nsolves += tsc;
+        count_launch((long long)tsc * le->step_kernels[adjoint]);
     } else {
         for (int j = 0; j < tsc; j++) {
             int rc = adjoint ? adj_step(le, false) : fwd_step(le, false);
@@ -946,12 +1037,15 @@ int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, 
     const LEParams &p = le->p;
     CK(cudaMemcpyAsync(le->xPhys, xPhys_dev, sizeof(double) * le->nel, cudaMemcpyDeviceToDevice, s));
     MatParams mp{p.sInt, p.mInt, Emin, Emax, penalK, Rmin, Rmax, penalM};
+    count_launch();
     k_interp<<<ew_blocks(le->nel), EW, 0, s>>>(le->nel, le->xPhys, mp, le->kf, le->dkf, le->mf, le->dmf, le->L[0].kff,
                                                le->L[0].mff);
-    for (int l = 1; l < le->nlev; l++)
+    for (int l = 1; l < le->nlev; l++) {
+        count_launch();
         k_coarsen<<<ew_blocks(le->L[l].g.nel()), EW, 0, s>>>(le->L[l - 1].g, le->L[l].g, le->L[l - 1].kfd,
                                                              le->L[l - 1].mfd, le->L[l].kfd, le->L[l].mfd,
                                                              le->L[l].kff, le->L[l].mff);
+    }
     int rc = setup_operator(le, 0);
     if (rc) return rc;
     rc = setup_operator(le, 1);
@@ -973,10 +1067,12 @@ int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, 
         }
         s0 /= (p.ny - 1);
     }
+    count_launch();
     k_init_accel_rhs<<<ew_blocks(le->nn), EW, 0, s>>>(le->nn, le->L[0].fixed, le->rhs0, s0, le->KL, le->ML, le->sb);
     CK(cudaMemsetAsync(le->sx, 0, sizeof(double) * nd, s));
     rc = solve(le, 1, le->sb, false);
     if (rc) return rc;
+    count_launch();
     k_copy<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sx, le->cp + 2 * nd);
     rc = check_err(le);
     if (rc) return rc;
@@ -1072,6 +1168,7 @@ int le_stats(TopoLE *le, LEStats *out) {
     CK(cudaStreamSynchronize(le->stream));
     le->stats.cg_iterations = h.total_it;
     le->stats.solves = le->nsolves;
+    le->stats.graph_body_launches = (h.total_it - le->direct_iters) * le->body_kernels;
     *out = le->stats;
     return TOPO_OK;
 }
@@ -1097,7 +1194,9 @@ int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms) {
     Level &l0 = le->L[0];
     Operator &op = le->ops[0];
     long long nd = le->ndof;
+    count_launch();
     k_fill<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sp, 1.0);
+    count_launch();
     k_d2f<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sp, l0.fr);
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));

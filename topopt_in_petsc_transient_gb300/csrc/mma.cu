@@ -395,6 +395,7 @@ int mma_set_asymptotes(TopoMMA *mm, double init, double dec, double inc) {
 
 int mma_movelimit_dev(TopoMMA *mm, double Xmin, double Xmax, double movlim, const double *x, double *xmin,
                       double *xmax) {
+    count_launch();
     k_mma_movelimit<<<ew_blocks(mm->n), EW, 0, mm->stream>>>(mm->n, Xmin, Xmax, movlim, x, xmin, xmax);
     MCK(cudaStreamSynchronize(mm->stream));
     return TOPO_OK;
@@ -407,17 +408,21 @@ static int solve_dip(TopoMMA *mm, double *x) {
     unsigned nb = ew_blocks(n);
     Partials<M + M * M> pgh{mm->part, mm->counter};
     Partials<M> pr{mm->part, mm->counter};
+    count_launch();
     k_mma_dual_init<<<1, 1, 0, s>>>(mm->S);
     double epsi = 1.0, err = 1.0;
     const double tol = 1.0e-9 * sqrt((double)(mm->m + mm->n));
     // SolveDIP loop structure (MMA.cc:651-674)
+    count_launch();
     k_mma_yz<<<1, 1, 0, s>>>(mm->S);
     while (epsi > tol) {
         int loop = 0;
         while (err > 0.9 * epsi && loop < 100) {
             loop++;
+            count_launch();
             k_mma_gradhess<M><<<nb, EW, 0, s>>>(n, x, mm->p0, mm->q0, mm->pij, mm->qij, mm->L, mm->U, mm->alpha,
                                                 mm->beta, mm->S, pgh);
+            count_launch();
             k_mma_resid<M><<<nb, EW, 0, s>>>(n, x, mm->p0, mm->q0, mm->pij, mm->qij, mm->L, mm->U, mm->alpha,
                                              mm->beta, mm->S, pr);
             MCK(cudaMemcpyAsync(&err, &mm->S->err, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -444,8 +449,10 @@ int mma_update_dev(TopoMMA *mm, double *xval, const double *dfdx, const double *
     memset(&g, 0, sizeof(g));
     for (int j = 0; j < mm->m; j++) g.v[j] = gx[j];
     Partials<MMA_MAXM> pb{mm->part, mm->counter};
+    count_launch();
     k_mma_gensub<<<ew_blocks(n), EW, 0, s>>>(n, mm->m, xval, dfdx, dgdx, xmin, xmax, mm->L, mm->U, mm->xo1, mm->xo2,
                                              mm->alpha, mm->beta, mm->p0, mm->q0, mm->pij, mm->qij, mm->S, g, pb);
+    count_launch();
     k_mma_shift<<<ew_blocks(n), EW, 0, s>>>(n, xval, mm->xo1, mm->xo2);
     int rc = (mm->m == 1) ? solve_dip<1>(mm, xval) : solve_dip<2>(mm, xval);
     if (rc) return rc;
@@ -455,6 +462,7 @@ int mma_update_dev(TopoMMA *mm, double *xval, const double *dfdx, const double *
 
 int mma_design_change_dev(TopoMMA *mm, const double *x, double *xold, double *ch) {
     MCK(cudaMemsetAsync(mm->bits, 0, sizeof(unsigned long long), mm->stream));
+    count_launch();
     k_mma_change<<<ew_blocks(mm->n), EW, 0, mm->stream>>>(mm->n, x, xold, mm->bits);
     unsigned long long b = 0;
     MCK(cudaMemcpyAsync(&b, mm->bits, sizeof(b), cudaMemcpyDeviceToHost, mm->stream));
@@ -471,6 +479,7 @@ int mma_kkt_dev(TopoMMA *mm, const double *x, const double *dfdx, const double *
     MCK(cudaMemsetAsync(mm->bits, 0, sizeof(unsigned long long), s));
     double *n2d = mm->part + 8 * 65536 - 1;
     Partials<1> p1{mm->part, mm->counter};
+    count_launch();
     k_mma_kkt<<<ew_blocks(mm->n), EW, 0, s>>>(mm->n, mm->m, x, dfdx, dgdx, xmin, xmax, mm->S, p1, mm->bits, n2d);
     unsigned long long b = 0;
     double n2 = 0.0;

@@ -27,6 +27,10 @@ struct SolveScalars {
     int done;         // 1 once converged / failed: later body kernels return
     int zero_x;       // rhs was exactly zero: solution is zero
     int total_it;     // accumulated iterations over all solves (diagnostics)
+    // reliable-update mixed precision (FP32 recurrence, FP64 replacements)
+    double rr_ref, tau2;
+    int need_replace, restart, inner_it, kmax;
+    int replacements, breakdowns32;
 };
 
 // ---------------------------------------------------------------------------
@@ -86,6 +90,10 @@ struct PolInitResid {
         S->status = 0;
         S->zero_x = (t[0] == 0.0);
         S->done = (t[0] == 0.0) || (t[1] <= S->tol2 * t[0]);
+        S->rr_ref = t[1];
+        S->need_replace = 0;
+        S->restart = 1;
+        S->inner_it = 0;
         if (!isfinite(t[1])) {
             S->status = TOPO_ERR_NAN;
             S->done = 1;
@@ -132,6 +140,103 @@ struct PolPQ {
         } else {
             S->alpha = S->rho / t[0];
         }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Mixed precision (reliable updates): the Krylov recurrence runs on FP32
+// vectors with the FP32 operator; FP64 is used for the iterate x, the dot
+// products and the true residual r = b - A x, recomputed ("replaced") with
+// the FP64 operator whenever the FP32 recurrence residual has dropped by
+// inner_tol or after inner_maxit iterations.  Convergence is decided on the
+// FP64 residual only, so the tolerance means the same as in the plain path.
+// ---------------------------------------------------------------------------
+struct PolPQ32 {
+    static constexpr int NIN = 1, NRED = 1;
+    static constexpr bool HAS_K = true, HAS_M = true;
+    const uint8_t *fixed;
+    Weights<float> w;
+    const float *p;
+    float *q;
+    SolveScalars *S;
+    Partials<1> part;
+    __device__ void load(long long n, float v[1][3]) const {
+        v[0][0] = p[3 * n];
+        v[0][1] = p[3 * n + 1];
+        v[0][2] = p[3 * n + 2];
+        mask3(fixed[n], v[0]);
+    }
+    __device__ void coef(long long e, float &ck, float &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const float y[3], double red[1]) const {
+        uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) {
+            float pv = p[3 * n + c];
+            float qv = ((f >> c) & 1) ? pv : y[c];
+            q[3 * n + c] = qv;
+            red[0] += (double)pv * (double)qv;
+        }
+    }
+    __device__ void finish(const double t[1]) const {
+        S->pq = t[0];
+        if (!(t[0] > 0.0) || !isfinite(t[0])) {
+            S->alpha = 0.0;  // FP32 breakdown: restart from the true residual
+            S->need_replace = 1;
+            S->breakdowns32 += 1;
+        } else {
+            S->alpha = S->rho / t[0];
+        }
+    }
+};
+
+// r = b - (N A N + I - N) x in FP64, r32 = (float) r; runs only when a
+// replacement is due; decides convergence and drives the graph condition
+struct PolReplace {
+    static constexpr int NIN = 1, NRED = 1;
+    static constexpr bool HAS_K = true, HAS_M = true;
+    const uint8_t *fixed;
+    Weights<double> w;
+    const double *x, *b;
+    double *r;
+    float *r32;
+    SolveScalars *S;
+    cudaGraphConditionalHandle cond;
+    int has_cond;
+    Partials<1> part;
+    __device__ bool skip() const { return S->need_replace == 0; }
+    __device__ void load(long long n, double v[1][3]) const {
+        v[0][0] = x[3 * n];
+        v[0][1] = x[3 * n + 1];
+        v[0][2] = x[3 * n + 2];
+        mask3(fixed[n], v[0]);
+    }
+    __device__ void coef(long long e, double &ck, double &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const double y[3], double red[1]) const {
+        uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) {
+            double xv = x[3 * n + c];
+            double rv = b[3 * n + c] - (((f >> c) & 1) ? xv : y[c]);
+            r[3 * n + c] = rv;
+            r32[3 * n + c] = (float)rv;
+            red[0] += rv * rv;
+        }
+    }
+    __device__ void finish(const double t[1]) const {
+        S->rr = t[0];
+        S->rr_ref = t[0];
+        S->need_replace = 0;
+        S->restart = 1;
+        S->inner_it = 0;
+        S->replacements += 1;
+        if (!isfinite(t[0])) {
+            S->status = TOPO_ERR_NAN;
+            S->done = 1;
+        } else if (t[0] <= S->tol2 * S->bb) {
+            S->done = 1;
+        } else if (S->it >= S->maxit) {
+            S->status = TOPO_ERR_NOT_CONVERGED;
+            S->done = 1;
+        }
+        if (has_cond) cudaGraphSetConditional(cond, S->done ? 0u : 1u);
     }
 };
 

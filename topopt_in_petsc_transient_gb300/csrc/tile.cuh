@@ -45,13 +45,25 @@ __host__ inline dim3 tile_grid(const GridDesc &g) {
 //   __device__ void epilogue(long long n, int i, int j, int k, const T y[3], double red[]) const;
 //   __device__ void finish(const double tot[]) const;   (thread 0 of last CTA)
 //   Partials<NRED> part;  (when NRED > 0)
+// optional early exit: a policy may define `bool skip() const` (read by every
+// thread before any shared-memory or reduction work, so the whole grid exits)
+template <class P>
+__device__ __forceinline__ auto pol_skip(const P &p, int) -> decltype(p.skip()) {
+    return p.skip();
+}
+template <class P>
+__device__ __forceinline__ bool pol_skip(const P &, long) {
+    return false;
+}
+
 template <class T, class Pol>
-__global__ void __launch_bounds__(TILE_THREADS, 1) k_tile(const GridDesc g, const ElemConst<T> C, const Pol pol) {
+__global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(const GridDesc g, const ElemConst<T> C, const Pol pol) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sIn = reinterpret_cast<T *>(smem_raw);
     T *sEl = sIn + Pol::NIN * TILE_STAGED * 3;
     const int tid = threadIdx.x;
     const int i0 = blockIdx.x * TILE, j0 = blockIdx.y * TILE, k0 = blockIdx.z * TILE;
+    if (pol_skip(pol, 0)) return;
 
     // ---- stage inputs (brick + halo), zero outside the domain ----
     for (int s = tid; s < TILE_STAGED; s += TILE_THREADS) {

@@ -59,6 +59,11 @@ class TopOpt:
     smooth: int = 3
     cheb_ratio: float = 30.0
     use_graphs: bool = True
+    coarse_dense_max: int = 4096
+    coarse_smooth: int = 8
+    sens_fp32: bool = False
+    inner_tol: float = 1e-4
+    inner_maxit: int = 40
     # state
     fscale: float = 1.0
     itr: int = 0
@@ -98,7 +103,9 @@ class TopOpt:
             ti=self.ti, objective=self.objective, stiffnessInterpolation=self.sInt, massInterpolation=self.mInt,
             boundaries=self.boundaries, loadloc=self.loadloc, dalpha=self.dalpha, dbeta=self.dbeta,
             optimizationRegion=self.optimizationRegion, h=self.h, loadsignal=self.loadsignal, mixed=self.mixed,
-            rtol=self.rtol, smooth=self.smooth, cheb_ratio=self.cheb_ratio, use_graphs=self.use_graphs)
+            rtol=self.rtol, smooth=self.smooth, cheb_ratio=self.cheb_ratio, use_graphs=self.use_graphs,
+            coarse_dense_max=self.coarse_dense_max, coarse_smooth=self.coarse_smooth, sens_fp32=self.sens_fp32,
+            inner_tol=self.inner_tol, inner_maxit=self.inner_maxit)
         self.filt = Filter(self.nelx, self.nely, self.nelz, self.filter, self.rmin, h=self.h, rtol=self.filter_rtol)
         self.mma = MMA(n, self.m, self.x)
         self.mma.SetAsymptotes(0.1, 0.6, 1.05)  # main.cc:58

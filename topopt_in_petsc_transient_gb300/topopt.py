@@ -47,7 +47,8 @@ class LinearElasticity:
     def __init__(self, nelx, nely, nelz, nu=0.3, nlvls=4, ncp=2, tsc=25, t1=50.0, ti=1, objective=0,
                  stiffnessInterpolation=1, massInterpolation=0, t0=0.0, boundaries=1, loadloc=1, reduction=False,
                  basis=5, dalpha=1e-4, dbeta=1e-4, omega0=1.0, optimizationRegion=2, V0=None, h=(1.0, 1.0, 1.0),
-                 loadsignal=0, mixed=True, rtol=1e-10, maxit=500, smooth=3, cheb_ratio=30.0, use_graphs=True):
+                 loadsignal=0, mixed=True, rtol=1e-10, maxit=500, smooth=3, cheb_ratio=30.0, use_graphs=True,
+                 coarse_dense_max=None, coarse_smooth=None, sens_fp32=None, inner_tol=None, inner_maxit=None):
         if reduction:
             raise TopoError(1, "LinearElasticity", "the SOMMG reduced-order path is not part of this build")
         L = _lib.load()
@@ -61,6 +62,16 @@ class LinearElasticity:
         p.dalpha, p.dbeta = dalpha, dbeta
         p.mixed, p.rtol, p.maxit, p.smooth = int(bool(mixed)), rtol, maxit, smooth
         p.cheb_ratio, p.use_graphs = cheb_ratio, int(bool(use_graphs))
+        if coarse_dense_max is not None:
+            p.coarse_dense_max = coarse_dense_max
+        if coarse_smooth is not None:
+            p.coarse_smooth = coarse_smooth
+        if sens_fp32 is not None:
+            p.sens_fp32 = int(bool(sens_fp32))
+        if inner_tol is not None:
+            p.inner_tol = inner_tol
+        if inner_maxit is not None:
+            p.inner_maxit = inner_maxit
         self.params = p
         self.nelx, self.nely, self.nelz = nelx, nely, nelz
         self.nel = nelx * nely * nelz
@@ -132,7 +143,7 @@ class LinearElasticity:
         s = LEStats()
         check(_lib.load().topo_le_get_stats(self._h, C.byref(s)), "get_stats")
         return {"cg_iterations": s.cg_iterations, "solves": s.solves, "device_bytes": s.device_bytes,
-                "last_fx": s.last_fx}
+                "last_fx": s.last_fx, "graph_body_launches": s.graph_body_launches}
 
 
 class PDEFilt:
@@ -250,10 +261,11 @@ class MMA:
     def SetOuterMovelimit(self, Xmin, Xmax, movlim, x, xmin, xmax):
         """MMA::SetOuterMovelimit (MMA.cc:374-393); device arrays."""
         d = [_addr(v, self.n, n) for v, n in ((x, "x"), (xmin, "xmin"), (xmax, "xmax"))]
-        if not all(t[0] for t in d):
-            raise TypeError("SetOuterMovelimit takes device (CUDA tensor) arrays")
-        check(_lib.load().topo_mma_set_outer_movelimit_dev(self._h, Xmin, Xmax, movlim, d[0][1], d[1][1], d[2][1]),
-              "MMA::SetOuterMovelimit")
+        if len({t[0] for t in d}) != 1:
+            raise TypeError("x, xmin, xmax must all be host or all be device arrays")
+        L = _lib.load()
+        f = L.topo_mma_set_outer_movelimit_dev if d[0][0] else L.topo_mma_set_outer_movelimit
+        check(f(self._h, Xmin, Xmax, movlim, d[0][1], d[1][1], d[2][1]), "MMA::SetOuterMovelimit")
         return 0
 
     def Update(self, xval, dfdx, gx, dgdx, xmin, xmax):
@@ -272,10 +284,12 @@ class MMA:
     def DesignChange(self, x, xold):
         """MMA::DesignChange (MMA.cc:395-414): returns the inf-norm change, xold <- x."""
         d = [_addr(v, self.n, n) for v, n in ((x, "x"), (xold, "xold"))]
-        if not all(t[0] for t in d):
-            raise TypeError("DesignChange takes device (CUDA tensor) arrays")
+        if len({t[0] for t in d}) != 1:
+            raise TypeError("x and xold must both be host or both be device arrays")
+        L = _lib.load()
+        f = L.topo_mma_design_change_dev if d[0][0] else L.topo_mma_design_change
         ch = C.c_double()
-        check(_lib.load().topo_mma_design_change_dev(self._h, d[0][1], d[1][1], C.byref(ch)), "MMA::DesignChange")
+        check(f(self._h, d[0][1], d[1][1], C.byref(ch)), "MMA::DesignChange")
         return ch.value
 
     def KKTresidual(self, x, dfdx, fx, dgdx, xmin, xmax):
