@@ -110,7 +110,8 @@ int topo_le_get_state(topo_le *le, int which, int j, double *out);
 int topo_le_apply_km(topo_le *le, const double *x, double *Kx, double *Mx);
 int topo_le_get_stats(topo_le *le, topo_le_stats *out);
 /* CUDA-event timing of the matrix-free operator apply on the object's stream:
- * `precision` 0 = FP64 (outer Krylov), 1 = FP32 (multigrid smoother);
+ * `precision` 0 = FP64, 1 = FP32 (multigrid smoother), 2 = double-float (the
+ * FP64-accurate passes of the mixed path);
  * `reps` back-to-back launches after `warmup`; returns mean ms per launch */
 int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double *ms_per_launch);
 /* 24x24 box element matrices (E = 1, unit density) as applied by the

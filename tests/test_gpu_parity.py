@@ -37,19 +37,22 @@ def _rel(a, b):
     return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
 
 
-def test_operator_apply_matches_assembled_matrices(gpu):
+@pytest.mark.parametrize("mixed", [False, True])
+def test_operator_apply_matches_assembled_matrices(gpu, mixed):
+    # mixed: the FP64-accurate passes run in double-float (FP32 pairs)
     n = (16, 8, 8)
     rng = np.random.default_rng(0)
     x = 0.1 + 0.8 * rng.random(np.prod(n))
-    le = _le(n, nlvls=3, ncp=1, tsc=2, t1=0.02, mixed=False)
+    le = _le(n, nlvls=3, ncp=1, tsc=2, t1=0.02, mixed=mixed)
     le.CompleteInitialState(x, *M6)
     ref = O.LinearElasticity(*n, ncp=1, tsc=2, t1=0.02)
     ref.CompleteInitialState(x)
     v = rng.standard_normal(le.ndof)
     K, M = le.apply_km(v)
     K2, M2 = ref.apply_KM(v)
-    assert _rel(K, K2) < 1e-13
-    assert _rel(M, M2) < 1e-13
+    tol = 1e-12 if mixed else 1e-13
+    assert _rel(K, K2) < tol
+    assert _rel(M, M2) < tol
 
 
 @pytest.mark.parametrize("objective", range(7))
@@ -60,7 +63,7 @@ def test_objective_and_sensitivities_match_oracle(gpu, objective, mixed):
               mInt=1 if objective == 4 else 0)
     rng = np.random.default_rng(10 + objective)
     x = 0.1 + 0.5 * rng.random(np.prod(n))
-    le = _le(n, nlvls=2, mixed=mixed, rtol=1e-12, **{k: v for k, v in kw.items() if k != "mInt"},
+    le = _le(n, nlvls=2, mixed=mixed, rtol=1e-12, sens_fp32=False, **{k: v for k, v in kw.items() if k != "mInt"},
              massInterpolation=kw["mInt"])
     fx, df = _run_gpu(le, x)
     ref = O.LinearElasticity(*n, **kw)
@@ -76,7 +79,7 @@ def test_states_and_checkpointing(gpu, ncp, tsc, graphs):
     rng = np.random.default_rng(3)
     x = 0.12 + 0.04 * rng.random(np.prod(n))
     kw = dict(ncp=ncp, tsc=tsc, t1=0.12, objective=3, loadsignal=1, dalpha=0.0, dbeta=1e-3)
-    le = _le(n, nlvls=3, mixed=True, rtol=1e-12, use_graphs=graphs, **kw)
+    le = _le(n, nlvls=3, mixed=True, rtol=1e-12, use_graphs=graphs, sens_fp32=False, **kw)
     fx, df = _run_gpu(le, x)
     ref = O.LinearElasticity(*n, **kw)
     rc, fx_r, df_r = ref.objective_sensitivities(x)
@@ -87,6 +90,23 @@ def test_states_and_checkpointing(gpu, ncp, tsc, graphs):
     assert _rel(le.state(0, tsc - 1), U) < 1e-10
     assert _rel(le.state(1, tsc - 1), DU) < 1e-9
     assert _rel(le.state(2, tsc - 1), DDU) < 1e-8
+
+
+@pytest.mark.parametrize("nlvls,coarse_smooth", [(1, 10), (2, 8), (3, 6)])
+def test_mixed_default_fp32_sensitivities(gpu, nlvls, coarse_smooth):
+    # the mixed-path default: FP32 element math in the sensitivity kernel
+    # (state combinations formed in FP64); stated tolerance 1e-6 on the
+    # objective and 1e-5 of max|dfdx| on the sensitivities
+    n = (16, 8, 8)
+    kw = dict(ncp=2, tsc=6, t1=0.06, objective=3, loadsignal=1, dalpha=0.0, dbeta=1e-3)
+    rng = np.random.default_rng(21)
+    x = 0.12 + 0.02 * (2 * rng.random(np.prod(n)) - 1)
+    le = _le(n, nlvls=nlvls, coarse_smooth=coarse_smooth, mixed=True, rtol=1e-10, **kw)
+    fx, df = _run_gpu(le, x)
+    ref = O.LinearElasticity(*n, **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert abs(fx - fx_r) <= 1e-6 * abs(fx_r)
+    assert _rel(df, df_r) < 1e-5
 
 
 def test_reference_pulse_and_defaults(gpu):
@@ -207,7 +227,7 @@ def test_finite_difference_check_on_gpu(gpu):
     # 192x96x96 workload, here on a small mesh)
     n = (8, 4, 4)
     kw = dict(nlvls=2, ncp=2, tsc=5, t1=0.5, objective=3, loadsignal=1, dalpha=0.0, dbeta=1e-3, mixed=True,
-              rtol=1e-13)
+              rtol=1e-13, sens_fp32=False)
     rng = np.random.default_rng(11)
     x = 0.12 + 0.02 * (2 * rng.random(np.prod(n)) - 1)
     le = _le(n, **kw)

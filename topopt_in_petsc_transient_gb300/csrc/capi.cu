@@ -97,7 +97,7 @@ void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz) {
     p->use_graphs = 1;
     p->coarse_dense_max = 4096;
     p->coarse_smooth = 8;
-    p->sens_fp32 = 0;
+    p->sens_fp32 = 1;
     p->inner_tol = 1e-4;
     p->inner_maxit = 40;
 }
@@ -175,7 +175,7 @@ int topo_le_volume_constraint_dev(topo_le *le, double *gx, double *dgdx_dev, con
     if (!le || !gx || !dgdx_dev || !xPhys_dev) return TOPO_ERR_ARG;
     double *gd = le->part + 65535;
     count_launch();
-    k_volume<<<ew_blocks(le->nel), EW>>>(le->nel, xPhys_dev, volfrac, dgdx_dev, Partials<1>{le->part, le->counter}, gd);
+    k_volume<<<red_blocks(le->nel), EW>>>(le->nel, xPhys_dev, volfrac, dgdx_dev, Partials<1>{le->part, le->counter}, gd);
     ACK(cudaMemcpy(gx, gd, sizeof(double), cudaMemcpyDeviceToHost));
     return TOPO_OK;
 }
@@ -216,7 +216,7 @@ int topo_le_get_stats(topo_le *le, topo_le_stats *out) {
 }
 
 int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double *ms_per_launch) {
-    if (!le || !ms_per_launch || reps < 1 || warmup < 0 || (precision != 0 && precision != 1)) return TOPO_ERR_ARG;
+    if (!le || !ms_per_launch || reps < 1 || warmup < 0 || precision < 0 || precision > 2) return TOPO_ERR_ARG;
     return le_time_apply(le->impl, precision, warmup, reps, ms_per_launch);
 }
 

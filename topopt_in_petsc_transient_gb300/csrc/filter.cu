@@ -343,14 +343,14 @@ static int helmholtz_solve(TopoPDEFilt *f, const double *x_dev) {
     count_launch();
     k_fprime<<<1, 1, 0, s>>>(f->S, f->rtol * f->rtol, f->maxit);
     count_launch();
-    k_fpcg_init<<<ew_blocks(nn), EW, 0, s>>>(nn, f->rhs, f->dinv, f->u, f->r, f->p, f->S, p2);
+    k_fpcg_init<<<red_blocks(nn), EW, 0, s>>>(nn, f->rhs, f->dinv, f->u, f->r, f->p, f->S, p2);
     FiltScalars h;
     for (int outer = 0; outer < 1000000; outer++) {
         for (int it = 0; it < 8; it++) {
             count_launch();
-            k_filt_apply<<<ew_blocks(nn), EW, 0, s>>>(f->g, K, f->p, f->q, p1, f->S, 1);
+            k_filt_apply<<<red_blocks(nn), EW, 0, s>>>(f->g, K, f->p, f->q, p1, f->S, 1);
             count_launch();
-            k_fpcg_update<<<ew_blocks(nn), EW, 0, s>>>(nn, f->dinv, f->u, f->r, f->p, f->q, f->S, p2);
+            k_fpcg_update<<<red_blocks(nn), EW, 0, s>>>(nn, f->dinv, f->u, f->r, f->p, f->q, f->S, p2);
             count_launch();
             k_fpcg_p<<<ew_blocks(nn), EW, 0, s>>>(nn, f->dinv, f->r, f->p, f->S);
         }
@@ -408,7 +408,7 @@ int filter_mnd_dev(TopoPDEFilt *f, const double *x_dev, double *mnd) {
     long long nel = f->g.nel();
     Partials<1> p1{f->part, f->counter};
     count_launch();
-    k_mnd<<<ew_blocks(nel), EW, 0, f->stream>>>(nel, x_dev, p1, f->e2);
+    k_mnd<<<red_blocks(nel), EW, 0, f->stream>>>(nel, x_dev, p1, f->e2);
     FCK(cudaMemcpyAsync(mnd, f->e2, sizeof(double), cudaMemcpyDeviceToHost, f->stream));
     FCK(cudaStreamSynchronize(f->stream));
     return TOPO_OK;

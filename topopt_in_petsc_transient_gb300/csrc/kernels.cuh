@@ -12,6 +12,26 @@ __host__ inline unsigned ew_blocks(long long n) {
     return (unsigned)(b < 1 ? 1 : (b > 65535LL * 64 ? 65535LL * 64 : b));
 }
 
+// grid of the element-wise kernels that end in a grid reduction: a single
+// wave of grid-stride CTAs (many short CTAs each doing a block reduction,
+// fence and counter atomic are latency-bound)
+__host__ inline unsigned red_blocks(long long n) {
+    unsigned b = ew_blocks(n);
+    return b < 608u ? b : 608u;
+}
+
+// Chebyshev coefficients (c1, c2) of steps k = 0..kmax-1 from the device-side
+// spectrum bounds; computed once per design iteration so that no kernel
+// repeats the FP64 divisions per thread
+static __global__ void k_cheb_table(const double *lohi, int kmax, double *coef) {
+    double c1, c2;
+    for (int k = 0; k < kmax; k++) {
+        cheb_coeffs<double>(lohi, k, c1, c2);
+        coef[2 * k] = c1;
+        coef[2 * k + 1] = c2;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // material interpolation, InterpolateStiffness / InterpolateMass
 // (LinearElasticity.cc:1580-1623)
@@ -37,7 +57,7 @@ struct MatParams {
 };
 
 static __global__ void k_interp(long long nel, const double *__restrict__ x, MatParams mp, double *kf, double *dkf, double *mf,
-                         double *dmf, float *kff, float *mff) {
+                         double *dmf, float *kff, float *mff, df *kfx, df *mfx) {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
         double k, dk, m, dm;
         interp_dev(mp.sInt, mp.Emax, mp.Emin, mp.penalK, x[e], k, dk);
@@ -48,6 +68,8 @@ static __global__ void k_interp(long long nel, const double *__restrict__ x, Mat
         dmf[e] = dm;
         kff[e] = (float)k;
         mff[e] = (float)m;
+        kfx[e] = df(k);
+        mfx[e] = df(m);
     }
 }
 
@@ -146,10 +168,9 @@ static __global__ void k_bounds_final(const unsigned long long *bits, double rat
 
 // first Chebyshev step from a zero initial guess: d = Dinv b / theta, x = d
 template <class T>
-static __global__ void k_cheb0(long long ndof, const T *__restrict__ b, const T *__restrict__ dinv, const double *lohi, T *x,
-                        T *d) {
-    T c1, c2;
-    cheb_coeffs<T>(lohi, 0, c1, c2);
+static __global__ void k_cheb0(long long ndof, const T *__restrict__ b, const T *__restrict__ dinv, const double *coef,
+                               T *x, T *d) {
+    const T c2 = (T)coef[1];
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
         T v = c2 * dinv[i] * b[i];
         d[i] = v;
@@ -363,12 +384,13 @@ static __global__ void k_fcg_update(long long ndof, double *x, double *r, float 
 // mixed-precision FCG pieces (FP32 vectors, FP64 scalars and iterate)
 static __global__ void k_mfcg_dot(long long ndof, const float *__restrict__ z, const float *__restrict__ r32,
                                   const float *__restrict__ q32, SolveScalars *S, Partials<2> part) {
-    double v[2] = {0.0, 0.0};
+    float s0 = 0.0f, s1 = 0.0f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
-        double zi = (double)z[i];
-        v[0] += zi * (double)r32[i];
-        v[1] += zi * (double)q32[i];
+        float zi = z[i];
+        s0 += zi * r32[i];
+        s1 += zi * q32[i];
     }
+    double v[2] = {(double)s0, (double)s1};
     double tot[2];
     if (grid_reduce<EW, 2>(v, part, tot)) {
         S->rho = tot[0];
@@ -388,13 +410,14 @@ static __global__ void k_mfcg_update(long long ndof, double *x, float *r32, cons
                                      const float *__restrict__ q, SolveScalars *S, Partials<1> part) {
     double alpha = S->alpha;
     float af = (float)alpha;
-    double v[1] = {0.0};
+    float s = 0.0f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
         x[i] += alpha * (double)p[i];
         float rv = r32[i] - af * q[i];
         r32[i] = rv;
-        v[0] += (double)rv * (double)rv;
+        s += rv * rv;
     }
+    double v[1] = {(double)s};
     double tot[1];
     if (grid_reduce<EW, 1>(v, part, tot)) {
         S->it += 1;

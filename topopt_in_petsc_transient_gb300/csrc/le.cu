@@ -138,6 +138,12 @@ static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol
 // ---------------------------------------------------------------------------
 // multigrid hierarchy
 // ---------------------------------------------------------------------------
+struct TopoLE;
+template <class A>
+static Weights<A> fine_weights(TopoLE *le, bool hk, bool hm, const double *P, double sK, double sM);
+template <class A>
+static const ElemConst<A> &fine_const(TopoLE *le);
+
 struct Level {
     GridDesc g;
     double h[3];
@@ -156,6 +162,7 @@ struct OpLevel {
     double *dinvd = nullptr;
     float *dinvf = nullptr;
     double *lohi = nullptr;  // device [2]
+    double *cheb = nullptr;  // device [kmax][2] Chebyshev step coefficients
 };
 
 struct Operator {
@@ -181,6 +188,8 @@ struct TopoLE {
     double *N_host_dummy = nullptr;
     double *rhs0 = nullptr, *P = nullptr, *xPhys = nullptr;
     double *kf = nullptr, *dkf = nullptr, *mf = nullptr, *dmf = nullptr;
+    df *kfx = nullptr, *mfx = nullptr;  // double-float copies for the mixed path
+    ElemConst<df> Cx;
     float *cntP = nullptr;
     double *cp = nullptr;                   // (ncp+1) x 3 x ndof
     double *Uh = nullptr, *DUh = nullptr, *DDUh = nullptr;  // tsc x ndof
@@ -214,6 +223,21 @@ struct TopoLE {
 };
 
 static Partials<1> P1(TopoLE *le) { return Partials<1>{le->part, le->counter}; }
+
+// fine-level element weights / constants for the FP64-accurate passes:
+// native double (plain path) or double-float (mixed path)
+template <>
+Weights<double> fine_weights<double>(TopoLE *le, bool hk, bool hm, const double *P, double sK, double sM) {
+    return Weights<double>{hk ? le->kf : nullptr, hm ? le->mf : nullptr, P, sK, sM};
+}
+template <>
+Weights<df> fine_weights<df>(TopoLE *le, bool hk, bool hm, const double *P, double sK, double sM) {
+    return Weights<df>{hk ? le->kfx : nullptr, hm ? le->mfx : nullptr, P, df(sK), df(sM)};
+}
+template <>
+const ElemConst<double> &fine_const<double>(TopoLE *le) { return le->L[0].Cd; }
+template <>
+const ElemConst<df> &fine_const<df>(TopoLE *le) { return le->Cx; }
 static Partials<2> P2(TopoLE *le) { return Partials<2>{le->part, le->counter}; }
 
 // ---------------------------------------------------------------------------
@@ -273,6 +297,8 @@ int le_alloc(TopoLE *le) {
     AG(le->dkf, ne);
     AG(le->mf, ne);
     AG(le->dmf, ne);
+    AG(le->kfx, ne);
+    AG(le->mfx, ne);
     AG(le->cntP, nn);
     AG(le->cp, (size_t)(p.ncp + 1) * 3 * nd);
     AG(le->Uh, (size_t)p.tsc * nd);
@@ -415,6 +441,7 @@ int le_alloc(TopoLE *le) {
     }
     le->L[0].kfd = le->kf;
     le->L[0].mfd = le->mf;
+    le->Cx = make_elem_const<df>(p.hx, p.hy, p.hz, p.nu);
     // fine-level float factors
     AG(le->L[0].kff, ne);
     AG(le->L[0].mff, ne);
@@ -433,6 +460,7 @@ int le_alloc(TopoLE *le) {
             AG(op.lv[l].dinvd, lnd);
             AG(op.lv[l].dinvf, lnd);
             AG(op.lv[l].lohi, 2);
+            AG(op.lv[l].cheb, 2 * 64);
         }
         if (le->coarse_dense) {
             AG(op.Ainv_d, (size_t)le->ncoarse * le->ncoarse);
@@ -456,6 +484,11 @@ void le_destroy(TopoLE *le) {
 // ---------------------------------------------------------------------------
 // per-design setup of the hierarchy (densities changed)
 // ---------------------------------------------------------------------------
+static int cheb_kmax(const TopoLE *le) {
+    int k = le->p.smooth > le->p.coarse_smooth ? le->p.smooth : le->p.coarse_smooth;
+    return k < 1 ? 1 : (k > 64 ? 64 : k);
+}
+
 static int setup_operator(TopoLE *le, int o) {
     Operator &op = le->ops[o];
     cudaStream_t s = le->stream;
@@ -472,6 +505,8 @@ static int setup_operator(TopoLE *le, int o) {
                                                       lv.dK[2], lv.dM, lv.lamK, 0.125, 3.375, le->bbits);
         count_launch();
         k_bounds_final<<<1, 1, 0, s>>>(le->bbits, le->p.cheb_ratio, op.lv[l].lohi);
+        count_launch();
+        k_cheb_table<<<1, 1, 0, s>>>(op.lv[l].lohi, cheb_kmax(le), op.lv[l].cheb);
     }
     // dense coarsest operator and its inverse (FP64 Gauss-Jordan)
     if (!le->coarse_dense) {
@@ -533,7 +568,7 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b) {
     Operator &op = le->ops[o];
     long long nd = 3 * lv.g.nn();
     Weights<T> wt{op.sK != 0.0 ? w.kf : nullptr, w.mf, nullptr, (T)op.sK, (T)op.sM};
-    const double *lohi = op.lv[l].lohi;
+    const double *lohi = op.lv[l].cheb;
     T *x = w.xa, *xo = w.xb;
     if (l == le->nlev - 1) {
         if (le->coarse_dense) {
@@ -600,14 +635,20 @@ __global__ void k_solve_check(const SolveScalars *S, int *err) {
 }
 
 static const double *&cur_b(TopoLE *le);
-static void solve_init(TopoLE *le, int o, const double *b, cudaGraphConditionalHandle cond, int has_cond) {
-    cur_b(le) = b;
+template <class A>
+static void solve_init_t(TopoLE *le, int o, const double *b, cudaGraphConditionalHandle cond, int has_cond) {
     Level &l0 = le->L[0];
     Operator &op = le->ops[o];
-    Weights<double> wt{op.sK != 0.0 ? l0.kfd : nullptr, l0.mfd, nullptr, op.sK, op.sM};
-    PolInitResid<double> pi{l0.fixed, wt, le->sx, b, le->sr, le->p.mixed ? le->sr32 : nullptr,
-                            le->S, cond, has_cond, P2(le)};
-    launch_tile<double>(l0.g, l0.Cd, pi, le->stream);
+    Weights<A> wt = fine_weights<A>(le, op.sK != 0.0, true, nullptr, op.sK, op.sM);
+    PolInitResid<A> pi{l0.fixed, wt, le->sx, b, le->sr, le->p.mixed ? le->sr32 : nullptr, le->S, cond, has_cond, P2(le)};
+    launch_tile<A>(l0.g, fine_const<A>(le), pi, le->stream);
+}
+static void solve_init(TopoLE *le, int o, const double *b, cudaGraphConditionalHandle cond, int has_cond) {
+    cur_b(le) = b;
+    if (le->p.mixed)
+        solve_init_t<df>(le, o, b, cond, has_cond);
+    else
+        solve_init_t<double>(le, o, b, cond, has_cond);
 }
 
 // right-hand side of the solve in flight (set by solve_init)
@@ -627,22 +668,22 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
         // reliable-update mixed precision: FP32 recurrence, FP64 replacements
         float *z = vcycle<float>(le, o, 0, le->sr32);
         count_launch();
-        k_mfcg_dot<<<nb, EW, 0, s>>>(nd, z, le->sr32, le->sq32, le->S, P2(le));
+        k_mfcg_dot<<<red_blocks(nd), EW, 0, s>>>(nd, z, le->sr32, le->sq32, le->S, P2(le));
         count_launch();
         k_mfcg_p<<<nb, EW, 0, s>>>(nd, z, le->sp32, le->S);
         Weights<float> wf{op.sK != 0.0 ? l0.kff : nullptr, l0.mff, nullptr, (float)op.sK, (float)op.sM};
         PolPQ32 pq32{l0.fixed, wf, le->sp32, le->sq32, le->S, P1(le)};
         launch_tile<float>(l0.g, l0.Cf, pq32, s);
         count_launch();
-        k_mfcg_update<<<nb, EW, 0, s>>>(nd, le->sx, le->sr32, le->sp32, le->sq32, le->S, P1(le));
-        Weights<double> wd{op.sK != 0.0 ? l0.kfd : nullptr, l0.mfd, nullptr, op.sK, op.sM};
-        PolReplace rp{l0.fixed, wd, le->sx, cur_b(le), le->sr, le->sr32, le->S, cond, has_cond, P1(le)};
-        launch_tile<double>(l0.g, l0.Cd, rp, s);
+        k_mfcg_update<<<red_blocks(nd), EW, 0, s>>>(nd, le->sx, le->sr32, le->sp32, le->sq32, le->S, P1(le));
+        Weights<df> wd = fine_weights<df>(le, op.sK != 0.0, true, nullptr, op.sK, op.sM);
+        PolReplace<df> rp{l0.fixed, wd, le->sx, cur_b(le), le->sr, le->sr32, le->S, cond, has_cond, P1(le)};
+        launch_tile<df>(l0.g, le->Cx, rp, s);
         return;
     } else {
         double *z = vcycle<double>(le, o, 0, le->sr);
         count_launch();
-        k_fcg_dot<double><<<nb, EW, 0, s>>>(nd, z, le->sr, le->sq, le->S, P2(le));
+        k_fcg_dot<double><<<red_blocks(nd), EW, 0, s>>>(nd, z, le->sr, le->sq, le->S, P2(le));
         count_launch();
         k_fcg_p<double><<<nb, EW, 0, s>>>(nd, z, le->sp, le->S);
     }
@@ -650,7 +691,7 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
     PolPQ<double> pq{l0.fixed, wt, le->sp, le->sq, le->S, P1(le)};
     launch_tile<double>(l0.g, l0.Cd, pq, s);
     count_launch();
-    k_fcg_update<<<nb, EW, 0, s>>>(nd, le->sx, le->sr, le->p.mixed ? le->sr32 : nullptr, le->sp, le->sq, le->S,
+    k_fcg_update<<<red_blocks(nd), EW, 0, s>>>(nd, le->sx, le->sr, le->p.mixed ? le->sr32 : nullptr, le->sp, le->sq, le->S,
                                    P1(le), cond, has_cond);
 }
 
@@ -728,14 +769,15 @@ static int solve(TopoLE *le, int o, const double *b, bool capturing) {
 // ---------------------------------------------------------------------------
 // forward step j of block c (SolveStateBlock, LinearElasticity.cc:1317-1385)
 // ---------------------------------------------------------------------------
-static void fwd_rhs(TopoLE *le) {
+template <class A>
+static void fwd_rhs_t(TopoLE *le) {
     const LEParams &p = le->p;
     Level &l0 = le->L[0];
     const double *a = le->a;
-    PolRhsFwd pr;
+    PolRhsFwd<A> pr;
     memset(&pr, 0, sizeof(pr));
     pr.fixed = l0.fixed;
-    pr.w = Weights<double>{le->kf, le->mf, nullptr, 1.0, 1.0};
+    pr.w = fine_weights<A>(le, true, true, nullptr, 1.0, 1.0);
     pr.cp = le->cp;
     pr.Uh = le->Uh;
     pr.DUh = le->DUh;
@@ -759,7 +801,13 @@ static void fwd_rhs(TopoLE *le) {
     pr.st = le->st;
     pr.b = le->sb;
     pr.x0 = le->sx;
-    launch_tile<double>(l0.g, l0.Cd, pr, le->stream);
+    launch_tile<A>(l0.g, fine_const<A>(le), pr, le->stream);
+}
+static void fwd_rhs(TopoLE *le) {
+    if (le->p.mixed)
+        fwd_rhs_t<df>(le);
+    else
+        fwd_rhs_t<double>(le);
 }
 
 static int fwd_step(TopoLE *le, bool capturing) {
@@ -779,11 +827,18 @@ static int fwd_step(TopoLE *le, bool capturing) {
 // ---------------------------------------------------------------------------
 // adjoint step j (SolveLagrangen body) and the t = 0 pass (SolveLagrange0)
 // ---------------------------------------------------------------------------
+template <class A, bool HK, bool HM>
+static void product_t(TopoLE *le, const double *x, double *y, const double *P, double sK, double sM) {
+    Level &l0 = le->L[0];
+    PolProduct<A, HK, HM> pp{fine_weights<A>(le, HK, HM, P, sK, sM), x, y, {}};
+    launch_tile<A>(l0.g, fine_const<A>(le), pp, le->stream);
+}
 template <bool HK, bool HM>
 static void product(TopoLE *le, const double *x, double *y, const double *P, double sK, double sM) {
-    Level &l0 = le->L[0];
-    PolProduct<double, HK, HM> pp{Weights<double>{HK ? le->kf : nullptr, HM ? le->mf : nullptr, P, sK, sM}, x, y, {}};
-    launch_tile<double>(l0.g, l0.Cd, pp, le->stream);
+    if (le->p.mixed)
+        product_t<df, HK, HM>(le, x, y, P, sK, sM);
+    else
+        product_t<double, HK, HM>(le, x, y, P, sK, sM);
 }
 
 // objective gradient products h (objectives 3-6) of the state `state_base`
@@ -911,9 +966,9 @@ template <int OBJ>
 static void launch_sens_obj(TopoLE *le, const SensArgs &S) {
     count_launch();
     if (le->p.mixed && le->p.sens_fp32)
-        k_sens<OBJ, float><<<ew_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cf);
+        k_sens<OBJ, float><<<red_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cf);
     else
-        k_sens<OBJ, double><<<ew_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cd);
+        k_sens<OBJ, double><<<red_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cd);
 }
 static void launch_sens(TopoLE *le, int t0mode) {
     SensArgs S = sens_args(le, t0mode);
@@ -1039,7 +1094,7 @@ int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, 
     MatParams mp{p.sInt, p.mInt, Emin, Emax, penalK, Rmin, Rmax, penalM};
     count_launch();
     k_interp<<<ew_blocks(le->nel), EW, 0, s>>>(le->nel, le->xPhys, mp, le->kf, le->dkf, le->mf, le->dmf, le->L[0].kff,
-                                               le->L[0].mff);
+                                               le->L[0].mff, le->kfx, le->mfx);
     for (int l = 1; l < le->nlev; l++) {
         count_launch();
         k_coarsen<<<ew_blocks(le->L[l].g.nel()), EW, 0, s>>>(le->L[l - 1].g, le->L[l].g, le->L[l - 1].kfd,
@@ -1206,6 +1261,10 @@ int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms) {
             Weights<double> wt{l0.kfd, l0.mfd, nullptr, op.sK, op.sM};
             PolResid<double> pr{l0.fixed, wt, le->sp, le->sb, le->sq, {}};
             launch_tile<double>(l0.g, l0.Cd, pr, s);
+        } else if (precision == 2) {
+            Weights<df> wt = fine_weights<df>(le, true, true, nullptr, op.sK, op.sM);
+            PolProduct<df, true, true> pp{wt, le->sp, le->sq, {}};
+            launch_tile<df>(l0.g, le->Cx, pp, s);
         } else {
             Weights<float> wt{l0.kff, l0.mff, nullptr, (float)op.sK, (float)op.sM};
             PolResid<float> pr{l0.fixed, wt, l0.fr, l0.fb, l0.fd, {}};

@@ -405,7 +405,7 @@ template <int M>
 static int solve_dip(TopoMMA *mm, double *x) {
     cudaStream_t s = mm->stream;
     long long n = mm->n;
-    unsigned nb = ew_blocks(n);
+    unsigned nb = red_blocks(n);
     Partials<M + M * M> pgh{mm->part, mm->counter};
     Partials<M> pr{mm->part, mm->counter};
     count_launch();
@@ -450,7 +450,7 @@ int mma_update_dev(TopoMMA *mm, double *xval, const double *dfdx, const double *
     for (int j = 0; j < mm->m; j++) g.v[j] = gx[j];
     Partials<MMA_MAXM> pb{mm->part, mm->counter};
     count_launch();
-    k_mma_gensub<<<ew_blocks(n), EW, 0, s>>>(n, mm->m, xval, dfdx, dgdx, xmin, xmax, mm->L, mm->U, mm->xo1, mm->xo2,
+    k_mma_gensub<<<red_blocks(n), EW, 0, s>>>(n, mm->m, xval, dfdx, dgdx, xmin, xmax, mm->L, mm->U, mm->xo1, mm->xo2,
                                              mm->alpha, mm->beta, mm->p0, mm->q0, mm->pij, mm->qij, mm->S, g, pb);
     count_launch();
     k_mma_shift<<<ew_blocks(n), EW, 0, s>>>(n, xval, mm->xo1, mm->xo2);
@@ -480,7 +480,7 @@ int mma_kkt_dev(TopoMMA *mm, const double *x, const double *dfdx, const double *
     double *n2d = mm->part + 8 * 65536 - 1;
     Partials<1> p1{mm->part, mm->counter};
     count_launch();
-    k_mma_kkt<<<ew_blocks(mm->n), EW, 0, s>>>(mm->n, mm->m, x, dfdx, dgdx, xmin, xmax, mm->S, p1, mm->bits, n2d);
+    k_mma_kkt<<<red_blocks(mm->n), EW, 0, s>>>(mm->n, mm->m, x, dfdx, dgdx, xmin, xmax, mm->S, p1, mm->bits, n2d);
     unsigned long long b = 0;
     double n2 = 0.0;
     MMAScalars h;

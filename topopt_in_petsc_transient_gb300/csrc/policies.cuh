@@ -7,6 +7,7 @@
 // LinearElasticity.cc:1118-1122), applied as: zero clamped inputs, apply the
 // element operator, zero clamped outputs, add the identity on clamped DOFs.
 #pragma once
+#include "df.cuh"
 #include "tile.cuh"
 
 namespace topo {
@@ -57,30 +58,30 @@ struct PolInitResid {
     static constexpr bool HAS_K = true, HAS_M = true;
     const uint8_t *fixed;
     Weights<T> w;
-    const T *x, *b;
-    T *r;
+    const double *x, *b;
+    double *r;
     float *r32;  // optional FP32 copy for the mixed-precision preconditioner
     SolveScalars *S;
     cudaGraphConditionalHandle cond;
     int has_cond;
     Partials<2> part;
     __device__ void load(long long n, T v[1][3]) const {
-        v[0][0] = x[3 * n];
-        v[0][1] = x[3 * n + 1];
-        v[0][2] = x[3 * n + 2];
+        v[0][0] = T(x[3 * n]);
+        v[0][1] = T(x[3 * n + 1]);
+        v[0][2] = T(x[3 * n + 2]);
         mask3(fixed[n], v[0]);
     }
     __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
     __device__ void epilogue(long long n, int, int, int, const T y[3], double red[2]) const {
         uint8_t f = fixed[n];
         for (int c = 0; c < 3; c++) {
-            T xv = x[3 * n + c], bv = b[3 * n + c];
-            T ax = ((f >> c) & 1) ? xv : y[c];
-            T rv = bv - ax;
+            double xv = x[3 * n + c], bv = b[3 * n + c];
+            double ax = ((f >> c) & 1) ? xv : todbl(y[c]);
+            double rv = bv - ax;
             r[3 * n + c] = rv;
             if (r32) r32[3 * n + c] = (float)rv;
-            red[0] += (double)bv * (double)bv;
-            red[1] += (double)rv * (double)rv;
+            red[0] += bv * bv;
+            red[1] += rv * rv;
         }
     }
     __device__ void finish(const double t[2]) const {
@@ -169,12 +170,14 @@ struct PolPQ32 {
     __device__ void coef(long long e, float &ck, float &cm) const { w.get(e, ck, cm); }
     __device__ void epilogue(long long n, int, int, int, const float y[3], double red[1]) const {
         uint8_t f = fixed[n];
+        float s = 0.0f;
         for (int c = 0; c < 3; c++) {
             float pv = p[3 * n + c];
             float qv = ((f >> c) & 1) ? pv : y[c];
             q[3 * n + c] = qv;
-            red[0] += (double)pv * (double)qv;
+            s += pv * qv;
         }
+        red[0] += (double)s;
     }
     __device__ void finish(const double t[1]) const {
         S->pq = t[0];
@@ -188,13 +191,15 @@ struct PolPQ32 {
     }
 };
 
-// r = b - (N A N + I - N) x in FP64, r32 = (float) r; runs only when a
-// replacement is due; decides convergence and drives the graph condition
+// r = b - (N A N + I - N) x, FP64-accurate (T = double or double-float),
+// r32 = (float) r; runs only when a replacement is due; decides convergence
+// and drives the graph condition
+template <class T>
 struct PolReplace {
     static constexpr int NIN = 1, NRED = 1;
     static constexpr bool HAS_K = true, HAS_M = true;
     const uint8_t *fixed;
-    Weights<double> w;
+    Weights<T> w;
     const double *x, *b;
     double *r;
     float *r32;
@@ -203,18 +208,18 @@ struct PolReplace {
     int has_cond;
     Partials<1> part;
     __device__ bool skip() const { return S->need_replace == 0; }
-    __device__ void load(long long n, double v[1][3]) const {
-        v[0][0] = x[3 * n];
-        v[0][1] = x[3 * n + 1];
-        v[0][2] = x[3 * n + 2];
+    __device__ void load(long long n, T v[1][3]) const {
+        v[0][0] = T(x[3 * n]);
+        v[0][1] = T(x[3 * n + 1]);
+        v[0][2] = T(x[3 * n + 2]);
         mask3(fixed[n], v[0]);
     }
-    __device__ void coef(long long e, double &ck, double &cm) const { w.get(e, ck, cm); }
-    __device__ void epilogue(long long n, int, int, int, const double y[3], double red[1]) const {
+    __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const T y[3], double red[1]) const {
         uint8_t f = fixed[n];
         for (int c = 0; c < 3; c++) {
             double xv = x[3 * n + c];
-            double rv = b[3 * n + c] - (((f >> c) & 1) ? xv : y[c]);
+            double rv = b[3 * n + c] - (((f >> c) & 1) ? xv : todbl(y[c]));
             r[3 * n + c] = rv;
             r32[3 * n + c] = (float)rv;
             red[0] += rv * rv;
@@ -271,7 +276,7 @@ struct PolCheb {
     Weights<T> w;
     const T *x_in, *b, *dinv;
     T *x_out, *d;
-    const double *lohi;
+    const double *ctab;  // Chebyshev table [k][2] = (c1, c2), built once per design
     int k;
     Partials<1> part;
     __device__ void load(long long n, T v[1][3]) const {
@@ -282,8 +287,7 @@ struct PolCheb {
     }
     __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
     __device__ void epilogue(long long n, int, int, int, const T y[3], double *) const {
-        T c1, c2;
-        cheb_coeffs<T>(lohi, k, c1, c2);
+        const T c1 = (T)ctab[2 * k], c2 = (T)ctab[2 * k + 1];
         uint8_t f = fixed[n];
         for (int c = 0; c < 3; c++) {
             T xv = x_in[3 * n + c];
@@ -329,19 +333,19 @@ struct PolProduct {
     static constexpr int NIN = 1, NRED = 0;
     static constexpr bool HAS_K = HK, HAS_M = HM;
     Weights<T> w;
-    const T *x;
-    T *y;
+    const double *x;
+    double *y;
     Partials<1> part;
     __device__ void load(long long n, T v[1][3]) const {
-        v[0][0] = x[3 * n];
-        v[0][1] = x[3 * n + 1];
-        v[0][2] = x[3 * n + 2];
+        v[0][0] = T(x[3 * n]);
+        v[0][1] = T(x[3 * n + 1]);
+        v[0][2] = T(x[3 * n + 2]);
     }
     __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
     __device__ void epilogue(long long n, int, int, int, const T yv[3], double *) const {
-        y[3 * n] = yv[0];
-        y[3 * n + 1] = yv[1];
-        y[3 * n + 2] = yv[2];
+        y[3 * n] = todbl(yv[0]);
+        y[3 * n + 1] = todbl(yv[1]);
+        y[3 * n + 2] = todbl(yv[2]);
     }
     __device__ void finish(const double *) const {}
 };
@@ -371,11 +375,12 @@ __device__ __forceinline__ double load_signal(int which, double t) {
     return exp(-(s * s) / ((2 * c) * (2 * c))) * cos(4.0 * s) * cos(5.0 * s) * cos(6.0 * s) * cos(7.0 * s);
 }
 
+template <class T>
 struct PolRhsFwd {
     static constexpr int NIN = 2, NRED = 0;
     static constexpr bool HAS_K = true, HAS_M = true;
     const uint8_t *fixed;
-    Weights<double> w;
+    Weights<T> w;
     const double *cp;                   // checkpoints: block start state (j == 0)
     const double *Uh, *DUh, *DDUh;      // block history [tsc][ndof]
     long long ndof;
@@ -400,19 +405,19 @@ struct PolRhsFwd {
             ddu = DDUh + (long long)(j - 1) * ndof;
         }
     }
-    __device__ void load(long long n, double v[2][3]) const {
+    __device__ void load(long long n, T v[2][3]) const {
         const double *u, *du, *ddu;
         prev(u, du, ddu);
         for (int c = 0; c < 3; c++) {
             double a = u[3 * n + c], bb = du[3 * n + c], cc = ddu[3 * n + c];
-            v[0][c] = cK[0] * a + cK[1] * bb + cK[2] * cc;
-            v[1][c] = cM[0] * a + cM[1] * bb + cM[2] * cc;
+            v[0][c] = T(cK[0] * a + cK[1] * bb + cK[2] * cc);
+            v[1][c] = T(cM[0] * a + cM[1] * bb + cM[2] * cc);
         }
         mask3(fixed[n], v[0]);
         mask3(fixed[n], v[1]);
     }
-    __device__ void coef(long long e, double &ck, double &cm) const { w.get(e, ck, cm); }
-    __device__ void epilogue(long long n, int, int, int, const double y[3], double *) const {
+    __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
+    __device__ void epilogue(long long n, int, int, int, const T y[3], double *) const {
         const double *u, *du, *ddu;
         prev(u, du, ddu);
         int t = st->tsc * st->block + st->j + 1;
@@ -420,7 +425,7 @@ struct PolRhsFwd {
         uint8_t f = fixed[n];
         for (int c = 0; c < 3; c++) {
             bool fx = (f >> c) & 1;
-            b[3 * n + c] = fx ? 0.0 : (rhs0[3 * n + c] * s + y[c]);
+            b[3 * n + c] = fx ? 0.0 : (rhs0[3 * n + c] * s + todbl(y[c]));
             x0[3 * n + c] = fx ? 0.0 : (pred[0] * u[3 * n + c] + pred[1] * du[3 * n + c] + pred[2] * ddu[3 * n + c]);
         }
     }

@@ -61,7 +61,7 @@ class TopOpt:
     use_graphs: bool = True
     coarse_dense_max: int = 4096
     coarse_smooth: int = 8
-    sens_fp32: bool = False
+    sens_fp32: bool = True
     inner_tol: float = 1e-4
     inner_maxit: int = 40
     # state
