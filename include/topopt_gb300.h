@@ -67,6 +67,11 @@ typedef struct topo_le_params {
     double inner_tol;        /* mixed mode: FP32 recurrence residual reduction
                                 between FP64 residual replacements                */
     int inner_maxit;         /* mixed mode: FP32 iterations between replacements    */
+    double adaptive_kappa;   /* V-cycle depth: descend only while the Jacobi-scaled
+                                operator's condition bound exceeds this; a level
+                                below it is solved by a full-spectrum Chebyshev
+                                polynomial (mass-dominated Newmark operators need
+                                no coarse correction); 0 = always full depth      */
 } topo_le_params;
 
 typedef struct topo_le_stats {
@@ -110,8 +115,8 @@ int topo_le_get_state(topo_le *le, int which, int j, double *out);
 int topo_le_apply_km(topo_le *le, const double *x, double *Kx, double *Mx);
 int topo_le_get_stats(topo_le *le, topo_le_stats *out);
 /* CUDA-event timing of the matrix-free operator apply on the object's stream:
- * `precision` 0 = FP64, 1 = FP32 (multigrid smoother), 2 = double-float (the
- * FP64-accurate passes of the mixed path);
+ * `precision` 0 = FP64, 1 = FP32 residual, 2 = double-float (the FP64-accurate
+ * passes of the mixed path), 3 = FP32 Chebyshev smoothing step;
  * `reps` back-to-back launches after `warmup`; returns mean ms per launch */
 int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double *ms_per_launch);
 /* 24x24 box element matrices (E = 1, unit density) as applied by the

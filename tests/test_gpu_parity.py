@@ -239,3 +239,19 @@ def test_finite_difference_check_on_gpu(gpu):
         xm[e] -= h
         fd = (_run_gpu(le, xp)[0] - _run_gpu(le, xm)[0]) / (2 * h)
         assert abs(fd - df[e]) <= 1e-6 * np.abs(df).max(), (e, fd, df[e])
+
+
+def test_mixed_path_is_scale_invariant(gpu):
+    # a 4-step horizon of the sine pulse leaves states ~1e-12 and adjoints far
+    # smaller: the FP32 recurrence must not underflow (it runs on residuals
+    # scaled to unit RMS)
+    n = (16, 8, 8)
+    kw = dict(ncp=1, tsc=4, t1=0.02, objective=3, loadsignal=1, dalpha=0.0, dbeta=1e-3)
+    x = np.full(np.prod(n), 0.12)
+    le = _le(n, nlvls=1, coarse_smooth=10, mixed=True, rtol=1e-10, sens_fp32=False, **kw)
+    fx, df = _run_gpu(le, x)
+    ref = O.LinearElasticity(*n, **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert fx_r < 1e-10
+    assert abs(fx - fx_r) <= 1e-8 * abs(fx_r)
+    assert _rel(df, df_r) < 1e-7

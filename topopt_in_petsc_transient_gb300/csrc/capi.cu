@@ -100,6 +100,7 @@ void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz) {
     p->sens_fp32 = 1;
     p->inner_tol = 1e-4;
     p->inner_maxit = 40;
+    p->adaptive_kappa = 40.0;
 }
 
 int topo_le_create(topo_le **out, const topo_le_params *p) {
@@ -216,7 +217,7 @@ int topo_le_get_stats(topo_le *le, topo_le_stats *out) {
 }
 
 int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double *ms_per_launch) {
-    if (!le || !ms_per_launch || reps < 1 || warmup < 0 || precision < 0 || precision > 2) return TOPO_ERR_ARG;
+    if (!le || !ms_per_launch || reps < 1 || warmup < 0 || precision < 0 || precision > 3) return TOPO_ERR_ARG;
     return le_time_apply(le->impl, precision, warmup, reps, ms_per_launch);
 }
 

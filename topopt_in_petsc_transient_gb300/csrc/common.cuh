@@ -47,15 +47,36 @@ struct GridDesc {
 // therefore applied with ~290 flops instead of the 1536 of the dense 24x24
 // products of LinearElasticity.cc:3089-3333, with identical results up to
 // rounding (the reference's truncated Gauss abscissa differs by 2e-16).
+// In the mode basis (index i = 8 c + m) the element stiffness Khat has 45
+// non-zeros that form symmetric diagonal blocks after a permutation: two 3x3,
+// six 2x2 and three 1x1 blocks (rigid translations, modes i = 0, 8, 16, are
+// its null space).  The pattern does not depend on the box shape or on nu.
+constexpr int KH_NB = 11;
+constexpr int KH_NNZ = 45;
+__host__ __device__ constexpr int kh_size(int b) { return b < 2 ? 3 : (b < 8 ? 2 : 1); }
+__host__ __device__ constexpr int kh_idx(int b, int r) {
+    // blocks: {1,10,20} {6,13,19} {2,9} {3,22} {4,17} {5,14} {11,21} {12,18} {7} {15} {23}
+    return b == 0 ? (r == 0 ? 1 : r == 1 ? 10 : 20)
+         : b == 1 ? (r == 0 ? 6 : r == 1 ? 13 : 19)
+         : b == 2 ? (r == 0 ? 2 : 9)
+         : b == 3 ? (r == 0 ? 3 : 22)
+         : b == 4 ? (r == 0 ? 4 : 17)
+         : b == 5 ? (r == 0 ? 5 : 14)
+         : b == 6 ? (r == 0 ? 11 : 21)
+         : b == 7 ? (r == 0 ? 12 : 18)
+         : b == 8 ? 7 : b == 9 ? 15 : 23;
+}
+
 template <class T>
 struct ElemConst {
-    T W[8];     // V * w_p * w_q * w_r
-    T g[3];     // 2 / h_a
-    T lam, mu;  // Lame parameters for E = 1 (LinearElasticity.cc:3134-3135)
+    T W[8];      // V * w_p * w_q * w_r
+    T g[3];      // 2 / h_a
+    T lam, mu;   // Lame parameters for E = 1 (LinearElasticity.cc:3134-3135)
+    T K[KH_NNZ]; // Khat blocks, row-major per block, blocks in kh_idx order
 };
 
 template <class T>
-__host__ __device__ inline ElemConst<T> make_elem_const(double hx, double hy, double hz, double nu) {
+__host__ __device__ inline ElemConst<T> make_elem_const_base(double hx, double hy, double hz, double nu) {
     ElemConst<T> c;
     double V = hx * hy * hz;
     const double w[2] = {0.25, 1.0 / 12.0};
@@ -65,6 +86,7 @@ __host__ __device__ inline ElemConst<T> make_elem_const(double hx, double hy, do
     c.g[2] = (T)(2.0 / hz);
     c.lam = (T)(nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
     c.mu = (T)(1.0 / (2.0 * (1.0 + nu)));
+    for (int i = 0; i < KH_NNZ; i++) c.K[i] = (T)0.0;
     return c;
 }
 
@@ -133,6 +155,73 @@ __host__ __device__ __forceinline__ void mode_stiffness(const ElemConst<T> &C, c
                 if (a == b) S += C.lam * D[m];
                 Y[b][m | (1 << a)] += C.g[a] * (C.W[m] * S);
             }
+}
+
+// element constants including the Khat blocks, evaluated in double by
+// applying the exact mode-basis stiffness to unit mode vectors
+template <class T>
+inline ElemConst<T> make_elem_const(double hx, double hy, double hz, double nu) {
+    ElemConst<T> c = make_elem_const_base<T>(hx, hy, hz, nu);
+    ElemConst<double> d = make_elem_const_base<double>(hx, hy, hz, nu);
+    double Kh[24][24];
+    for (int j = 0; j < 24; j++) {
+        double U[3][8] = {{0}}, Y[3][8];
+        U[j / 8][j % 8] = 1.0;
+        mode_stiffness(d, U, Y);
+        for (int i = 0; i < 24; i++) Kh[i][j] = Y[i / 8][i % 8];
+    }
+    int k = 0;
+    for (int b = 0; b < KH_NB; b++)
+        for (int r = 0; r < kh_size(b); r++)
+            for (int s = 0; s < kh_size(b); s++) c.K[k++] = (T)Kh[kh_idx(b, r)][kh_idx(b, s)];
+    return c;
+}
+
+// Y = Khat U with the block structure (45 multiply-adds); U, Y in [comp][mode]
+template <class T>
+__host__ __device__ __forceinline__ void mode_khat(const ElemConst<T> &C, const T U[3][8], T Y[3][8]) {
+    Y[0][0] = Y[1][0] = Y[2][0] = T(0);
+    int k = 0;
+#pragma unroll
+    for (int b = 0; b < KH_NB; b++) {
+        const int n = kh_size(b);
+#pragma unroll
+        for (int r = 0; r < n; r++) {
+            const int ir = kh_idx(b, r);
+            T acc = C.K[k + r * n] * U[kh_idx(b, 0) / 8][kh_idx(b, 0) % 8];
+#pragma unroll
+            for (int s = 1; s < n; s++) acc += C.K[k + r * n + s] * U[kh_idx(b, s) / 8][kh_idx(b, s) % 8];
+            Y[ir / 8][ir % 8] = acc;
+        }
+        k += n * n;
+    }
+}
+
+// Y = ck Khat U + cm W .* U (stiffness + mass in mode space); each U entry
+// is consumed by one block, so the live range shrinks as blocks complete
+template <class T>
+__host__ __device__ __forceinline__ void mode_khat_mass(const ElemConst<T> &C, T ck, T cm, const T U[3][8],
+                                                        T Y[3][8]) {
+    T cw[8];
+#pragma unroll
+    for (int m = 0; m < 8; m++) cw[m] = cm * C.W[m];
+    Y[0][0] = cw[0] * U[0][0];
+    Y[1][0] = cw[0] * U[1][0];
+    Y[2][0] = cw[0] * U[2][0];
+    int k = 0;
+#pragma unroll
+    for (int b = 0; b < KH_NB; b++) {
+        const int n = kh_size(b);
+#pragma unroll
+        for (int r = 0; r < n; r++) {
+            const int ir = kh_idx(b, r);
+            T acc = C.K[k + r * n] * U[kh_idx(b, 0) / 8][kh_idx(b, 0) % 8];
+#pragma unroll
+            for (int s = 1; s < n; s++) acc += C.K[k + r * n + s] * U[kh_idx(b, s) / 8][kh_idx(b, s) % 8];
+            Y[ir / 8][ir % 8] = ck * acc + cw[ir % 8] * U[ir / 8][ir % 8];
+        }
+        k += n * n;
+    }
 }
 
 // y_e = ck * KE u_e + cm * ME u_e for one element: in/out indexed [comp][L]

@@ -156,6 +156,7 @@ static __global__ void k_bounds_init(unsigned long long *bits) {
 
 // Chebyshev interval: [max(lo_bound, hi/ratio), hi]; the Dirichlet identity
 // rows contribute eigenvalue 1 and are kept inside the interval.
+// lohi[0..1]: smoothing interval, lohi[2..3]: full-spectrum bounds
 static __global__ void k_bounds_final(const unsigned long long *bits, double ratio, double *lohi) {
     double hi = __longlong_as_double((long long)bits[0]);
     double lo = __longlong_as_double((long long)bits[1]);
@@ -164,6 +165,8 @@ static __global__ void k_bounds_final(const unsigned long long *bits, double rat
     l = fmin(l, 1.0);
     lohi[0] = l;
     lohi[1] = hi;
+    lohi[2] = fmin(lo, 1.0);
+    lohi[3] = hi;
 }
 
 // first Chebyshev step from a zero initial guess: d = Dinv b / theta, x = d
@@ -382,6 +385,14 @@ static __global__ void k_fcg_update(long long ndof, double *x, double *r, float 
 }
 
 // mixed-precision FCG pieces (FP32 vectors, FP64 scalars and iterate)
+// r32 = sigma * r after an FP64 residual (init or replacement)
+static __global__ void k_mfcg_scale(long long ndof, const double *__restrict__ r, float *r32, const SolveScalars *S) {
+    if (!S->rescale) return;
+    double sg = S->sigma;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)
+        r32[i] = (float)(sg * r[i]);
+}
+
 static __global__ void k_mfcg_dot(long long ndof, const float *__restrict__ z, const float *__restrict__ r32,
                                   const float *__restrict__ q32, SolveScalars *S, Partials<2> part) {
     float s0 = 0.0f, s1 = 0.0f;
@@ -397,6 +408,7 @@ static __global__ void k_mfcg_dot(long long ndof, const float *__restrict__ z, c
         S->gam = tot[1];
         S->beta = S->restart ? 0.0 : -tot[1] / S->pq;
         if (!isfinite(S->beta)) S->beta = 0.0;
+        S->rescale = 0;
     }
 }
 
@@ -410,9 +422,10 @@ static __global__ void k_mfcg_update(long long ndof, double *x, float *r32, cons
                                      const float *__restrict__ q, SolveScalars *S, Partials<1> part) {
     double alpha = S->alpha;
     float af = (float)alpha;
+    double ax = alpha / S->sigma;  // correction in unscaled units
     float s = 0.0f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
-        x[i] += alpha * (double)p[i];
+        x[i] += ax * (double)p[i];
         float rv = r32[i] - af * q[i];
         r32[i] = rv;
         s += rv * rv;

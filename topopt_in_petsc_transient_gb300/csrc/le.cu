@@ -162,11 +162,14 @@ struct OpLevel {
     double *dinvd = nullptr;
     float *dinvf = nullptr;
     double *lohi = nullptr;  // device [2]
-    double *cheb = nullptr;  // device [kmax][2] Chebyshev step coefficients
+    double *cheb = nullptr;   // device [kmax][2] Chebyshev step coefficients (smoothing)
+    double *chebf = nullptr;  // same over the full spectrum (smoother-as-solver level)
+    double hlohi[4] = {0, 0, 0, 0};
 };
 
 struct Operator {
     double sK = 0.0, sM = 1.0;  // A = sK * K(kf) + sM * M(mf)
+    int depth = 1;              // levels the V-cycle descends (adaptive)
     std::vector<OpLevel> lv;
     double *Ainv_d = nullptr;
     float *Ainv_f = nullptr;
@@ -216,6 +219,7 @@ struct TopoLE {
     // graphs
     cudaGraphExec_t gx_fwd = nullptr, gx_adj = nullptr;
     int graphs_ok = 0;
+    int captured_depth = -1;  // V-cycle depth baked into the step graphs
     // diagnostics
     LEStats stats;
     int last_block_resident = -1;
@@ -459,8 +463,9 @@ int le_alloc(TopoLE *le) {
             long long lnd = 3 * le->L[l].g.nn();
             AG(op.lv[l].dinvd, lnd);
             AG(op.lv[l].dinvf, lnd);
-            AG(op.lv[l].lohi, 2);
+            AG(op.lv[l].lohi, 4);
             AG(op.lv[l].cheb, 2 * 64);
+            AG(op.lv[l].chebf, 2 * 64);
         }
         if (le->coarse_dense) {
             AG(op.Ainv_d, (size_t)le->ncoarse * le->ncoarse);
@@ -507,6 +512,25 @@ static int setup_operator(TopoLE *le, int o) {
         k_bounds_final<<<1, 1, 0, s>>>(le->bbits, le->p.cheb_ratio, op.lv[l].lohi);
         count_launch();
         k_cheb_table<<<1, 1, 0, s>>>(op.lv[l].lohi, cheb_kmax(le), op.lv[l].cheb);
+        count_launch();
+        k_cheb_table<<<1, 1, 0, s>>>(op.lv[l].lohi + 2, cheb_kmax(le), op.lv[l].chebf);
+    }
+    // adaptive depth: stop at the first level whose Jacobi-scaled operator is
+    // well conditioned (bound hi/lo <= adaptive_kappa); a full-spectrum
+    // Chebyshev polynomial solves it, so coarser corrections add nothing
+    op.depth = le->nlev;
+    if (le->p.adaptive_kappa > 0.0) {
+        for (int l = 0; l < le->nlev; l++) {
+            CK(cudaMemcpyAsync(op.lv[l].hlohi, op.lv[l].lohi, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        CK(cudaStreamSynchronize(s));
+        for (int l = 0; l < le->nlev - 1; l++) {
+            const double *hb = op.lv[l].hlohi;
+            if (hb[2] > 0.0 && hb[3] / hb[2] <= le->p.adaptive_kappa) {
+                op.depth = l + 1;
+                break;
+            }
+        }
     }
     // dense coarsest operator and its inverse (FP64 Gauss-Jordan)
     if (!le->coarse_dense) {
@@ -570,6 +594,20 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b) {
     Weights<T> wt{op.sK != 0.0 ? w.kf : nullptr, w.mf, nullptr, (T)op.sK, (T)op.sM};
     const double *lohi = op.lv[l].cheb;
     T *x = w.xa, *xo = w.xb;
+    if (l == op.depth - 1 && op.depth < le->nlev) {
+        // well-conditioned level: full-spectrum Chebyshev-Jacobi solve from zero
+        const double *full = op.lv[l].chebf;
+        count_launch();
+        k_cheb0<T><<<ew_blocks(nd), EW, 0, s>>>(nd, b, w.dinv, full, x, w.d);
+        for (int k = 1; k < le->p.coarse_smooth; k++) {
+            PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, full, k, {}};
+            launch_tile<T>(lv.g, *w.C, pc, s);
+            T *t = x;
+            x = xo;
+            xo = t;
+        }
+        return x;
+    }
     if (l == le->nlev - 1) {
         if (le->coarse_dense) {
             int n = le->ncoarse;
@@ -621,7 +659,8 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b) {
 // ---------------------------------------------------------------------------
 // flexible CG:  (N A N + I - N) x = b for operator o; sx holds the initial guess
 // ---------------------------------------------------------------------------
-__global__ void k_solve_prime(SolveScalars *S, double tol2, int maxit, double tau2, int kmax) {
+__global__ void k_solve_prime(SolveScalars *S, double tol2, int maxit, double tau2, int kmax, double ndof) {
+    S->ndof = ndof;
     S->tol2 = tol2;
     S->maxit = maxit;
     S->tau2 = tau2;
@@ -666,6 +705,8 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
     unsigned nb = ew_blocks(nd);
     if (le->p.mixed) {
         // reliable-update mixed precision: FP32 recurrence, FP64 replacements
+        count_launch();
+        k_mfcg_scale<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sr, le->sr32, le->S);
         float *z = vcycle<float>(le, o, 0, le->sr32);
         count_launch();
         k_mfcg_dot<<<red_blocks(nd), EW, 0, s>>>(nd, z, le->sr32, le->sq32, le->S, P2(le));
@@ -699,7 +740,8 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
 static int solve_direct(TopoLE *le, int o, const double *b) {
     count_launch();
     k_solve_prime<<<1, 1, 0, le->stream>>>(le->S, le->p.rtol * le->p.rtol, le->p.maxit,
-                                              le->p.inner_tol * le->p.inner_tol, le->p.inner_maxit);
+                                              le->p.inner_tol * le->p.inner_tol, le->p.inner_maxit,
+                                              (double)le->ndof);
     solve_init(le, o, b, 0, 0);
     SolveScalars h;
     for (;;) {
@@ -724,7 +766,7 @@ static int solve_captured(TopoLE *le, int o, const double *b) {
     cudaStream_t s = le->stream;
     count_launch();
     k_solve_prime<<<1, 1, 0, s>>>(le->S, le->p.rtol * le->p.rtol, le->p.maxit, le->p.inner_tol * le->p.inner_tol,
-                                  le->p.inner_maxit);
+                                  le->p.inner_maxit, (double)le->ndof);
     cudaStreamCaptureStatus cs;
     cudaGraph_t graph;
     const cudaGraphNode_t *deps = nullptr;
@@ -1018,6 +1060,12 @@ static int lagrange0(TopoLE *le) {
 
 // graph of one step, captured on first use and replayed for every step
 static int get_graph(TopoLE *le, int adjoint, cudaGraphExec_t *out) {
+    if (le->captured_depth != le->ops[0].depth) {
+        if (le->gx_fwd) cudaGraphExecDestroy(le->gx_fwd);
+        if (le->gx_adj) cudaGraphExecDestroy(le->gx_adj);
+        le->gx_fwd = le->gx_adj = nullptr;
+        le->captured_depth = le->ops[0].depth;
+    }
     cudaGraphExec_t &gx = adjoint ? le->gx_adj : le->gx_fwd;
     if (!gx) {
         CK(cudaStreamBeginCapture(le->stream, cudaStreamCaptureModeRelaxed));
@@ -1261,6 +1309,10 @@ int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms) {
             Weights<double> wt{l0.kfd, l0.mfd, nullptr, op.sK, op.sM};
             PolResid<double> pr{l0.fixed, wt, le->sp, le->sb, le->sq, {}};
             launch_tile<double>(l0.g, l0.Cd, pr, s);
+        } else if (precision == 3) {
+            Weights<float> wt{l0.kff, l0.mff, nullptr, (float)op.sK, (float)op.sM};
+            PolCheb<float> pc{l0.fixed, wt, l0.fr, l0.fb, op.lv[0].dinvf, l0.fxa, l0.fd, op.lv[0].cheb, 1, {}};
+            launch_tile<float>(l0.g, l0.Cf, pc, s);
         } else if (precision == 2) {
             Weights<df> wt = fine_weights<df>(le, true, true, nullptr, op.sK, op.sM);
             PolProduct<df, true, true> pp{wt, le->sp, le->sq, {}};

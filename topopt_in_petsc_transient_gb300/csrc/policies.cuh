@@ -32,6 +32,10 @@ struct SolveScalars {
     double rr_ref, tau2;
     int need_replace, restart, inner_it, kmax;
     int replacements, breakdowns32;
+    // the FP32 recurrence runs on r32 = sigma * r (sigma = 1/rms(r) at the
+    // last FP64 residual), so FP32 never sees the absolute scale of the state
+    double sigma, ndof;
+    int rescale;
 };
 
 // ---------------------------------------------------------------------------
@@ -79,7 +83,6 @@ struct PolInitResid {
             double ax = ((f >> c) & 1) ? xv : todbl(y[c]);
             double rv = bv - ax;
             r[3 * n + c] = rv;
-            if (r32) r32[3 * n + c] = (float)rv;
             red[0] += bv * bv;
             red[1] += rv * rv;
         }
@@ -91,10 +94,12 @@ struct PolInitResid {
         S->status = 0;
         S->zero_x = (t[0] == 0.0);
         S->done = (t[0] == 0.0) || (t[1] <= S->tol2 * t[0]);
-        S->rr_ref = t[1];
         S->need_replace = 0;
         S->restart = 1;
         S->inner_it = 0;
+        S->sigma = (t[1] > 0.0) ? sqrt(S->ndof / t[1]) : 1.0;
+        S->rr_ref = t[1] * S->sigma * S->sigma;
+        S->rescale = (r32 != nullptr);
         if (!isfinite(t[1])) {
             S->status = TOPO_ERR_NAN;
             S->done = 1;
@@ -168,12 +173,21 @@ struct PolPQ32 {
         mask3(fixed[n], v[0]);
     }
     __device__ void coef(long long e, float &ck, float &cm) const { w.get(e, ck, cm); }
-    __device__ void epilogue(long long n, int, int, int, const float y[3], double red[1]) const {
-        uint8_t f = fixed[n];
+    struct Pre {
+        float p[3];
+        uint8_t f;
+    };
+    __device__ Pre pre(long long n) const {
+        Pre r;
+        for (int c = 0; c < 3; c++) r.p[c] = p[3 * n + c];
+        r.f = fixed[n];
+        return r;
+    }
+    __device__ void epilogue(long long n, int, int, int, const float y[3], double red[1], const Pre &r) const {
         float s = 0.0f;
         for (int c = 0; c < 3; c++) {
-            float pv = p[3 * n + c];
-            float qv = ((f >> c) & 1) ? pv : y[c];
+            float pv = r.p[c];
+            float qv = ((r.f >> c) & 1) ? pv : y[c];
             q[3 * n + c] = qv;
             s += pv * qv;
         }
@@ -221,17 +235,18 @@ struct PolReplace {
             double xv = x[3 * n + c];
             double rv = b[3 * n + c] - (((f >> c) & 1) ? xv : todbl(y[c]));
             r[3 * n + c] = rv;
-            r32[3 * n + c] = (float)rv;
             red[0] += rv * rv;
         }
     }
     __device__ void finish(const double t[1]) const {
         S->rr = t[0];
-        S->rr_ref = t[0];
         S->need_replace = 0;
         S->restart = 1;
         S->inner_it = 0;
         S->replacements += 1;
+        S->sigma = (t[0] > 0.0) ? sqrt(S->ndof / t[0]) : 1.0;
+        S->rr_ref = t[0] * S->sigma * S->sigma;
+        S->rescale = 1;
         if (!isfinite(t[0])) {
             S->status = TOPO_ERR_NAN;
             S->done = 1;
@@ -286,15 +301,28 @@ struct PolCheb {
         mask3(fixed[n], v[0]);
     }
     __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
-    __device__ void epilogue(long long n, int, int, int, const T y[3], double *) const {
-        const T c1 = (T)ctab[2 * k], c2 = (T)ctab[2 * k + 1];
-        uint8_t f = fixed[n];
+    struct Pre {
+        T x[3], b[3], di[3], d[3];
+        uint8_t f;
+    };
+    __device__ Pre pre(long long n) const {
+        Pre q;
         for (int c = 0; c < 3; c++) {
-            T xv = x_in[3 * n + c];
-            T rv = b[3 * n + c] - (((f >> c) & 1) ? xv : y[c]);
-            T dv = (k == 0 ? T(0) : c1 * d[3 * n + c]) + c2 * dinv[3 * n + c] * rv;
+            q.x[c] = x_in[3 * n + c];
+            q.b[c] = b[3 * n + c];
+            q.di[c] = dinv[3 * n + c];
+            q.d[c] = (k == 0) ? T(0) : d[3 * n + c];
+        }
+        q.f = fixed[n];
+        return q;
+    }
+    __device__ void epilogue(long long n, int, int, int, const T y[3], double *, const Pre &q) const {
+        const T c1 = (T)ctab[2 * k], c2 = (T)ctab[2 * k + 1];
+        for (int c = 0; c < 3; c++) {
+            T rv = q.b[c] - (((q.f >> c) & 1) ? q.x[c] : y[c]);
+            T dv = c1 * q.d[c] + c2 * q.di[c] * rv;
             d[3 * n + c] = dv;
-            x_out[3 * n + c] = xv + dv;
+            x_out[3 * n + c] = q.x[c] + dv;
         }
     }
     __device__ void finish(const double *) const {}

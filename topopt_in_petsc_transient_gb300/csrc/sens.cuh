@@ -158,7 +158,7 @@ template <class T>
 __device__ __forceinline__ T quad_K(const ElemConst<T> &C, T A[3][8], T B[3][8]) {
     // A, B already in mode space; returns A' Khat B
     T Y[3][8];
-    mode_stiffness(C, B, Y);
+    mode_khat(C, B, Y);
     T s = T(0);
 #pragma unroll
     for (int c = 0; c < 3; c++)
@@ -208,13 +208,27 @@ static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const Elem
 #pragma unroll
         for (int L = 0; L < 8; L++)
             nodes[L] = (i + (L & 1)) + (long long)g.nx * ((jj + ((L >> 1) & 1)) + (long long)g.ny * (k + (L >> 2)));
-        T Lm[3][8], WK[3][8], WM[3][8];
-        gather8<T>(A.lam, nodes, Lm);
-        // combination vectors (nodal), then transform
+        // lam' KE wK = (Khat Lam)' WK in mode space (Khat symmetric); the
+        // combination vectors are formed one component at a time so only
+        // Khat Lam and W Lam stay live
+        T KL[3][8], ML[3][8];
+        {
+            T Lm[3][8];
+            gather8<T>(A.lam, nodes, Lm);
 #pragma unroll
-        for (int L = 0; L < 8; L++)
+            for (int c = 0; c < 3; c++) mode_fwd(Lm[c]);
+            mode_khat(C, Lm, KL);
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
+            for (int c = 0; c < 3; c++)
+#pragma unroll
+                for (int m = 0; m < 8; m++) ML[c][m] = C.W[m] * Lm[c][m];
+        }
+        T sK = T(0), sM = T(0);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            T wk8[8], wm8[8];
+#pragma unroll
+            for (int L = 0; L < 8; L++) {
                 long long q = 3 * nodes[L] + c;
                 double s0 = u[q], s1 = du[q], s2 = ddu[q];
                 double wk = A.aK[0] * s0 + A.aK[1] * s1 + A.aK[2] * s2;
@@ -224,17 +238,19 @@ static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const Elem
                     wk += A.bK[0] * p0 + A.bK[1] * p1 + A.bK[2] * p2;
                     wm += A.bM[0] * p0 + A.bM[1] * p1 + A.bM[2] * p2;
                 }
-                WK[c][L] = (T)wk;
-                WM[c][L] = (T)wm;
+                wk8[L] = (T)wk;
+                wm8[L] = (T)wm;
             }
+            mode_fwd(wk8);
+            mode_fwd(wm8);
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            mode_fwd(Lm[c]);
-            mode_fwd(WK[c]);
-            mode_fwd(WM[c]);
+            for (int m = 0; m < 8; m++) {
+                sK += KL[c][m] * wk8[m];
+                sM += ML[c][m] * wm8[m];
+            }
         }
         double dkfe = A.dkf[e], dmfe = A.dmf[e], kfe = A.kf[e], mfe = A.mf[e], Pe = A.P[e];
-        double t3 = dkfe * (double)quad_K(C, Lm, WK) + dmfe * (double)quad_M(C, Lm, WM);
+        double t3 = dkfe * (double)sK + dmfe * (double)sM;
         // objective value h0 and its explicit density derivative dfx0
         double h0 = 0.0, dfx0 = 0.0;
         if (OBJ == 0 || OBJ == 1 || OBJ == 2) {

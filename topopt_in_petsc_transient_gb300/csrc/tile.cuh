@@ -56,6 +56,29 @@ __device__ __forceinline__ bool pol_skip(const P &, long) {
     return false;
 }
 
+// optional epilogue-operand prefetch: a policy may define `Pre pre(long long n)`
+// and `epilogue(n, i, j, k, y, red, const Pre &)`; the kernel issues pre()
+// before the element phase so the loads overlap the element arithmetic
+struct NoPre {};
+template <class P>
+__device__ __forceinline__ auto pol_pre(const P &p, long long n, int) -> decltype(p.pre(n)) {
+    return p.pre(n);
+}
+template <class P>
+__device__ __forceinline__ NoPre pol_pre(const P &, long long, long) {
+    return NoPre{};
+}
+template <class P, class T, class R>
+__device__ __forceinline__ auto pol_epi(const P &p, long long n, int i, int j, int k, const T y[3], double *red,
+                                        const R &pre, int) -> decltype(p.epilogue(n, i, j, k, y, red, pre)) {
+    return p.epilogue(n, i, j, k, y, red, pre);
+}
+template <class P, class T, class R>
+__device__ __forceinline__ void pol_epi(const P &p, long long n, int i, int j, int k, const T y[3], double *red,
+                                        const R &, long) {
+    p.epilogue(n, i, j, k, y, red);
+}
+
 template <class T, class Pol>
 __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(const GridDesc g, const ElemConst<T> C, const Pol pol) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -65,23 +88,41 @@ __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(c
     const int i0 = blockIdx.x * TILE, j0 = blockIdx.y * TILE, k0 = blockIdx.z * TILE;
     if (pol_skip(pol, 0)) return;
 
-    // ---- stage inputs (brick + halo), zero outside the domain ----
-    for (int s = tid; s < TILE_STAGED; s += TILE_THREADS) {
-        int lx = s % TILE_N, ly = (s / TILE_N) % TILE_N, lz = s / (TILE_N * TILE_N);
-        int gi = i0 - 1 + lx, gj = j0 - 1 + ly, gk = k0 - 1 + lz;
-        T v[Pol::NIN][3];
-        if (gi >= 0 && gi < g.nx && gj >= 0 && gj < g.ny && gk >= 0 && gk < g.nz) {
-            long long n = gi + (long long)g.nx * (gj + (long long)g.ny * gk);
-            pol.load(n, v);
-        } else {
+    // ---- stage inputs (brick + halo), zero outside the domain: every
+    // thread issues its (at most two) node loads before any shared store ----
+    static_assert(TILE_STAGED <= 2 * TILE_THREADS, "staging assumes two passes");
+    {
+        T v[2][Pol::NIN][3];
 #pragma unroll
-            for (int f = 0; f < Pol::NIN; f++) v[f][0] = v[f][1] = v[f][2] = T(0);
+        for (int it = 0; it < 2; it++) {
+            const int s = tid + it * TILE_THREADS;
+            const int lx = s % TILE_N, ly = (s / TILE_N) % TILE_N, lz = s / (TILE_N * TILE_N);
+            const int gi = i0 - 1 + lx, gj = j0 - 1 + ly, gk = k0 - 1 + lz;
+            if (s < TILE_STAGED && gi >= 0 && gi < g.nx && gj >= 0 && gj < g.ny && gk >= 0 && gk < g.nz) {
+                long long n = gi + (long long)g.nx * (gj + (long long)g.ny * gk);
+                pol.load(n, v[it]);
+            } else {
+#pragma unroll
+                for (int f = 0; f < Pol::NIN; f++) v[it][f][0] = v[it][f][1] = v[it][f][2] = T(0);
+            }
         }
 #pragma unroll
-        for (int f = 0; f < Pol::NIN; f++)
+        for (int it = 0; it < 2; it++) {
+            const int s = tid + it * TILE_THREADS;
+            if (s < TILE_STAGED) {
 #pragma unroll
-            for (int c = 0; c < 3; c++) sIn[(f * TILE_STAGED + s) * 3 + c] = v[f][c];
+                for (int f = 0; f < Pol::NIN; f++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) sIn[(f * TILE_STAGED + s) * 3 + c] = v[it][f][c];
+            }
+        }
     }
+    // output node of this thread and its prefetched epilogue operands
+    const int tx = tid % TILE, ty = (tid / TILE) % TILE, tz = tid / (TILE * TILE);
+    const int oi = i0 + tx, oj = j0 + ty, ok = k0 + tz;
+    const bool has_out = tid < TILE_OUT && oi < g.nx && oj < g.ny && ok < g.nz;
+    const long long on = has_out ? oi + (long long)g.nx * (oj + (long long)g.ny * ok) : 0;
+    const auto pre = pol_pre(pol, on, 0);
     __syncthreads();
 
     // ---- one element per thread ----
@@ -102,56 +143,47 @@ __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(c
             }
 #pragma unroll
             for (int c = 0; c < 3; c++) mode_fwd(U[c]);
-            T D[8];
-            if (Pol::HAS_K) {
+            T Y[3][8];
+            if (Pol::HAS_K && Pol::HAS_M && Pol::NIN == 1) {
+                mode_khat_mass(C, ck, cm, U, Y);
+            } else {
+                if (Pol::HAS_K) {
+                    mode_khat(C, U, Y);
 #pragma unroll
-                for (int m = 0; m < 8; m++) {
-                    T acc = T(0);
+                    for (int c = 0; c < 3; c++)
 #pragma unroll
-                    for (int a = 0; a < 3; a++)
-                        if (!(m & (1 << a))) acc += C.g[a] * U[a][m | (1 << a)];
-                    D[m] = acc;
+                        for (int m = 0; m < 8; m++) Y[c][m] *= ck;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 3; c++)
+#pragma unroll
+                        for (int m = 0; m < 8; m++) Y[c][m] = T(0);
+                }
+                if (Pol::HAS_M) {
+#pragma unroll
+                    for (int b = 0; b < 3; b++) {
+                        T V[8];
+                        if (Pol::NIN == 2) {
+#pragma unroll
+                            for (int L = 0; L < 8; L++) {
+                                int s = (lx + (L & 1)) + TILE_N * ((ly + ((L >> 1) & 1)) + TILE_N * (lz + (L >> 2)));
+                                V[L] = sIn[((Pol::NIN - 1) * TILE_STAGED + s) * 3 + b];
+                            }
+                            mode_fwd(V);
+                        } else {
+#pragma unroll
+                            for (int m = 0; m < 8; m++) V[m] = U[b][m];
+                        }
+#pragma unroll
+                        for (int m = 0; m < 8; m++) Y[b][m] += (cm * C.W[m]) * V[m];
+                    }
                 }
             }
 #pragma unroll
             for (int b = 0; b < 3; b++) {
-                T Y[8];
+                mode_bwd(Y[b]);
 #pragma unroll
-                for (int m = 0; m < 8; m++) Y[m] = T(0);
-                if (Pol::HAS_K) {
-#pragma unroll
-                    for (int a = 0; a < 3; a++)
-#pragma unroll
-                        for (int m = 0; m < 8; m++) {
-                            if (m & (1 << a)) continue;
-                            T sym = C.g[a] * U[b][m | (1 << a)];
-                            if (!(m & (1 << b))) sym += C.g[b] * U[a][m | (1 << b)];
-                            T S = C.mu * sym;
-                            if (a == b) S += C.lam * D[m];
-                            Y[m | (1 << a)] += (C.g[a] * C.W[m]) * S;
-                        }
-#pragma unroll
-                    for (int m = 0; m < 8; m++) Y[m] *= ck;
-                }
-                if (Pol::HAS_M) {
-                    T V[8];
-                    if (Pol::NIN == 2) {
-#pragma unroll
-                        for (int L = 0; L < 8; L++) {
-                            int s = (lx + (L & 1)) + TILE_N * ((ly + ((L >> 1) & 1)) + TILE_N * (lz + (L >> 2)));
-                            V[L] = sIn[((Pol::NIN - 1) * TILE_STAGED + s) * 3 + b];
-                        }
-                        mode_fwd(V);
-                    } else {
-#pragma unroll
-                        for (int m = 0; m < 8; m++) V[m] = U[b][m];
-                    }
-#pragma unroll
-                    for (int m = 0; m < 8; m++) Y[m] += (cm * C.W[m]) * V[m];
-                }
-                mode_bwd(Y);
-#pragma unroll
-                for (int L = 0; L < 8; L++) out[L * 3 + b] = Y[L];
+                for (int L = 0; L < 8; L++) out[L * 3 + b] = Y[b][L];
             }
         } else {
 #pragma unroll
@@ -164,21 +196,16 @@ __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(c
     double red[Pol::NRED > 0 ? Pol::NRED : 1];
 #pragma unroll
     for (int r = 0; r < (Pol::NRED > 0 ? Pol::NRED : 1); r++) red[r] = 0.0;
-    if (tid < TILE_OUT) {
-        const int tx = tid % TILE, ty = (tid / TILE) % TILE, tz = tid / (TILE * TILE);
-        const int gi = i0 + tx, gj = j0 + ty, gk = k0 + tz;
-        if (gi < g.nx && gj < g.ny && gk < g.nz) {
-            T y[3] = {T(0), T(0), T(0)};
+    if (has_out) {
+        T y[3] = {T(0), T(0), T(0)};
 #pragma unroll
-            for (int L = 0; L < 8; L++) {
-                int ax = L & 1, ay = (L >> 1) & 1, az = L >> 2;
-                int le = (tx + 1 - ax) + TILE_E * ((ty + 1 - ay) + TILE_E * (tz + 1 - az));
+        for (int L = 0; L < 8; L++) {
+            int ax = L & 1, ay = (L >> 1) & 1, az = L >> 2;
+            int le = (tx + 1 - ax) + TILE_E * ((ty + 1 - ay) + TILE_E * (tz + 1 - az));
 #pragma unroll
-                for (int c = 0; c < 3; c++) y[c] += sEl[le * EL_STRIDE + L * 3 + c];
-            }
-            long long n = gi + (long long)g.nx * (gj + (long long)g.ny * gk);
-            pol.epilogue(n, gi, gj, gk, y, red);
+            for (int c = 0; c < 3; c++) y[c] += sEl[le * EL_STRIDE + L * 3 + c];
         }
+        pol_epi(pol, on, oi, oj, ok, y, red, pre, 0);
     }
     if constexpr (Pol::NRED > 0) {
         double tot[Pol::NRED];

@@ -48,7 +48,8 @@ class LinearElasticity:
                  stiffnessInterpolation=1, massInterpolation=0, t0=0.0, boundaries=1, loadloc=1, reduction=False,
                  basis=5, dalpha=1e-4, dbeta=1e-4, omega0=1.0, optimizationRegion=2, V0=None, h=(1.0, 1.0, 1.0),
                  loadsignal=0, mixed=True, rtol=1e-10, maxit=500, smooth=3, cheb_ratio=30.0, use_graphs=True,
-                 coarse_dense_max=None, coarse_smooth=None, sens_fp32=None, inner_tol=None, inner_maxit=None):
+                 coarse_dense_max=None, coarse_smooth=None, sens_fp32=None, inner_tol=None, inner_maxit=None,
+                 adaptive_kappa=None):
         if reduction:
             raise TopoError(1, "LinearElasticity", "the SOMMG reduced-order path is not part of this build")
         L = _lib.load()
@@ -72,6 +73,8 @@ class LinearElasticity:
             p.inner_tol = inner_tol
         if inner_maxit is not None:
             p.inner_maxit = inner_maxit
+        if adaptive_kappa is not None:
+            p.adaptive_kappa = adaptive_kappa
         self.params = p
         self.nelx, self.nely, self.nelz = nelx, nely, nelz
         self.nel = nelx * nely * nelz
