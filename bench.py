@@ -196,27 +196,39 @@ def run_gb300(args):
     if args.e2e_steps > 0:
         e2e = run_e2e(args, wl, flush_l2)
 
-    # ---- live roofline of the operator apply kernels (CUDA events on the library stream) ----
+    # ---- roofline of the dominant kernel, timed in the solve ----
+    # The fine-level FP32 Chebyshev smoothing step k_tile<float,PolCheb> is
+    # the top kernel of the mixed path.  One extra design iteration (outside
+    # the timed region, same kernels launched directly instead of from CUDA
+    # graphs) brackets each of its launches with CUDA events on the library
+    # stream; achieved = algorithmic bytes per launch / mean launch time.
     import ctypes as C
     nel = opt.nel
     nn = (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1)
-    ms = {}
-    for prec, name in ((1, "fp32"), (0, "fp64")):
-        v = C.c_double()
-        _lib.check(L.topo_le_time_apply(opt.physics._h, prec, 5, 50, C.byref(v)), "time_apply")
-        ms[name] = v.value
+    probe = TopOpt(mixed=True, **dict(wl, use_graphs=False)).setup()
+    design_iteration(probe)
+    _lib.check(L.topo_le_smoother_timing(probe.physics._h, 1, None, None), "smoother_timing")
+    design_iteration(probe)
+    tot_ms, nlaunch = C.c_double(), C.c_longlong()
+    _lib.check(L.topo_le_smoother_timing(probe.physics._h, 0, C.byref(tot_ms), C.byref(nlaunch)), "smoother_timing")
+    ms_launch = tot_ms.value / max(1, nlaunch.value)
+    ms_fp64 = C.c_double()
+    _lib.check(L.topo_le_time_apply(probe.physics._h, 0, 5, 50, C.byref(ms_fp64)), "time_apply")
+    del probe
     peaks = load_peaks()
-    # algorithmic bytes of r = b - A x (masked): read x, b; write r (3 nn each);
-    # element factors kf, mf (nel each); fixed mask (nn bytes)
-    s32 = 4
-    bytes32 = 3 * nn * 3 * s32 + 2 * nel * s32 + nn
-    achieved = bytes32 / (ms["fp32"] * 1e-3) / 1e9
-    roof = {"kernel": "k_tile<float,PolResid> (FP32 matrix-free hex8 apply, multigrid smoother)",
+    # per launch: stage x (3 nn f32), read b, 1/diag, the previous update d
+    # (absent in the first post-smoothing step, 1 of the 5 fine-level launches
+    # of a V-cycle), write d and the new iterate (3 nn f32 each), the clamp
+    # mask (1 byte/node) and the two element factors (2 nel f32)
+    bytes_cheb = (3 * 4 * (4 * 6 + 1 * 5) / 5 + 1) * nn + 2 * 4 * nel
+    achieved = bytes_cheb / (ms_launch * 1e-3) / 1e9
+    roof = {"kernel": "k_tile<float,PolCheb> (fine-level FP32 Chebyshev-Jacobi smoothing step, matrix-free hex8)",
             "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / peaks["hbm_gbs"], "traffic": args.traffic, "peak_source": peaks["source"],
-            "ms_per_launch": ms["fp32"], "algorithmic_bytes": bytes32,
-            "fp64_apply": {"ms_per_launch": ms["fp64"],
-                           "achieved_gbs": (3 * nn * 3 * 8 + 2 * nel * 8 + nn) / (ms["fp64"] * 1e-3) / 1e9}}
+            "ms_per_launch": ms_launch, "launches_timed": nlaunch.value, "algorithmic_bytes": bytes_cheb,
+            "timing": "CUDA events around every launch of one design iteration, library stream",
+            "fp64_apply": {"kernel": "k_tile<double,PolResid>", "ms_per_launch": ms_fp64.value,
+                           "achieved_gbs": (3 * nn * 3 * 8 + 2 * nel * 8 + nn) / (ms_fp64.value * 1e-3) / 1e9}}
 
     cpu = None
     if rank == 0 and args.cpu_sample and ws == 1:

@@ -119,6 +119,13 @@ int topo_le_get_stats(topo_le *le, topo_le_stats *out);
  * passes of the mixed path), 3 = FP32 Chebyshev smoothing step;
  * `reps` back-to-back launches after `warmup`; returns mean ms per launch */
 int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double *ms_per_launch);
+/* in-solve timing of the fine-level FP32 Chebyshev smoothing kernel (the
+ * dominant kernel of the mixed path): enable = 1 arms CUDA events around each
+ * of its direct launches on the object's stream (launches replayed from CUDA
+ * graphs are not seen: create the object with use_graphs = 0); enable = 0
+ * disarms, waits for the stream and returns the summed launch time (ms) and
+ * the number of timed launches.  One armed object per process. */
+int topo_le_smoother_timing(topo_le *le, int enable, double *ms_total, long long *launches);
 /* 24x24 box element matrices (E = 1, unit density) as applied by the
  * matrix-free kernels, in the local node order of DMDAGetElements_3D
  * (LinearElasticity.cc:3067-3074), row-major: the Hex8IsoparametricKE/ME

@@ -221,6 +221,11 @@ int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double 
     return le_time_apply(le->impl, precision, warmup, reps, ms_per_launch);
 }
 
+int topo_le_smoother_timing(topo_le *le, int enable, double *ms_total, long long *launches) {
+    if (!le) return TOPO_ERR_ARG;
+    return le_smoother_timing(le->impl, enable, ms_total, launches);
+}
+
 void topo_box_element_matrices(double hx, double hy, double hz, double nu, double *KE, double *ME) {
     // kernels use lexicographic local nodes L = ax + 2ay + 4az; the reference
     // order is (0,0,0),(1,0,0),(1,1,0),(0,1,0),(0,0,1),(1,0,1),(1,1,1),(0,1,1)

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "le.h"
@@ -123,6 +124,17 @@ struct Arena {
         if (rc_) return rc_;                     \
     } while (0)
 
+// In-solve timing of the fine-level FP32 Chebyshev smoothing kernel, the
+// kernel that dominates the mixed path: when armed, every direct launch of it
+// on the grid `nn` is bracketed by a pair of CUDA events on its stream.
+// Launches recorded into a CUDA graph are not timed.
+struct LaunchTimer {
+    long long nn = -1;
+    std::vector<cudaEvent_t> ev;
+    size_t used = 0;
+};
+static LaunchTimer *g_timer = nullptr;
+
 template <class T, class Pol>
 static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, cudaStream_t s) {
     static bool attr = false;
@@ -131,8 +143,29 @@ static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol
         cudaFuncSetAttribute(k_tile<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         attr = true;
     }
+    bool timed = false;
+    if (std::is_same<Pol, PolCheb<float>>::value && g_timer && g.nn() == g_timer->nn) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s, &cs);
+        timed = cs == cudaStreamCaptureStatusNone;
+        if (timed) {
+            while (g_timer->ev.size() < g_timer->used + 2) {
+                cudaEvent_t e;
+                if (cudaEventCreate(&e) != cudaSuccess) {
+                    timed = false;
+                    break;
+                }
+                g_timer->ev.push_back(e);
+            }
+        }
+        if (timed) cudaEventRecord(g_timer->ev[g_timer->used], s);
+    }
     count_launch();
     k_tile<T, Pol><<<tile_grid(g), TILE_THREADS, sm, s>>>(g, C, pol);
+    if (timed) {
+        cudaEventRecord(g_timer->ev[g_timer->used + 1], s);
+        g_timer->used += 2;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1333,6 +1366,31 @@ int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms = (double)t / reps;
+    return TOPO_OK;
+}
+int le_smoother_timing(TopoLE *le, int enable, double *ms_total, long long *launches) {
+    static LaunchTimer timer;
+    if (enable) {
+        timer.nn = le->L[0].g.nn();
+        timer.used = 0;
+        g_timer = &timer;
+        return TOPO_OK;
+    }
+    if (g_timer != &timer) {
+        set_error("smoother timing was not armed");
+        return TOPO_ERR_STATE;
+    }
+    g_timer = nullptr;
+    CK(cudaStreamSynchronize(le->stream));
+    double tot = 0.0;
+    for (size_t i = 0; i + 1 < timer.used; i += 2) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, timer.ev[i], timer.ev[i + 1]));
+        tot += t;
+    }
+    if (ms_total) *ms_total = tot;
+    if (launches) *launches = (long long)(timer.used / 2);
+    timer.used = 0;
     return TOPO_OK;
 }
 }  // namespace topo
