@@ -108,6 +108,19 @@ int topo_le_volume_constraint(topo_le *le, double *gx, double *dgdx, const doubl
 int topo_le_volume_constraint_dev(topo_le *le, double *gx, double *dgdx_dev, const double *xPhys_dev,
                                   double volfrac);
 
+/* Allocation-free volume constraint.  No counterpart in the reference: it
+ * computes what LinearElasticity::VolumeConstraint (LinearElasticity.cc:1283-1296)
+ * and topo_le_volume_constraint_dev compute, gx = mean(xPhys) - volfrac and
+ * dgdx = 1/nel, without a topo_le object and without allocating device memory
+ * (its reduction scratch is a fixed 64 KB static device array).  For callers
+ * that hold only design vectors and may not allocate.  nel must be in
+ * 1..16,777,216 (TOPO_ERR_ARG otherwise).  The first call on a device looks up
+ * the scratch address and should come before any stream capture.  Calls that
+ * overlap in time on one device share the scratch and race; each call runs on
+ * the legacy default stream and returns after gx has been copied to the host. */
+int topo_volume_constraint_noalloc_dev(long long nel, double *gx, double *dgdx_dev, const double *xPhys_dev,
+                                       double volfrac);
+
 /* inspection (tests / output): which = 0 U, 1 DU, 2 DDU of step j of the
  * resident block (j = -1: block start state); copies 3*nn values to host */
 int topo_le_get_state(topo_le *le, int which, int j, double *out);
