@@ -172,6 +172,7 @@ def run_gb300(args):
         a = TopOpt(mixed=True, **wl).setup()
         b = TopOpt(mixed=False, **wl).setup()
         fa = design_iteration(a)[0]
+        dfa = a.dfdx.clone()
         torch.cuda.synchronize()
         tp = []
         fb = None
@@ -186,8 +187,10 @@ def run_gb300(args):
             tp.append(e0.elapsed_time(e1) / 1e3)
             if k == 0:
                 fb = r[0]
+                dfb = b.dfdx.clone()
         plain = {"value": len(tp) / sum(tp), "unit": UNIT, "steps": len(tp),
                  "objective_rel_diff_mixed_vs_plain": abs(fa - fb) / abs(fb),
+                 "dfdx_maxrel_diff_mixed_vs_plain": float((dfa - dfb).abs().max() / dfb.abs().max()),
                  "speedup_mixed_over_plain": (len(tp) / sum(tp)) and value / ws / (len(tp) / sum(tp))}
         del a, b
 
@@ -415,8 +418,9 @@ def main():
     ap.add_argument("--cheb-ratio", dest="cheb_ratio", type=float, default=30.0)
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--coarse-dense-max", dest="coarse_dense_max", type=int, default=4096)
-    ap.add_argument("--coarse-smooth", dest="coarse_smooth", type=int, default=8)
-    ap.add_argument("--sens-fp32", dest="sens_fp32", action="store_true")
+    ap.add_argument("--coarse-smooth", dest="coarse_smooth", type=int, default=12)
+    ap.add_argument("--sens-fp64", dest="sens_fp32", action="store_false",
+                    help="FP64 element math in the sensitivity kernel of the mixed path (default FP32)")
     ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-4)
     ap.add_argument("--inner-maxit", dest="inner_maxit", type=int, default=40)
     ap.add_argument("--no-graphs", dest="no_graphs", action="store_true",

@@ -72,6 +72,11 @@ typedef struct topo_le_params {
                                 below it is solved by a full-spectrum Chebyshev
                                 polynomial (mass-dominated Newmark operators need
                                 no coarse correction); 0 = always full depth      */
+    int extrapolate;         /* initial guesses of the step solves: 1 = second-order
+                                (forward: Newmark predictor with the acceleration
+                                held, u + dt v + dt^2/2 a; adjoint: linear
+                                extrapolation 2 lambda+ - lambda++), 0 = the
+                                Newmark predictor u + dt v + dt^2/4 a and lambda+ */
 } topo_le_params;
 
 typedef struct topo_le_stats {

@@ -109,6 +109,22 @@ def test_mixed_default_fp32_sensitivities(gpu, nlvls, coarse_smooth):
     assert _rel(df, df_r) < 1e-5
 
 
+@pytest.mark.parametrize("objective", range(7))
+def test_fp32_sensitivities_every_objective(gpu, objective):
+    # FP32 element math of the sensitivity kernel for every objective, on the
+    # per-node FP64 combinations and FP32 copies of lambda and the states
+    n = (12, 6, 6)
+    kw = dict(ncp=2, tsc=4, t1=0.08, objective=objective, loadsignal=1, dalpha=1e-3, dbeta=1e-3)
+    rng = np.random.default_rng(5 + objective)
+    x = 0.3 + 0.1 * (2 * rng.random(np.prod(n)) - 1)
+    le = _le(n, nlvls=2, mixed=True, rtol=1e-12, sens_fp32=True, **kw)
+    fx, df = _run_gpu(le, x)
+    ref = O.LinearElasticity(*n, **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert abs(fx - fx_r) <= 1e-6 * abs(fx_r)
+    assert _rel(df, df_r) < 1e-5
+
+
 def test_reference_pulse_and_defaults(gpu):
     # reference defaults: Emax 1e3, Rmax 4.1667e-4, reference load pulse, dt = 0.4
     n = (8, 4, 4)

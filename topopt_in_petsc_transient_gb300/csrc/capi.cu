@@ -96,11 +96,12 @@ void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz) {
     p->cheb_ratio = 30.0;
     p->use_graphs = 1;
     p->coarse_dense_max = 4096;
-    p->coarse_smooth = 8;
+    p->coarse_smooth = 12;
     p->sens_fp32 = 1;
     p->inner_tol = 1e-4;
     p->inner_maxit = 40;
     p->adaptive_kappa = 40.0;
+    p->extrapolate = 1;
 }
 
 int topo_le_create(topo_le **out, const topo_le_params *p) {

@@ -181,6 +181,29 @@ static __global__ void k_cheb0(long long ndof, const T *__restrict__ b, const T 
     }
 }
 
+// The fine-level first Chebyshev step of the mixed-precision FCG.  After a
+// residual replacement (S->rescale) the FP32 right-hand side is re-formed
+// here as r32 = sigma r from the scaled FP64 residual before the step uses it.
+static __global__ void k_cheb0_rescale(long long ndof, const double *__restrict__ r, float *b,
+                                       const float *__restrict__ dinv, const double *coef, float *x, float *d,
+                                       const SolveScalars *S) {
+    const float c2 = (float)coef[1];
+    const bool rs = S->rescale != 0;
+    const double sg = S->sigma;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        float bv;
+        if (rs) {
+            bv = (float)(sg * r[i]);
+            b[i] = bv;
+        } else {
+            bv = b[i];
+        }
+        float v = c2 * dinv[i] * bv;
+        d[i] = v;
+        x[i] = v;
+    }
+}
+
 // Restriction = transpose of trilinear prolongation (the DMDA Q1
 // interpolation of DMCreateInterpolation, LinearElasticity.cc:2838-2842):
 // coarse node gathers fine nodes 2I-1..2I+1 with weights 1/2, 1, 1/2 per axis.
@@ -412,14 +435,11 @@ static __global__ void k_mfcg_dot(long long ndof, const float *__restrict__ z, c
     }
 }
 
-static __global__ void k_mfcg_p(long long ndof, const float *__restrict__ z, float *p, const SolveScalars *S) {
-    float beta = (float)S->beta;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)
-        p[i] = (beta == 0.0f) ? z[i] : z[i] + beta * p[i];
-}
-
-static __global__ void k_mfcg_update(long long ndof, double *x, float *r32, const float *__restrict__ p,
+// p is double-buffered (PolPQ32 reads the previous p from pb[it & 1] and
+// writes the new one to pb[(it + 1) & 1])
+static __global__ void k_mfcg_update(long long ndof, double *x, float *r32, const float *pb0, const float *pb1,
                                      const float *__restrict__ q, SolveScalars *S, Partials<1> part) {
+    const float *__restrict__ p = ((S->it + 1) & 1) ? pb1 : pb0;
     double alpha = S->alpha;
     float af = (float)alpha;
     double ax = alpha / S->sigma;  // correction in unscaled units
@@ -484,6 +504,9 @@ static __global__ void k_step_set(StepCtx *st, int block, int j) {
     st->block = block;
     st->j = j;
 }
-static __global__ void k_step_add(StepCtx *st, int delta) { st->j += delta; }
+static __global__ void k_step_add(StepCtx *st, int delta) {
+    st->j += delta;
+    if (delta < 0) st->nadj += 1;
+}
 
 }  // namespace topo

@@ -144,7 +144,8 @@ static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol
         attr = true;
     }
     bool timed = false;
-    if (std::is_same<Pol, PolCheb<float>>::value && g_timer && g.nn() == g_timer->nn) {
+    if ((std::is_same<Pol, PolCheb<float>>::value || std::is_same<Pol, PolChebDot>::value) && g_timer &&
+        g.nn() == g_timer->nn) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(s, &cs);
         timed = cs == cudaStreamCaptureStatusNone;
@@ -229,13 +230,16 @@ struct TopoLE {
     float *cntP = nullptr;
     double *cp = nullptr;                   // (ncp+1) x 3 x ndof
     double *Uh = nullptr, *DUh = nullptr, *DDUh = nullptr;  // tsc x ndof
-    double *Lp1 = nullptr, *DLp1 = nullptr, *DDLp1 = nullptr, *DLc = nullptr, *DDLc = nullptr;
+    double *Lp1 = nullptr, *DLp1 = nullptr, *DDLp1 = nullptr, *DLc = nullptr, *DDLc = nullptr, *Lp2 = nullptr;
     double *KL = nullptr, *ML = nullptr, *hK = nullptr, *hM = nullptr;
     double *DDL0 = nullptr;
     double *df = nullptr;
+    // per-node sensitivity combinations: FP64 (2 x ndof) or FP32 (5 x ndof)
+    double *sw64 = nullptr;
+    float *sw32 = nullptr;
     // solver vectors
     double *sx = nullptr, *sb = nullptr, *sr = nullptr, *sp = nullptr, *sq = nullptr, *sz = nullptr;
-    float *sr32 = nullptr, *sp32 = nullptr, *sq32 = nullptr;
+    float *sr32 = nullptr, *sp32 = nullptr, *sp32b = nullptr, *sq32 = nullptr;
     int coarse_dense = 1;
     // coarse assembly scratch
     double *KEc = nullptr, *MEc = nullptr, *Acoarse = nullptr, *gj_row = nullptr, *gj_col = nullptr;
@@ -344,6 +348,7 @@ int le_alloc(TopoLE *le) {
     AG(le->Lp1, nd);
     AG(le->DLp1, nd);
     AG(le->DDLp1, nd);
+    AG(le->Lp2, nd);
     AG(le->DLc, nd);
     AG(le->DDLc, nd);
     AG(le->KL, nd);
@@ -352,6 +357,10 @@ int le_alloc(TopoLE *le) {
     AG(le->hM, nd);
     AG(le->DDL0, nd);
     AG(le->df, ne);
+    if (p.mixed && p.sens_fp32)
+        AG(le->sw32, 5 * nd);
+    else
+        AG(le->sw64, 2 * nd);
     AG(le->sx, nd);
     AG(le->sb, nd);
     AG(le->sr, nd);
@@ -360,6 +369,7 @@ int le_alloc(TopoLE *le) {
     AG(le->sz, nd);
     AG(le->sr32, nd);
     AG(le->sp32, nd);
+    AG(le->sp32b, nd);
     AG(le->sq32, nd);
     AG(le->S, 1);
     AG(le->st, 1);
@@ -565,8 +575,9 @@ static int setup_operator(TopoLE *le, int o) {
             }
         }
     }
-    // dense coarsest operator and its inverse (FP64 Gauss-Jordan)
-    if (!le->coarse_dense) {
+    // dense coarsest operator and its inverse (FP64 Gauss-Jordan); not needed
+    // when the V-cycle of this operator stops above the coarsest level
+    if (!le->coarse_dense || op.depth < le->nlev) {
         CK(cudaGetLastError());
         return TOPO_OK;
     }
@@ -617,8 +628,20 @@ const float *ainv<float>(TopoLE *le, int o) { return le->ops[o].Ainv_f; }
 template <>
 const double *ainv<double>(TopoLE *le, int o) { return le->ops[o].Ainv_d; }
 
+// Work of the mixed FCG fused into the fine level of its FP32 V-cycle: the
+// first smoothing step re-forms r32 = sigma r after a residual replacement
+// (k_mfcg_scale), and the last one computes the FCG dot products of its
+// output (k_mfcg_dot).
+struct VFuse {
+    const double *r64;
+    SolveScalars *S;
+    const float *q32;
+    Partials<2> part;
+    bool scaled = false, dotted = false;
+};
+
 template <class T>
-static T *vcycle(TopoLE *le, int o, int l, const T *b) {
+static T *vcycle(TopoLE *le, int o, int l, const T *b, VFuse *fz = nullptr) {
     cudaStream_t s = le->stream;
     Level &lv = le->L[l];
     VW<T> w = vw<T>(le, o, l);
@@ -627,18 +650,46 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b) {
     Weights<T> wt{op.sK != 0.0 ? w.kf : nullptr, w.mf, nullptr, (T)op.sK, (T)op.sM};
     const double *lohi = op.lv[l].cheb;
     T *x = w.xa, *xo = w.xb;
+    const bool fuse = fz && l == 0 && std::is_same<T, float>::value;
+    // first step from zero: x = d = c2 Dinv b
+    auto first = [&](const double *tab) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (fuse) {
+                count_launch();
+                k_cheb0_rescale<<<ew_blocks(nd), EW, 0, s>>>(nd, fz->r64, const_cast<float *>(b), w.dinv, tab, x, w.d,
+                                                             fz->S);
+                fz->scaled = true;
+                return;
+            }
+        }
+        count_launch();
+        k_cheb0<T><<<ew_blocks(nd), EW, 0, s>>>(nd, b, w.dinv, tab, x, w.d);
+    };
+    // smoothing step k (one operator application); `last`: this level's
+    // final step, whose output is the V-cycle result at the fine level
+    auto step = [&](const double *tab, int k, bool last) {
+        bool done = false;
+        if constexpr (std::is_same<T, float>::value) {
+            if (fuse && last) {
+                PolChebDot pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, tab, k, fz->q32, fz->S, fz->part};
+                launch_tile<float>(lv.g, *w.C, pc, s);
+                fz->dotted = true;
+                done = true;
+            }
+        }
+        if (!done) {
+            PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, tab, k, {}};
+            launch_tile<T>(lv.g, *w.C, pc, s);
+        }
+        T *t = x;
+        x = xo;
+        xo = t;
+    };
     if (l == op.depth - 1 && op.depth < le->nlev) {
         // well-conditioned level: full-spectrum Chebyshev-Jacobi solve from zero
         const double *full = op.lv[l].chebf;
-        count_launch();
-        k_cheb0<T><<<ew_blocks(nd), EW, 0, s>>>(nd, b, w.dinv, full, x, w.d);
-        for (int k = 1; k < le->p.coarse_smooth; k++) {
-            PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, full, k, {}};
-            launch_tile<T>(lv.g, *w.C, pc, s);
-            T *t = x;
-            x = xo;
-            xo = t;
-        }
+        first(full);
+        for (int k = 1; k < le->p.coarse_smooth; k++) step(full, k, k == le->p.coarse_smooth - 1);
         return x;
     }
     if (l == le->nlev - 1) {
@@ -649,27 +700,13 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b) {
             return w.xa;
         }
         // iterative coarse solve: Chebyshev-Jacobi polynomial from zero
-        count_launch();
-        k_cheb0<T><<<ew_blocks(nd), EW, 0, s>>>(nd, b, w.dinv, lohi, x, w.d);
-        for (int k = 1; k < le->p.coarse_smooth; k++) {
-            PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, lohi, k, {}};
-            launch_tile<T>(lv.g, *w.C, pc, s);
-            T *t = x;
-            x = xo;
-            xo = t;
-        }
+        first(lohi);
+        for (int k = 1; k < le->p.coarse_smooth; k++) step(lohi, k, k == le->p.coarse_smooth - 1);
         return x;
     }
     const int nu = le->p.smooth;
-    count_launch();
-    k_cheb0<T><<<ew_blocks(nd), EW, 0, s>>>(nd, b, w.dinv, lohi, x, w.d);
-    for (int k = 1; k < nu; k++) {
-        PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, lohi, k, {}};
-        launch_tile<T>(lv.g, *w.C, pc, s);
-        T *t = x;
-        x = xo;
-        xo = t;
-    }
+    first(lohi);
+    for (int k = 1; k < nu; k++) step(lohi, k, false);
     PolResid<T> pr{lv.fixed, wt, x, b, w.r, {}};
     launch_tile<T>(lv.g, *w.C, pr, s);
     Level &lc = le->L[l + 1];
@@ -679,13 +716,7 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b) {
     T *xc = vcycle<T>(le, o, l + 1, wc.b);
     count_launch();
     k_prolong<T><<<ew_blocks(lv.g.nn()), EW, 0, s>>>(lv.g, lc.g, lv.fixed, xc, x);
-    for (int k = 0; k < nu; k++) {
-        PolCheb<T> pc{lv.fixed, wt, x, b, w.dinv, xo, w.d, lohi, k, {}};
-        launch_tile<T>(lv.g, *w.C, pc, s);
-        T *t = x;
-        x = xo;
-        xo = t;
-    }
+    for (int k = 0; k < nu; k++) step(lohi, k, k == nu - 1);
     return x;
 }
 
@@ -737,19 +768,25 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
     long long nd = le->ndof;
     unsigned nb = ew_blocks(nd);
     if (le->p.mixed) {
-        // reliable-update mixed precision: FP32 recurrence, FP64 replacements
-        count_launch();
-        k_mfcg_scale<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sr, le->sr32, le->S);
-        float *z = vcycle<float>(le, o, 0, le->sr32);
-        count_launch();
-        k_mfcg_dot<<<red_blocks(nd), EW, 0, s>>>(nd, z, le->sr32, le->sq32, le->S, P2(le));
-        count_launch();
-        k_mfcg_p<<<nb, EW, 0, s>>>(nd, z, le->sp32, le->S);
+        // reliable-update mixed precision: FP32 recurrence, FP64 replacements.
+        // The rescaling of r32 and the dot products ride on the first and
+        // last fine-level smoothing steps, the direction update on PolPQ32.
+        VFuse fz{le->sr, le->S, le->sq32, P2(le)};
+        if (le->ops[o].depth == 1 && le->nlev == 1 && le->coarse_dense) {
+            count_launch();  // the dense coarse solve has no smoothing step to carry the rescaling
+            k_mfcg_scale<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sr, le->sr32, le->S);
+        }
+        float *z = vcycle<float>(le, o, 0, le->sr32, &fz);
+        if (!fz.dotted) {
+            count_launch();
+            k_mfcg_dot<<<red_blocks(nd), EW, 0, s>>>(nd, z, le->sr32, le->sq32, le->S, P2(le));
+        }
         Weights<float> wf{op.sK != 0.0 ? l0.kff : nullptr, l0.mff, nullptr, (float)op.sK, (float)op.sM};
-        PolPQ32 pq32{l0.fixed, wf, le->sp32, le->sq32, le->S, P1(le)};
+        PolPQ32 pq32{l0.fixed, wf, z, {le->sp32, le->sp32b}, le->sq32, le->S, P1(le)};
         launch_tile<float>(l0.g, l0.Cf, pq32, s);
         count_launch();
-        k_mfcg_update<<<red_blocks(nd), EW, 0, s>>>(nd, le->sx, le->sr32, le->sp32, le->sq32, le->S, P1(le));
+        k_mfcg_update<<<red_blocks(nd), EW, 0, s>>>(nd, le->sx, le->sr32, le->sp32, le->sp32b, le->sq32, le->S,
+                                                    P1(le));
         Weights<df> wd = fine_weights<df>(le, op.sK != 0.0, true, nullptr, op.sK, op.sM);
         PolReplace<df> rp{l0.fixed, wd, le->sx, cur_b(le), le->sr, le->sr32, le->S, cond, has_cond, P1(le)};
         launch_tile<df>(l0.g, le->Cx, rp, s);
@@ -872,7 +909,9 @@ static void fwd_rhs_t(TopoLE *le) {
     double dt = le->dt;
     pr.pred[0] = 1.0;
     pr.pred[1] = (p.ti == 0) ? 0.0 : dt;
-    pr.pred[2] = (p.ti == 0) ? 0.0 : 0.25 * dt * dt;
+    // (second-order guess: the same with the acceleration held over the step,
+    // u- + dt du- + dt^2/2 ddu-, the Newmark update with ddu+ = ddu-)
+    pr.pred[2] = (p.ti == 0) ? 0.0 : (p.extrapolate ? 0.5 : 0.25) * dt * dt;
     pr.st = le->st;
     pr.b = le->sb;
     pr.x0 = le->sx;
@@ -963,6 +1002,8 @@ static AdjCombine adj_args(TopoLE *le, int t0mode) {
     A.Lp1 = le->Lp1;
     A.DLp1 = le->DLp1;
     A.DDLp1 = le->DDLp1;
+    A.Lp2 = le->Lp2;
+    A.extrapolate = le->p.extrapolate;
     A.hK = le->hK;
     A.hM = le->hM;
     A.cntP = le->cntP;
@@ -1037,16 +1078,32 @@ static SensArgs sens_args(TopoLE *le, int t0mode) {
     return S;
 }
 
+static bool sens_in_fp32(const TopoLE *le) { return le->p.mixed && le->p.sens_fp32; }
+
 template <int OBJ>
 static void launch_sens_obj(TopoLE *le, const SensArgs &S) {
     count_launch();
-    if (le->p.mixed && le->p.sens_fp32)
+    if (sens_in_fp32(le))
         k_sens<OBJ, float><<<red_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cf);
     else
         k_sens<OBJ, double><<<red_blocks(le->nel), EW, 0, le->stream>>>(S, le->L[0].Cd);
 }
 static void launch_sens(TopoLE *le, int t0mode) {
     SensArgs S = sens_args(le, t0mode);
+    long long nd = le->ndof;
+    if (sens_in_fp32(le)) {
+        const int ob = le->p.objective;
+        S.wKf = le->sw32;
+        S.wMf = le->sw32 + nd;
+        S.lamf = le->sw32 + 2 * nd;
+        S.uf = (ob == 3 || ob == 5) ? le->sw32 + 3 * nd : nullptr;
+        S.duf = (ob == 4 || ob == 5 || ob == 6) ? le->sw32 + 4 * nd : nullptr;
+    } else {
+        S.wKd = le->sw64;
+        S.wMd = le->sw64 + nd;
+    }
+    count_launch();
+    k_sens_nodal<<<ew_blocks(nd), EW, 0, le->stream>>>(S);
     switch (le->p.objective) {
     case 0: launch_sens_obj<0>(le, S); break;
     case 1: launch_sens_obj<1>(le, S); break;
@@ -1070,7 +1127,8 @@ static int adj_step(TopoLE *le, bool capturing) {
     if (rc) return rc;
     launch_sens(le, 0);
     count_launch();
-    k_adj_advance<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->DLc, le->DDLc, le->Lp1, le->DLp1, le->DDLp1);
+    k_adj_advance<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->DLc, le->DDLc, le->Lp1, le->DLp1, le->DDLp1,
+                                                      le->Lp2, le->st);
     count_launch();
     k_step_add<<<1, 1, 0, s>>>(le->st, -1);
     return TOPO_OK;
@@ -1250,6 +1308,8 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
     CK(cudaMemsetAsync(le->Lp1, 0, sizeof(double) * nd, s));
     CK(cudaMemsetAsync(le->DLp1, 0, sizeof(double) * nd, s));
     CK(cudaMemsetAsync(le->DDLp1, 0, sizeof(double) * nd, s));
+    CK(cudaMemsetAsync(le->Lp2, 0, sizeof(double) * nd, s));
+    CK(cudaMemsetAsync(&le->st->nadj, 0, sizeof(int), s));
     CK(cudaMemsetAsync(&le->st->fx, 0, sizeof(double), s));
     for (int c = le->p.ncp - 1; c >= 0; c--) {
         if (le->last_block_resident != c) {

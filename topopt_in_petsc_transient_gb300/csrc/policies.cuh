@@ -158,18 +158,26 @@ struct PolPQ {
 // FP64 residual only, so the tolerance means the same as in the plain path.
 // ---------------------------------------------------------------------------
 struct PolPQ32 {
+    // q = (N A N + I - N) p and p.q, with the FCG direction update
+    // p = z + beta p_prev (k_mfcg_p) done while staging: p_prev is read from
+    // pb[it & 1] and the new p written to pb[(it + 1) & 1], so no CTA
+    // overwrites a halo value another CTA still stages
     static constexpr int NIN = 1, NRED = 1;
     static constexpr bool HAS_K = true, HAS_M = true;
     const uint8_t *fixed;
     Weights<float> w;
-    const float *p;
+    const float *z;
+    float *pb[2];
     float *q;
     SolveScalars *S;
     Partials<1> part;
+    __device__ __forceinline__ void pnew(long long n, float v[3]) const {
+        const float beta = (float)S->beta;
+        const float *pp = pb[S->it & 1];
+        for (int c = 0; c < 3; c++) v[c] = (beta == 0.0f) ? z[3 * n + c] : z[3 * n + c] + beta * pp[3 * n + c];
+    }
     __device__ void load(long long n, float v[1][3]) const {
-        v[0][0] = p[3 * n];
-        v[0][1] = p[3 * n + 1];
-        v[0][2] = p[3 * n + 2];
+        pnew(n, v[0]);
         mask3(fixed[n], v[0]);
     }
     __device__ void coef(long long e, float &ck, float &cm) const { w.get(e, ck, cm); }
@@ -179,15 +187,17 @@ struct PolPQ32 {
     };
     __device__ Pre pre(long long n) const {
         Pre r;
-        for (int c = 0; c < 3; c++) r.p[c] = p[3 * n + c];
+        pnew(n, r.p);
         r.f = fixed[n];
         return r;
     }
     __device__ void epilogue(long long n, int, int, int, const float y[3], double red[1], const Pre &r) const {
+        float *pout = pb[(S->it + 1) & 1];
         float s = 0.0f;
         for (int c = 0; c < 3; c++) {
             float pv = r.p[c];
             float qv = ((r.f >> c) & 1) ? pv : y[c];
+            pout[3 * n + c] = pv;
             q[3 * n + c] = qv;
             s += pv * qv;
         }
@@ -328,6 +338,69 @@ struct PolCheb {
     __device__ void finish(const double *) const {}
 };
 
+// The last fine-level smoothing step of the FP32 preconditioner in the mixed
+// FCG, fused with the FCG dot products of its output z (the preconditioned
+// residual): z.r32 -> rho, z.q32 -> gamma, beta = -gamma / (p.q)  (k_mfcg_dot).
+// Here b is r32.
+struct PolChebDot {
+    static constexpr int NIN = 1, NRED = 2;
+    static constexpr bool HAS_K = true, HAS_M = true;
+    const uint8_t *fixed;
+    Weights<float> w;
+    const float *x_in, *b, *dinv;
+    float *x_out, *d;
+    const double *ctab;
+    int k;
+    const float *q32;
+    SolveScalars *S;
+    Partials<2> part;
+    __device__ void load(long long n, float v[1][3]) const {
+        v[0][0] = x_in[3 * n];
+        v[0][1] = x_in[3 * n + 1];
+        v[0][2] = x_in[3 * n + 2];
+        mask3(fixed[n], v[0]);
+    }
+    __device__ void coef(long long e, float &ck, float &cm) const { w.get(e, ck, cm); }
+    struct Pre {
+        float x[3], b[3], di[3], d[3], q[3];
+        uint8_t f;
+    };
+    __device__ Pre pre(long long n) const {
+        Pre r;
+        for (int c = 0; c < 3; c++) {
+            r.x[c] = x_in[3 * n + c];
+            r.b[c] = b[3 * n + c];
+            r.di[c] = dinv[3 * n + c];
+            r.d[c] = (k == 0) ? 0.0f : d[3 * n + c];
+            r.q[c] = q32[3 * n + c];
+        }
+        r.f = fixed[n];
+        return r;
+    }
+    __device__ void epilogue(long long n, int, int, int, const float y[3], double red[2], const Pre &q) const {
+        const float c1 = (float)ctab[2 * k], c2 = (float)ctab[2 * k + 1];
+        float s0 = 0.0f, s1 = 0.0f;
+        for (int c = 0; c < 3; c++) {
+            float rv = q.b[c] - (((q.f >> c) & 1) ? q.x[c] : y[c]);
+            float dv = c1 * q.d[c] + c2 * q.di[c] * rv;
+            float zv = q.x[c] + dv;
+            d[3 * n + c] = dv;
+            x_out[3 * n + c] = zv;
+            s0 += zv * q.b[c];
+            s1 += zv * q.q[c];
+        }
+        red[0] += (double)s0;
+        red[1] += (double)s1;
+    }
+    __device__ void finish(const double t[2]) const {
+        S->rho = t[0];
+        S->gam = t[1];
+        S->beta = S->restart ? 0.0 : -t[1] / S->pq;
+        if (!isfinite(S->beta)) S->beta = 0.0;
+        S->rescale = 0;
+    }
+};
+
 // residual only: r = b - (N A N + I - N) x   (before restriction)
 template <class T>
 struct PolResid {
@@ -390,7 +463,7 @@ struct StepCtx {   // device-resident time-stepping state
     int block;     // checkpoint block c
     int j;         // step within block
     int tsc;
-    int pad;
+    int nadj;      // adjoint steps completed in the current reverse sweep
     double dt;
     double fx;     // objective accumulator
 };

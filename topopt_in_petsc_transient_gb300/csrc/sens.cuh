@@ -20,6 +20,8 @@ struct AdjCombine {
     const uint8_t *fixed;
     const double *KL, *ML;        // K L+ and M L+ (unmasked element sums, masked input)
     const double *Lp1, *DLp1, *DDLp1;
+    const double *Lp2;            // lambda two steps later (initial-guess extrapolation)
+    int extrapolate;
     const double *hK, *hM;        // product-form objective gradients (or null)
     const float *cntP;            // per node sum of P over adjacent elements
     const double *Ustate, *DUstate, *DDUstate;  // state at this step (base of history)
@@ -86,7 +88,7 @@ static __global__ void k_adj_combine(AdjCombine A) {
                 // the reference solves (N A N + I - N) L = R1 with A = -Keff
                 // (LinearElasticity.cc:1022-1026, :924): Keff L = -R1 on free DOFs
                 A.b[i] = fx ? 0.0 : -R1;
-                A.x0[i] = fx ? 0.0 : A.Lp1[i];
+                A.x0[i] = fx ? 0.0 : (A.extrapolate ? 2.0 * A.Lp1[i] - A.Lp2[i] : A.Lp1[i]);
             }
         }
     }
@@ -107,10 +109,15 @@ static __global__ void k_count_region(GridDesc g, const double *__restrict__ P, 
     }
 }
 
-// after the adjoint solve of step j: L+ <- lambda_j, DL+ <- DL_j, DDL+ <- DDL_j
+// after the adjoint solve of step j: L++ <- L+ (lambda_j after the first
+// step of the sweep, so that the extrapolated guess of the next step is
+// lambda_j itself), L+ <- lambda_j, DL+ <- DL_j, DDL+ <- DDL_j
 static __global__ void k_adj_advance(long long ndof, const double *__restrict__ lam, const double *__restrict__ DL,
-                              const double *__restrict__ DDL, double *Lp1, double *DLp1, double *DDLp1) {
+                              const double *__restrict__ DDL, double *Lp1, double *DLp1, double *DDLp1, double *Lp2,
+                              const StepCtx *st) {
+    const bool first = st->nadj == 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        Lp2[i] = first ? lam[i] : Lp1[i];
         Lp1[i] = lam[i];
         DLp1[i] = DL[i];
         DDLp1[i] = DDL[i];
@@ -125,7 +132,8 @@ static __global__ void k_adj_advance(long long ndof, const double *__restrict__ 
 // The 4 x 576 multiply-adds per element of the reference reduce to
 //   df_e += P_e dfx0_e + lam_e' (dkfac_e KE wK_e + dmfac_e ME wM_e)
 // with wK = sum aK_i s_i + bK_i p_i and wM likewise over the current state
-// s = (u, du, ddu) and the previous state p; evaluated in the mode basis as
+// s = (u, du, ddu) and the previous state p (formed per node by
+// k_sens_nodal); evaluated in the mode basis as
 //   Lam' Khat WK  and  sum_m W_m Lam_m WM_m.
 // One thread per element; OBJ is the reference objective (EvaluateObjective,
 // :1416-1465, EvaluateObjectiveGradient :1469-1514).
@@ -141,13 +149,74 @@ struct SensArgs {
     int t0mode;                              // 1: state = t = 0, no previous state
     int with_objective;                      // accumulate the objective of the current state
     const StepCtx *st;
+    // per-node vectors written by k_sens_nodal: FP64 combinations (element
+    // math in FP64) or FP32 combinations plus FP32 copies of lambda and of the
+    // states the objective quadratic form reads (element math in FP32)
+    double *wKd, *wMd;
+    float *wKf, *wMf, *lamf, *uf, *duf;
     double *df;
     double *fx;                              // device accumulator
     Partials<1> part;
 };
 
-template <class T>
-__device__ __forceinline__ void gather8(const double *v, const long long nodes[8], T out[3][8]) {
+// current state (t0mode: the t = 0 state) and previous state of the step
+__device__ __forceinline__ void sens_states(const SensArgs &A, long long ndof, const double *&u, const double *&du,
+                                            const double *&ddu, const double *&up, const double *&dup,
+                                            const double *&ddup) {
+    up = dup = ddup = nullptr;
+    if (A.t0mode) {
+        u = A.cp;
+        du = A.cp + ndof;
+        ddu = A.cp + 2 * ndof;
+        return;
+    }
+    int j = A.st->j;
+    u = A.Uh + (long long)j * ndof;
+    du = A.DUh + (long long)j * ndof;
+    ddu = A.DDUh + (long long)j * ndof;
+    if (j == 0) {
+        const double *base = A.cp + (long long)A.st->block * 3 * ndof;
+        up = base;
+        dup = base + ndof;
+        ddup = base + 2 * ndof;
+    } else {
+        up = A.Uh + (long long)(j - 1) * ndof;
+        dup = A.DUh + (long long)(j - 1) * ndof;
+        ddup = A.DDUh + (long long)(j - 1) * ndof;
+    }
+}
+
+// wK = aK . (u, du, ddu) + bK . (u-, du-, ddu-) and wM likewise, once per DOF
+// (every node is shared by up to 8 elements, so this is 8x less FP64 work
+// than forming them inside the element loop)
+static __global__ void k_sens_nodal(const SensArgs A) {
+    const long long ndof = 3 * A.g.nn();
+    const double *u, *du, *ddu, *up, *dup, *ddup;
+    sens_states(A, ndof, u, du, ddu, up, dup, ddup);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ndof; q += (long long)gridDim.x * blockDim.x) {
+        double s0 = u[q], s1 = du[q], s2 = ddu[q];
+        double wk = A.aK[0] * s0 + A.aK[1] * s1 + A.aK[2] * s2;
+        double wm = A.aM[0] * s0 + A.aM[1] * s1 + A.aM[2] * s2;
+        if (!A.t0mode) {
+            double p0 = up[q], p1 = dup[q], p2 = ddup[q];
+            wk += A.bK[0] * p0 + A.bK[1] * p1 + A.bK[2] * p2;
+            wm += A.bM[0] * p0 + A.bM[1] * p1 + A.bM[2] * p2;
+        }
+        if (A.wKd) {
+            A.wKd[q] = wk;
+            A.wMd[q] = wm;
+        } else {
+            A.wKf[q] = (float)wk;
+            A.wMf[q] = (float)wm;
+            A.lamf[q] = (float)A.lam[q];
+            if (A.uf) A.uf[q] = (float)s0;
+            if (A.duf) A.duf[q] = (float)s1;
+        }
+    }
+}
+
+template <class T, class S>
+__device__ __forceinline__ void gather8(const S *v, const long long nodes[8], T out[3][8]) {
 #pragma unroll
     for (int L = 0; L < 8; L++)
 #pragma unroll
@@ -176,31 +245,22 @@ __device__ __forceinline__ T quad_M(const ElemConst<T> &C, T A[3][8], T B[3][8])
     return s;
 }
 
+// source of a gathered vector: the FP64 vector for FP64 element math, its
+// FP32 copy for FP32 element math
+__device__ __forceinline__ const double *sens_src(const double *d, const float *, double) { return d; }
+__device__ __forceinline__ const float *sens_src(const double *, const float *f, float) { return f; }
+
 template <int OBJ, class T>
 static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const ElemConst<T> C) {
     const GridDesc g = A.g;
     const long long nel = g.nel(), ndof = 3 * g.nn();
-    const double *u, *du, *ddu, *up = nullptr, *dup = nullptr, *ddup = nullptr;
-    if (A.t0mode) {
-        u = A.cp;
-        du = A.cp + ndof;
-        ddu = A.cp + 2 * ndof;
-    } else {
-        int j = A.st->j;
-        u = A.Uh + (long long)j * ndof;
-        du = A.DUh + (long long)j * ndof;
-        ddu = A.DDUh + (long long)j * ndof;
-        if (j == 0) {
-            const double *base = A.cp + (long long)A.st->block * 3 * ndof;
-            up = base;
-            dup = base + ndof;
-            ddup = base + 2 * ndof;
-        } else {
-            up = A.Uh + (long long)(j - 1) * ndof;
-            dup = A.DUh + (long long)(j - 1) * ndof;
-            ddup = A.DDUh + (long long)(j - 1) * ndof;
-        }
-    }
+    const double *u, *du, *ddu, *up, *dup, *ddup;
+    sens_states(A, ndof, u, du, ddu, up, dup, ddup);
+    const auto lam = sens_src(A.lam, A.lamf, T());
+    const auto wK = sens_src(A.wKd, A.wKf, T());
+    const auto wM = sens_src(A.wMd, A.wMf, T());
+    const auto su = sens_src(u, A.uf, T());
+    const auto sdu = sens_src(du, A.duf, T());
     double fxv[1] = {0.0};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
         int i = (int)(e % g.ex), jj = (int)((e / g.ex) % g.ey), k = (int)(e / ((long long)g.ex * g.ey));
@@ -208,13 +268,12 @@ static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const Elem
 #pragma unroll
         for (int L = 0; L < 8; L++)
             nodes[L] = (i + (L & 1)) + (long long)g.nx * ((jj + ((L >> 1) & 1)) + (long long)g.ny * (k + (L >> 2)));
-        // lam' KE wK = (Khat Lam)' WK in mode space (Khat symmetric); the
-        // combination vectors are formed one component at a time so only
-        // Khat Lam and W Lam stay live
+        // lam' KE wK = (Khat Lam)' WK in mode space (Khat symmetric): only
+        // Khat Lam and W Lam stay live while WK and WM stream in per component
         T KL[3][8], ML[3][8];
         {
             T Lm[3][8];
-            gather8<T>(A.lam, nodes, Lm);
+            gather8<T>(lam, nodes, Lm);
 #pragma unroll
             for (int c = 0; c < 3; c++) mode_fwd(Lm[c]);
             mode_khat(C, Lm, KL);
@@ -229,17 +288,8 @@ static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const Elem
             T wk8[8], wm8[8];
 #pragma unroll
             for (int L = 0; L < 8; L++) {
-                long long q = 3 * nodes[L] + c;
-                double s0 = u[q], s1 = du[q], s2 = ddu[q];
-                double wk = A.aK[0] * s0 + A.aK[1] * s1 + A.aK[2] * s2;
-                double wm = A.aM[0] * s0 + A.aM[1] * s1 + A.aM[2] * s2;
-                if (!A.t0mode) {
-                    double p0 = up[q], p1 = dup[q], p2 = ddup[q];
-                    wk += A.bK[0] * p0 + A.bK[1] * p1 + A.bK[2] * p2;
-                    wm += A.bM[0] * p0 + A.bM[1] * p1 + A.bM[2] * p2;
-                }
-                wk8[L] = (T)wk;
-                wm8[L] = (T)wm;
+                wk8[L] = (T)wK[3 * nodes[L] + c];
+                wm8[L] = (T)wM[3 * nodes[L] + c];
             }
             mode_fwd(wk8);
             mode_fwd(wm8);
@@ -268,8 +318,7 @@ static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const Elem
             }
         } else {
             T S0[3][8];
-            const double *s = (OBJ == 3) ? u : du;
-            gather8<T>(s, nodes, S0);
+            gather8<T>((OBJ == 3) ? su : sdu, nodes, S0);
 #pragma unroll
             for (int c = 0; c < 3; c++) mode_fwd(S0[c]);
             if (OBJ == 3) {
@@ -281,12 +330,12 @@ static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const Elem
                 h0 = A.dt * 0.5 * mfe * vMv;
                 dfx0 = A.dt * 0.5 * dmfe * vMv;
             } else if (OBJ == 5) {
+                double vMv = (double)quad_M(C, S0, S0);
                 T S1[3][8];
-                gather8<T>(u, nodes, S1);
+                gather8<T>(su, nodes, S1);
 #pragma unroll
                 for (int c = 0; c < 3; c++) mode_fwd(S1[c]);
                 double uKu = (double)quad_K(C, S1, S1);
-                double vMv = (double)quad_M(C, S0, S0);
                 h0 = A.dt * 0.5 * (kfe * uKu + mfe * vMv);
                 dfx0 = A.dt * 0.5 * (dkfe * uKu + dmfe * vMv);
             } else {  // 6: dissipated energy with interpolated damping

@@ -49,7 +49,7 @@ class LinearElasticity:
                  basis=5, dalpha=1e-4, dbeta=1e-4, omega0=1.0, optimizationRegion=2, V0=None, h=(1.0, 1.0, 1.0),
                  loadsignal=0, mixed=True, rtol=1e-10, maxit=500, smooth=3, cheb_ratio=30.0, use_graphs=True,
                  coarse_dense_max=None, coarse_smooth=None, sens_fp32=None, inner_tol=None, inner_maxit=None,
-                 adaptive_kappa=None):
+                 adaptive_kappa=None, extrapolate=None):
         if reduction:
             raise TopoError(1, "LinearElasticity", "the SOMMG reduced-order path is not part of this build")
         L = _lib.load()
@@ -75,6 +75,8 @@ class LinearElasticity:
             p.inner_maxit = inner_maxit
         if adaptive_kappa is not None:
             p.adaptive_kappa = adaptive_kappa
+        if extrapolate is not None:
+            p.extrapolate = int(bool(extrapolate))
         self.params = p
         self.nelx, self.nely, self.nelz = nelx, nely, nelz
         self.nel = nelx * nely * nelz
