@@ -145,10 +145,12 @@ def run_gb300(args):
         flush_l2()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("timed_design_iteration")  # lets a profiler select the timed region
         e0.record()
         fx, fxs_, gx, ch, mnd = design_iteration(opt)  # every library call returns synchronised
         e1.record()
         e1.synchronize()
+        torch.cuda.nvtx.range_pop()
         times.append(e0.elapsed_time(e1) / 1e3)
         fxs.append(fx)
     barrier()
@@ -169,30 +171,34 @@ def run_gb300(args):
     # ---- plain FP64 path and objective agreement on the same initial design ----
     plain = None
     if args.plain_steps > 0:
+        # both paths from the same uniform design: objective and sensitivity
+        # agreement on the first iteration; the plain path is then timed on
+        # the same iterations as the headline (after the warm-up iterations)
         a = TopOpt(mixed=True, **wl).setup()
         b = TopOpt(mixed=False, **wl).setup()
         fa = design_iteration(a)[0]
         dfa = a.dfdx.clone()
+        fb = design_iteration(b)[0]
+        dfb = b.dfdx.clone()
+        del a
+        for _ in range(max(0, args.warmup - 1)):
+            design_iteration(b)
         torch.cuda.synchronize()
         tp = []
-        fb = None
         for k in range(args.plain_steps):
             flush_l2()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
-            r = design_iteration(b)
+            design_iteration(b)
             e1.record()
             e1.synchronize()
             tp.append(e0.elapsed_time(e1) / 1e3)
-            if k == 0:
-                fb = r[0]
-                dfb = b.dfdx.clone()
-        plain = {"value": len(tp) / sum(tp), "unit": UNIT, "steps": len(tp),
+        plain = {"value": len(tp) / sum(tp), "unit": UNIT, "steps": len(tp), "warmup": args.warmup,
                  "objective_rel_diff_mixed_vs_plain": abs(fa - fb) / abs(fb),
                  "dfdx_maxrel_diff_mixed_vs_plain": float((dfa - dfb).abs().max() / dfb.abs().max()),
-                 "speedup_mixed_over_plain": (len(tp) / sum(tp)) and value / ws / (len(tp) / sum(tp))}
-        del a, b
+                 "speedup_mixed_over_plain": value / ws / (len(tp) / sum(tp))}
+        del b
 
     # ---- end to end through the C ABI with host buffers ----
     e2e = None
@@ -214,7 +220,7 @@ def run_gb300(args):
     design_iteration(probe)
     tot_ms, nlaunch = C.c_double(), C.c_longlong()
     _lib.check(L.topo_le_smoother_timing(probe.physics._h, 0, C.byref(tot_ms), C.byref(nlaunch)), "smoother_timing")
-    ms_launch = tot_ms.value / max(1, nlaunch.value)
+    ms_launch = tot_ms.value / nlaunch.value if nlaunch.value > 0 else float("nan")
     ms_fp64 = C.c_double()
     _lib.check(L.topo_le_time_apply(probe.physics._h, 0, 5, 50, C.byref(ms_fp64)), "time_apply")
     del probe
@@ -421,7 +427,7 @@ def main():
     ap.add_argument("--coarse-smooth", dest="coarse_smooth", type=int, default=12)
     ap.add_argument("--sens-fp64", dest="sens_fp32", action="store_false",
                     help="FP64 element math in the sensitivity kernel of the mixed path (default FP32)")
-    ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-4)
+    ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-5)
     ap.add_argument("--inner-maxit", dest="inner_maxit", type=int, default=40)
     ap.add_argument("--no-graphs", dest="no_graphs", action="store_true",
                     help="launch every kernel directly (profilers see each launch); same kernels")

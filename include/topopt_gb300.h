@@ -77,6 +77,18 @@ typedef struct topo_le_params {
                                 held, u + dt v + dt^2/2 a; adjoint: linear
                                 extrapolation 2 lambda+ - lambda++), 0 = the
                                 Newmark predictor u + dt v + dt^2/4 a and lambda+ */
+    int mass_precond;        /* preconditioner of the step solves: 0 = multigrid
+                                V-cycle with Chebyshev-Jacobi smoothing, 1 =
+                                Kronecker mass preconditioner (tensor product of
+                                1-D tridiagonal mass solves, density scaled),
+                                2 = the Kronecker one whenever the operator's
+                                stiffness share is at most mass_precond_share   */
+    double mass_precond_share; /* bound on (sK/sM) max_e(kf_e/mf_e) lambda_max(KE,ME)
+                                for mass_precond = 2                              */
+    int mass_precond_smooth; /* Chebyshev-Jacobi steps (full spectrum of Dinv A)
+                                applied after the Kronecker solve; they remove
+                                the error of its density scaling where the
+                                design varies sharply                             */
 } topo_le_params;
 
 typedef struct topo_le_stats {

@@ -39,7 +39,8 @@ class LEParams(C.Structure):
         ("cheb_ratio", C.c_double), ("use_graphs", C.c_int),
         ("coarse_dense_max", C.c_int), ("coarse_smooth", C.c_int), ("sens_fp32", C.c_int),
         ("inner_tol", C.c_double), ("inner_maxit", C.c_int), ("adaptive_kappa", C.c_double),
-        ("extrapolate", C.c_int),
+        ("extrapolate", C.c_int), ("mass_precond", C.c_int), ("mass_precond_share", C.c_double),
+        ("mass_precond_smooth", C.c_int),
     ]
 
 

@@ -98,10 +98,13 @@ void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz) {
     p->coarse_dense_max = 4096;
     p->coarse_smooth = 12;
     p->sens_fp32 = 1;
-    p->inner_tol = 1e-4;
+    p->inner_tol = 1e-5;
     p->inner_maxit = 40;
     p->adaptive_kappa = 40.0;
     p->extrapolate = 1;
+    p->mass_precond = 2;
+    p->mass_precond_share = 0.25;
+    p->mass_precond_smooth = 0;
 }
 
 int topo_le_create(topo_le **out, const topo_le_params *p) {

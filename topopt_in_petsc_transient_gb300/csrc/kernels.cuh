@@ -457,7 +457,12 @@ static __global__ void k_mfcg_update(long long ndof, double *x, float *r32, cons
         S->total_it += 1;
         S->inner_it += 1;
         S->restart = 0;
-        if (!isfinite(tot[0]) || tot[0] <= S->tau2 * S->rr_ref || S->inner_it >= S->kmax || S->it >= S->maxit)
+        // replace when the recurrence residual has dropped by inner_tol, or
+        // when it says the solve has converged (the replacement then checks
+        // that on the true residual)
+        const double est = tot[0] / (S->sigma * S->sigma);
+        if (!isfinite(tot[0]) || tot[0] <= S->tau2 * S->rr_ref || est <= S->tol2 * S->bb || S->inner_it >= S->kmax ||
+            S->it >= S->maxit)
             S->need_replace = 1;
     }
 }

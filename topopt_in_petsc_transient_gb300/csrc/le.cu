@@ -13,6 +13,7 @@
 // multigrid V-cycle (Chebyshev-Jacobi smoothing, trilinear transfer,
 // rediscretised coarse operators, dense coarsest inverse), run either in FP64
 // ("plain") or in FP32 inside the FP64 outer iteration ("mixed").
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -21,6 +22,7 @@
 #include <vector>
 
 #include "le.h"
+#include "kron.cuh"
 #include "sens.cuh"
 
 namespace topo {
@@ -87,6 +89,87 @@ static double jacobi_scaled_lmax(const double *A) {
         for (int i = 0; i < 24; i++) v[i] = w[i] / nrm;
     }
     return lam;
+}
+
+// largest eigenvalue of the generalized problem KE v = mu ME v (ME SPD):
+// power iteration on C = L^-1 KE L^-T with ME = L L^T
+static double mass_scaled_lmax(const double *KE, const double *ME) {
+    double Lc[24][24] = {{0}};
+    for (int i = 0; i < 24; i++)
+        for (int j = 0; j <= i; j++) {
+            double s = ME[i * 24 + j];
+            for (int k = 0; k < j; k++) s -= Lc[i][k] * Lc[j][k];
+            Lc[i][j] = (i == j) ? sqrt(s) : s / Lc[j][j];
+        }
+    auto lsolve = [&](const double *b, double *x) {  // L x = b
+        for (int i = 0; i < 24; i++) {
+            double s = b[i];
+            for (int k = 0; k < i; k++) s -= Lc[i][k] * x[k];
+            x[i] = s / Lc[i][i];
+        }
+    };
+    auto ltsolve = [&](const double *b, double *x) {  // L^T x = b
+        for (int i = 23; i >= 0; i--) {
+            double s = b[i];
+            for (int k = i + 1; k < 24; k++) s -= Lc[k][i] * x[k];
+            x[i] = s / Lc[i][i];
+        }
+    };
+    double v[24], w[24], t[24];
+    for (int i = 0; i < 24; i++) v[i] = 1.0 + 0.37 * i - 0.01 * i * i;
+    double lam = 0.0;
+    for (int it = 0; it < 3000; it++) {
+        ltsolve(v, t);
+        for (int i = 0; i < 24; i++) {
+            double s = 0.0;
+            for (int j = 0; j < 24; j++) s += KE[i * 24 + j] * t[j];
+            w[i] = s;
+        }
+        lsolve(w, t);
+        double vv = 0.0, vt = 0.0, tt = 0.0;
+        for (int i = 0; i < 24; i++) {
+            vv += v[i] * v[i];
+            vt += v[i] * t[i];
+            tt += t[i] * t[i];
+        }
+        lam = vt / vv;
+        double nt = sqrt(tt);
+        for (int i = 0; i < 24; i++) v[i] = t[i] / nt;
+    }
+    return lam;
+}
+
+// Rows of the inverse of the assembled 1-D mass h/6 [2 1; 1 2] on n nodes
+// (a Dirichlet end decouples that node: identity row), truncated to the band
+// |i - j| <= KRON_B: tap[i][KRON_B + d] = (T^-1)_{i, i+d}.  Thomas
+// elimination per unit right-hand side.
+static void kron_band_1d(int n, double h, bool d0, bool d1, double *tap) {
+    std::vector<double> d(n), off(n, 0.0), l(n), im(n), y(n), x(n);
+    for (int i = 0; i < n; i++) d[i] = (i == 0 || i == n - 1) ? h / 3.0 : 2.0 * h / 3.0;
+    for (int i = 0; i + 1 < n; i++) off[i] = h / 6.0;
+    if (d0) {
+        d[0] = 1.0;
+        off[0] = 0.0;
+    }
+    if (d1) {
+        d[n - 1] = 1.0;
+        off[n - 2] = 0.0;
+    }
+    double m = d[0];
+    l[0] = 0.0;
+    im[0] = 1.0 / m;
+    for (int i = 1; i < n; i++) {
+        l[i] = off[i - 1] / m;
+        m = d[i] - l[i] * off[i - 1];
+        im[i] = 1.0 / m;
+    }
+    for (int i = 0; i < n * KRON_W; i++) tap[i] = 0.0;
+    for (int col = 0; col < n; col++) {  // column col of T^-1 (T symmetric: also row col)
+        for (int i = 0; i < n; i++) y[i] = (i == col ? 1.0 : 0.0) - (i > 0 ? l[i] * y[i - 1] : 0.0);
+        for (int i = n - 1; i >= 0; i--) x[i] = (y[i] - (i < n - 1 ? off[i] * x[i + 1] : 0.0)) * im[i];
+        for (int i = std::max(0, col - KRON_B); i <= std::min(n - 1, col + KRON_B); i++)
+            tap[(size_t)i * KRON_W + KRON_B + (col - i)] = x[i];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -207,6 +290,11 @@ struct Operator {
     std::vector<OpLevel> lv;
     double *Ainv_d = nullptr;
     float *Ainv_f = nullptr;
+    // Kronecker mass preconditioner: node scaling and whether it is in use
+    bool kron = false;
+    double share = 0.0;  // stiffness share (sK/sM) max(kf/mf) lambda_max(KE, ME)
+    double *kscale_d = nullptr;
+    float *kscale_f = nullptr;
 };
 
 struct TopoLE {
@@ -250,6 +338,11 @@ struct TopoLE {
     double *part = nullptr;
     unsigned int *counter = nullptr;
     unsigned long long *bbits = nullptr;
+    // Kronecker mass preconditioner tables
+    double *kron_d = nullptr;  // banded 1-D inverses [3][3][nmax][KRON_W]
+    float *kron_f = nullptr;
+    int kron_nmax = 0;
+    double mu_KM = 0.0;  // largest generalized eigenvalue of (KE, ME), fine box
     int *err = nullptr;
     long long nsolves = 0;
     long long step_kernels[2] = {0, 0}, body_kernels = 0, direct_iters = 0;
@@ -375,7 +468,7 @@ int le_alloc(TopoLE *le) {
     AG(le->st, 1);
     AG(le->part, 4 * 65536);
     AG(le->counter, 4);
-    AG(le->bbits, 2);
+    AG(le->bbits, 4);
     AG(le->err, 1);
 
     // ---- host-side geometry: masks, load location, region (SetUpBC,
@@ -428,6 +521,45 @@ int le_alloc(TopoLE *le) {
     CK(cudaMemcpy(le->P, P.data(), sizeof(double) * ne, cudaMemcpyHostToDevice));
     count_launch();
     k_count_region<<<ew_blocks(nn), EW, 0, le->stream>>>(le->g, le->P, le->cntP);
+
+    // ---- Kronecker mass preconditioner: banded 1-D inverses per axis and
+    // component; a face plane clamped for a component decouples that end ----
+    {
+        const int n3[3] = {p.nx, p.ny, p.nz};
+        const double h3[3] = {p.hx, p.hy, p.hz};
+        const int nmax = std::max(p.nx, std::max(p.ny, p.nz));
+        le->kron_nmax = nmax;
+        std::vector<double> tab((size_t)9 * nmax * KRON_W, 0.0);
+        auto plane_fixed = [&](int a, int idx, int c) {
+            const int u = (a + 1) % 3, v = (a + 2) % 3;
+            for (int jv = 0; jv < n3[v]; jv++)
+                for (int ju = 0; ju < n3[u]; ju++) {
+                    int ijk[3];
+                    ijk[a] = idx;
+                    ijk[u] = ju;
+                    ijk[v] = jv;
+                    long long n = ijk[0] + (long long)p.nx * (ijk[1] + (long long)p.ny * ijk[2]);
+                    if (!((fixed[n] >> c) & 1)) return false;
+                }
+            return true;
+        };
+        for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++)
+                kron_band_1d(n3[a], h3[a], plane_fixed(a, 0, c), plane_fixed(a, n3[a] - 1, c),
+                             tab.data() + (size_t)(a * 3 + c) * nmax * KRON_W);
+        std::vector<float> tabf(tab.begin(), tab.end());
+        AG(le->kron_d, tab.size());
+        AG(le->kron_f, tab.size());
+        CK(cudaMemcpy(le->kron_d, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(le->kron_f, tabf.data(), sizeof(float) * tabf.size(), cudaMemcpyHostToDevice));
+        double KE[576], ME[576];
+        box_element_matrices(p.hx, p.hy, p.hz, p.nu, KE, ME);
+        le->mu_KM = mass_scaled_lmax(KE, ME);
+        for (int o = 0; o < 2; o++) {
+            AG(le->ops[o].kscale_d, nn);
+            AG(le->ops[o].kscale_f, nn);
+        }
+    }
 
     // ---- multigrid levels ----
     le->nlev = p.nlvls;
@@ -558,6 +690,29 @@ static int setup_operator(TopoLE *le, int o) {
         count_launch();
         k_cheb_table<<<1, 1, 0, s>>>(op.lv[l].lohi + 2, cheb_kmax(le), op.lv[l].chebf);
     }
+    // Kronecker mass preconditioner: node scaling and the stiffness share
+    // (sK / sM) max_e(kf_e / mf_e) lambda_max(KE, ME), which bounds the
+    // operator against its mass part: u'Au <= (1 + share) sM u'Mu
+    {
+        Level &l0 = le->L[0];
+        count_launch();
+        k_kron_scale<double><<<ew_blocks(l0.g.nn()), EW, 0, s>>>(l0.g, l0.mfd, op.sM, op.kscale_d);
+        count_launch();
+        k_kron_scale<float><<<ew_blocks(l0.g.nn()), EW, 0, s>>>(l0.g, l0.mfd, op.sM, op.kscale_f);
+        op.share = 0.0;
+        if (op.sK != 0.0) {
+            unsigned long long hb = 0ull;
+            CK(cudaMemsetAsync(le->bbits + 2, 0, sizeof(unsigned long long), s));
+            count_launch();
+            k_ratio_max<<<red_blocks(l0.g.nel()), EW, 0, s>>>(l0.g.nel(), l0.kfd, l0.mfd, le->bbits + 2);
+            CK(cudaMemcpyAsync(&hb, le->bbits + 2, sizeof(hb), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            double ratio;
+            memcpy(&ratio, &hb, sizeof(ratio));
+            op.share = op.sK / op.sM * ratio * le->mu_KM;
+        }
+        op.kron = le->p.mass_precond == 1 || (le->p.mass_precond == 2 && op.share <= le->p.mass_precond_share);
+    }
     // adaptive depth: stop at the first level whose Jacobi-scaled operator is
     // well conditioned (bound hi/lo <= adaptive_kappa); a full-spectrum
     // Chebyshev polynomial solves it, so coarser corrections add nothing
@@ -621,6 +776,18 @@ VW<double> vw<double>(TopoLE *le, int o, int l) {
     Level &lv = le->L[l];
     return VW<double>{lv.db, lv.dxa, lv.dxb, lv.dd, lv.dr, le->ops[o].lv[l].dinvd, lv.kfd, lv.mfd, &lv.Cd};
 }
+template <class T>
+static const T *kron_fac(TopoLE *le);
+template <>
+const float *kron_fac<float>(TopoLE *le) { return le->kron_f; }
+template <>
+const double *kron_fac<double>(TopoLE *le) { return le->kron_d; }
+template <class T>
+static const T *kron_scale(const Operator &op);
+template <>
+const float *kron_scale<float>(const Operator &op) { return op.kscale_f; }
+template <>
+const double *kron_scale<double>(const Operator &op) { return op.kscale_d; }
 template <class T>
 static const T *ainv(TopoLE *le, int o);
 template <>
@@ -720,6 +887,62 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b, VFuse *fz = nullptr) {
     return x;
 }
 
+// Kronecker mass preconditioner applied to the fine-level residual r;
+// returns the buffer holding z = P^-1 r
+template <class T>
+static T *kron_apply(TopoLE *le, int o, const T *r) {
+    cudaStream_t s = le->stream;
+    Level &l0 = le->L[0];
+    VW<T> w = vw<T>(le, o, 0);
+    const GridDesc &g = l0.g;
+    KronBand<T> B{kron_fac<T>(le), le->kron_nmax};
+    const T *sc = kron_scale<T>(le->ops[o]);
+    const long long nd = 3 * g.nn();
+    const unsigned nb = (unsigned)((nd + 255) / 256);
+    count_launch();
+    k_kron_band<T, T, 0><<<nb, 256, 0, s>>>(g, l0.fixed, r, sc, B, nullptr, w.xb);
+    count_launch();
+    k_kron_band<T, T, 1><<<nb, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xb, w.xa);
+    count_launch();
+    k_kron_band<T, T, 2><<<nb, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb);
+    return w.xb;
+}
+
+// Chebyshev-Jacobi steps over the full spectrum of Dinv A after the
+// Kronecker solve z0: z <- z + d, d = c1 d + c2 Dinv (r - A z); with `fz`
+// (mixed FCG) the last step also forms the FCG dot products
+template <class T>
+static T *kron_smooth(TopoLE *le, int o, const T *r, T *z0, VFuse *fz) {
+    const int ns = le->p.mass_precond_smooth;
+    if (ns <= 0) return z0;
+    cudaStream_t s = le->stream;
+    Level &l0 = le->L[0];
+    VW<T> w = vw<T>(le, o, 0);
+    Operator &op = le->ops[o];
+    Weights<T> wt{op.sK != 0.0 ? w.kf : nullptr, w.mf, nullptr, (T)op.sK, (T)op.sM};
+    const double *tab = op.lv[0].chebf;
+    T *x = z0, *xo = (z0 == w.xa) ? w.xb : w.xa;
+    for (int k = 0; k < ns; k++) {
+        bool done = false;
+        if constexpr (std::is_same<T, float>::value) {
+            if (fz && k == ns - 1) {
+                PolChebDot pc{l0.fixed, wt, x, r, w.dinv, xo, w.d, tab, k, fz->q32, fz->S, fz->part};
+                launch_tile<float>(l0.g, *w.C, pc, s);
+                fz->dotted = true;
+                done = true;
+            }
+        }
+        if (!done) {
+            PolCheb<T> pc{l0.fixed, wt, x, r, w.dinv, xo, w.d, tab, k, {}};
+            launch_tile<T>(l0.g, *w.C, pc, s);
+        }
+        T *t = x;
+        x = xo;
+        xo = t;
+    }
+    return x;
+}
+
 // ---------------------------------------------------------------------------
 // flexible CG:  (N A N + I - N) x = b for operator o; sx holds the initial guess
 // ---------------------------------------------------------------------------
@@ -772,11 +995,19 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
         // The rescaling of r32 and the dot products ride on the first and
         // last fine-level smoothing steps, the direction update on PolPQ32.
         VFuse fz{le->sr, le->S, le->sq32, P2(le)};
-        if (le->ops[o].depth == 1 && le->nlev == 1 && le->coarse_dense) {
-            count_launch();  // the dense coarse solve has no smoothing step to carry the rescaling
+        float *z = nullptr;
+        if (op.kron) {
+            count_launch();
             k_mfcg_scale<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sr, le->sr32, le->S);
+            z = kron_apply<float>(le, o, le->sr32);
+            z = kron_smooth<float>(le, o, le->sr32, z, &fz);
+        } else {
+            if (le->ops[o].depth == 1 && le->nlev == 1 && le->coarse_dense) {
+                count_launch();  // the dense coarse solve has no smoothing step to carry the rescaling
+                k_mfcg_scale<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sr, le->sr32, le->S);
+            }
+            z = vcycle<float>(le, o, 0, le->sr32, &fz);
         }
-        float *z = vcycle<float>(le, o, 0, le->sr32, &fz);
         if (!fz.dotted) {
             count_launch();
             k_mfcg_dot<<<red_blocks(nd), EW, 0, s>>>(nd, z, le->sr32, le->sq32, le->S, P2(le));
@@ -792,7 +1023,8 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
         launch_tile<df>(l0.g, le->Cx, rp, s);
         return;
     } else {
-        double *z = vcycle<double>(le, o, 0, le->sr);
+        double *z = op.kron ? kron_smooth<double>(le, o, le->sr, kron_apply<double>(le, o, le->sr), nullptr)
+                            : vcycle<double>(le, o, 0, le->sr);
         count_launch();
         k_fcg_dot<double><<<red_blocks(nd), EW, 0, s>>>(nd, z, le->sr, le->sq, le->S, P2(le));
         count_launch();

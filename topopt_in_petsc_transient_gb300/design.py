@@ -62,10 +62,12 @@ class TopOpt:
     coarse_dense_max: int = 4096
     coarse_smooth: int = 12
     sens_fp32: bool = True
-    inner_tol: float = 1e-4
+    inner_tol: float = 1e-5
     inner_maxit: int = 40
     adaptive_kappa: float = 40.0
     extrapolate: bool = True
+    mass_precond: int = 2
+    mass_precond_smooth: int = 0
     # state
     fscale: float = 1.0
     itr: int = 0
@@ -108,7 +110,8 @@ class TopOpt:
             rtol=self.rtol, smooth=self.smooth, cheb_ratio=self.cheb_ratio, use_graphs=self.use_graphs,
             coarse_dense_max=self.coarse_dense_max, coarse_smooth=self.coarse_smooth, sens_fp32=self.sens_fp32,
             inner_tol=self.inner_tol, inner_maxit=self.inner_maxit, adaptive_kappa=self.adaptive_kappa,
-            extrapolate=self.extrapolate)
+            extrapolate=self.extrapolate, mass_precond=self.mass_precond,
+            mass_precond_smooth=self.mass_precond_smooth)
         self.filt = Filter(self.nelx, self.nely, self.nelz, self.filter, self.rmin, h=self.h, rtol=self.filter_rtol)
         self.mma = MMA(n, self.m, self.x)
         self.mma.SetAsymptotes(0.1, 0.6, 1.05)  # main.cc:58

@@ -49,7 +49,8 @@ class LinearElasticity:
                  basis=5, dalpha=1e-4, dbeta=1e-4, omega0=1.0, optimizationRegion=2, V0=None, h=(1.0, 1.0, 1.0),
                  loadsignal=0, mixed=True, rtol=1e-10, maxit=500, smooth=3, cheb_ratio=30.0, use_graphs=True,
                  coarse_dense_max=None, coarse_smooth=None, sens_fp32=None, inner_tol=None, inner_maxit=None,
-                 adaptive_kappa=None, extrapolate=None):
+                 adaptive_kappa=None, extrapolate=None, mass_precond=None, mass_precond_share=None,
+                 mass_precond_smooth=None):
         if reduction:
             raise TopoError(1, "LinearElasticity", "the SOMMG reduced-order path is not part of this build")
         L = _lib.load()
@@ -77,6 +78,12 @@ class LinearElasticity:
             p.adaptive_kappa = adaptive_kappa
         if extrapolate is not None:
             p.extrapolate = int(bool(extrapolate))
+        if mass_precond is not None:
+            p.mass_precond = int(mass_precond)
+        if mass_precond_share is not None:
+            p.mass_precond_share = mass_precond_share
+        if mass_precond_smooth is not None:
+            p.mass_precond_smooth = mass_precond_smooth
         self.params = p
         self.nelx, self.nely, self.nelz = nelx, nely, nelz
         self.nel = nelx * nely * nelz
