@@ -72,11 +72,12 @@ typedef struct topo_le_params {
                                 below it is solved by a full-spectrum Chebyshev
                                 polynomial (mass-dominated Newmark operators need
                                 no coarse correction); 0 = always full depth      */
-    int extrapolate;         /* initial guesses of the step solves: 1 = second-order
-                                (forward: Newmark predictor with the acceleration
-                                held, u + dt v + dt^2/2 a; adjoint: linear
-                                extrapolation 2 lambda+ - lambda++), 0 = the
-                                Newmark predictor u + dt v + dt^2/4 a and lambda+ */
+    int extrapolate;         /* initial guesses of the step solves: 0 = the Newmark
+                                predictor u + dt v + dt^2/4 a and lambda+;
+                                1 = u + dt v + dt^2/2 a (acceleration held) and
+                                2 lambda+ - lambda++; 2 = u + dt v + dt^2/4 (3a - a-)
+                                (acceleration extrapolated) and
+                                3 lambda+ - 3 lambda++ + lambda+++               */
     int mass_precond;        /* preconditioner of the step solves: 0 = multigrid
                                 V-cycle with Chebyshev-Jacobi smoothing, 1 =
                                 Kronecker mass preconditioner (tensor product of

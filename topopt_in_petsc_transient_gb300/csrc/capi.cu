@@ -101,7 +101,7 @@ void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz) {
     p->inner_tol = 1e-5;
     p->inner_maxit = 40;
     p->adaptive_kappa = 40.0;
-    p->extrapolate = 1;
+    p->extrapolate = 2;
     p->mass_precond = 2;
     p->mass_precond_share = 0.25;
     p->mass_precond_smooth = 0;

@@ -55,10 +55,10 @@ static __global__ void k_ratio_max(long long nel, const double *__restrict__ kf,
 // Banded application of the 1-D inverses.  T^-1 of the 1-D mass decays like
 // (2 - sqrt(3))^|i-j| = 0.268^|i-j| away from the diagonal, so each axis pass
 // applies the exact inverse rows truncated to |i - j| <= KRON_B (truncation
-// 0.268^13 < 4e-8 relative): a 25-tap stencil along that axis with position
-// dependent taps, data-parallel over all DOFs.  Tap table per axis a and
-// component c: [a][c][n_a][2 KRON_B + 1].
-constexpr int KRON_B = 12;
+// 0.268^9 < 1e-5 relative, well below the error of the density scaling): a
+// 17-tap stencil along that axis with position dependent taps, data-parallel
+// over all DOFs.  Tap table per axis a and component c: [a][c][n_a][2 KRON_B + 1].
+constexpr int KRON_B = 8;
 constexpr int KRON_W = 2 * KRON_B + 1;
 
 template <class T>
@@ -70,39 +70,90 @@ struct KronBand {
     }
 };
 
-// one axis pass over every DOF: out_q = sum_d tap[d] v_{q + d stride};
-// AXIS 0 reads the residual (masked, node-scaled), AXIS 2 writes S x on free
-// DOFs and the residual on clamped ones
-template <class T, class R, int AXIS>
-static __global__ void __launch_bounds__(256) k_kron_band(GridDesc g, const uint8_t *__restrict__ fixed,
-                                                          const R *__restrict__ r, const T *__restrict__ scale,
-                                                          KronBand<T> B, const T *__restrict__ in, T *out) {
-    const long long nd = 3 * g.nn();
-    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+// t = S N r (masked, node-scaled input of the x pass).  In the mixed FCG it
+// also re-forms r32 = sigma r after a residual replacement (S->rescale).
+template <class T, class R>
+static __global__ void __launch_bounds__(256) k_kron_prep(GridDesc g, const uint8_t *__restrict__ fixed, R *r,
+                                                          const double *__restrict__ r64, const SolveScalars *S,
+                                                          const T *__restrict__ scale, T *t) {
+    const unsigned nd = 3u * (unsigned)g.nn();
+    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nd) return;
-    const long long n = q / 3;
-    const int c = (int)(q - 3 * n);
-    const int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
-    const int pos = AXIS == 0 ? i : (AXIS == 1 ? j : k);
-    const int len = AXIS == 0 ? g.nx : (AXIS == 1 ? g.ny : g.nz);
-    const long long stride = AXIS == 0 ? 1 : (AXIS == 1 ? (long long)g.nx : (long long)g.nx * g.ny);
-    const int dlo = pos - KRON_B < 0 ? -pos : -KRON_B;
-    const int dhi = pos + KRON_B > len - 1 ? len - 1 - pos : KRON_B;
-    const T *tap = B.row(AXIS, c, pos) + KRON_B;
-    T acc = T(0);
-    for (int d = dlo; d <= dhi; d++) {
-        const long long m = n + d * stride;
-        T v;
-        if (AXIS == 0)
-            v = ((fixed[m] >> c) & 1) ? T(0) : (T)r[3 * m + c] * scale[m];
-        else
-            v = in[3 * m + c];
-        acc += tap[d] * v;
+    const unsigned n = q / 3u, c = q - 3u * n;
+    R rv;
+    if (S && S->rescale) {
+        rv = (R)(S->sigma * r64[q]);
+        r[q] = rv;
+    } else {
+        rv = r[q];
     }
-    if (AXIS == 2)
-        out[q] = ((fixed[n] >> c) & 1) ? (T)r[q] : scale[n] * acc;
-    else
-        out[q] = acc;
+    t[q] = ((fixed[n] >> c) & 1) ? T(0) : (T)rv * scale[n];
+}
+
+// one axis pass: out_q = sum_{|d| <= KRON_B} tap[pos][d] in_{q + d stride},
+// flat grid over the 3 nn DOFs (32-bit index arithmetic: 3 nn < 2^32).
+// Positions at least KRON_B from both ends read their taps' inputs directly;
+// the others clamp indices past the line end (their taps are zero).  AXIS 2
+// finishes P^-1: out = S x on free DOFs, r on clamped ones; with DOT it also
+// forms the FCG dot products z.r and z.q of its output (the role of
+// k_mfcg_dot).
+struct KronDot {
+    const float *q32;
+    SolveScalars *S;
+    Partials<2> part;
+};
+
+template <class T, class R, int AXIS, bool DOT>
+static __global__ void __launch_bounds__(256) k_kron_pass(GridDesc g, const uint8_t *__restrict__ fixed,
+                                                          const R *__restrict__ r, const T *__restrict__ scale,
+                                                          KronBand<T> B, const T *__restrict__ in, T *out, KronDot kd) {
+    const unsigned nd = 3u * (unsigned)g.nn();
+    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
+    double red[2] = {0.0, 0.0};
+    if (q < nd) {
+        const unsigned n = q / 3u, c = q - 3u * n;
+        const unsigned nx = (unsigned)g.nx, nxy = nx * (unsigned)g.ny;
+        const unsigned k = n / nxy, rem = n - k * nxy, j = rem / nx, i = rem - j * nx;
+        const int pos = AXIS == 0 ? (int)i : (AXIS == 1 ? (int)j : (int)k);
+        const int len = AXIS == 0 ? g.nx : (AXIS == 1 ? g.ny : g.nz);
+        const int stride = AXIS == 0 ? 3 : (AXIS == 1 ? 3 * (int)nx : 3 * (int)nxy);
+        const T *tap = B.row(AXIS, (int)c, pos);
+        const T *src = in + q;
+        T acc = T(0);
+        if (pos >= KRON_B && pos < len - KRON_B) {
+#pragma unroll
+            for (int d = -KRON_B; d <= KRON_B; d++) acc += tap[d + KRON_B] * src[d * stride];
+        } else {
+#pragma unroll
+            for (int d = -KRON_B; d <= KRON_B; d++) {
+                int p = pos + d;
+                p = p < 0 ? 0 : (p > len - 1 ? len - 1 : p);
+                acc += tap[d + KRON_B] * src[(p - pos) * stride];
+            }
+        }
+        if (AXIS == 2) {
+            const bool fx = (fixed[n] >> c) & 1;
+            const T z = fx ? (T)r[q] : scale[n] * acc;
+            out[q] = z;
+            if (DOT) {
+                red[0] = (double)((float)z * (float)r[q]);
+                red[1] = (double)((float)z * kd.q32[q]);
+            }
+        } else {
+            out[q] = acc;
+        }
+    }
+    if constexpr (DOT) {
+        double tot[2];
+        if (grid_reduce<256, 2>(red, kd.part, tot)) {
+            SolveScalars *S = kd.S;
+            S->rho = tot[0];
+            S->gam = tot[1];
+            S->beta = S->restart ? 0.0 : -tot[1] / S->pq;
+            if (!isfinite(S->beta)) S->beta = 0.0;
+            S->rescale = 0;
+        }
+    }
 }
 
 }  // namespace topo

@@ -318,7 +318,7 @@ struct TopoLE {
     float *cntP = nullptr;
     double *cp = nullptr;                   // (ncp+1) x 3 x ndof
     double *Uh = nullptr, *DUh = nullptr, *DDUh = nullptr;  // tsc x ndof
-    double *Lp1 = nullptr, *DLp1 = nullptr, *DDLp1 = nullptr, *DLc = nullptr, *DDLc = nullptr, *Lp2 = nullptr;
+    double *Lp1 = nullptr, *DLp1 = nullptr, *DDLp1 = nullptr, *DLc = nullptr, *DDLc = nullptr, *Lp2 = nullptr, *Lp3 = nullptr;
     double *KL = nullptr, *ML = nullptr, *hK = nullptr, *hM = nullptr;
     double *DDL0 = nullptr;
     double *df = nullptr;
@@ -442,6 +442,7 @@ int le_alloc(TopoLE *le) {
     AG(le->DLp1, nd);
     AG(le->DDLp1, nd);
     AG(le->Lp2, nd);
+    AG(le->Lp3, nd);
     AG(le->DLc, nd);
     AG(le->DDLc, nd);
     AG(le->KL, nd);
@@ -466,7 +467,12 @@ int le_alloc(TopoLE *le) {
     AG(le->sq32, nd);
     AG(le->S, 1);
     AG(le->st, 1);
-    AG(le->part, 4 * 65536);
+    {
+        // per-CTA partials: tile kernels (<= 4 sums per CTA) and the
+        // Kronecker pass with the fused dot products (2 sums per CTA)
+        const long long kron_blocks = (3LL * p.nx * p.ny * p.nz + 255) / 256;
+        AG(le->part, std::max(4LL * 65536, 2 * kron_blocks));
+    }
     AG(le->counter, 4);
     AG(le->bbits, 4);
     AG(le->err, 1);
@@ -890,21 +896,31 @@ static T *vcycle(TopoLE *le, int o, int l, const T *b, VFuse *fz = nullptr) {
 // Kronecker mass preconditioner applied to the fine-level residual r;
 // returns the buffer holding z = P^-1 r
 template <class T>
-static T *kron_apply(TopoLE *le, int o, const T *r) {
+static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     cudaStream_t s = le->stream;
     Level &l0 = le->L[0];
     VW<T> w = vw<T>(le, o, 0);
     const GridDesc &g = l0.g;
     KronBand<T> B{kron_fac<T>(le), le->kron_nmax};
     const T *sc = kron_scale<T>(le->ops[o]);
-    const long long nd = 3 * g.nn();
-    const unsigned nb = (unsigned)((nd + 255) / 256);
+    const unsigned grid = (unsigned)((3 * g.nn() + 255) / 256);
+    const bool mixed = fz && std::is_same<T, float>::value;
     count_launch();
-    k_kron_band<T, T, 0><<<nb, 256, 0, s>>>(g, l0.fixed, r, sc, B, nullptr, w.xb);
+    k_kron_prep<T, T><<<grid, 256, 0, s>>>(g, l0.fixed, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc,
+                                            w.xa);
     count_launch();
-    k_kron_band<T, T, 1><<<nb, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xb, w.xa);
+    k_kron_pass<T, T, 0, false><<<grid, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb, KronDot{});
     count_launch();
-    k_kron_band<T, T, 2><<<nb, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb);
+    k_kron_pass<T, T, 1, false><<<grid, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xb, w.xa, KronDot{});
+    count_launch();
+    if (mixed && le->p.mass_precond_smooth <= 0) {
+        k_kron_pass<T, T, 2, true><<<grid, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb,
+                                                        KronDot{fz->q32, fz->S, fz->part});
+        fz->dotted = true;
+    } else {
+        k_kron_pass<T, T, 2, false><<<grid, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb, KronDot{});
+    }
+    if (mixed) fz->scaled = true;
     return w.xb;
 }
 
@@ -997,9 +1013,7 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
         VFuse fz{le->sr, le->S, le->sq32, P2(le)};
         float *z = nullptr;
         if (op.kron) {
-            count_launch();
-            k_mfcg_scale<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sr, le->sr32, le->S);
-            z = kron_apply<float>(le, o, le->sr32);
+            z = kron_apply<float>(le, o, le->sr32, &fz);
             z = kron_smooth<float>(le, o, le->sr32, z, &fz);
         } else {
             if (le->ops[o].depth == 1 && le->nlev == 1 && le->coarse_dense) {
@@ -1144,6 +1158,11 @@ static void fwd_rhs_t(TopoLE *le) {
     // (second-order guess: the same with the acceleration held over the step,
     // u- + dt du- + dt^2/2 ddu-, the Newmark update with ddu+ = ddu-)
     pr.pred[2] = (p.ti == 0) ? 0.0 : (p.extrapolate ? 0.5 : 0.25) * dt * dt;
+    // third-order guess: the Newmark update with ddu+ extrapolated linearly,
+    // u- + dt du- + dt^2/4 (ddu- + 2 ddu- - ddu--)
+    pr.use_pred2 = (p.ti != 0 && p.extrapolate >= 2) ? 1 : 0;
+    pr.pred2[0] = 0.75 * dt * dt;
+    pr.pred2[1] = -0.25 * dt * dt;
     pr.st = le->st;
     pr.b = le->sb;
     pr.x0 = le->sx;
@@ -1235,6 +1254,7 @@ static AdjCombine adj_args(TopoLE *le, int t0mode) {
     A.DLp1 = le->DLp1;
     A.DDLp1 = le->DDLp1;
     A.Lp2 = le->Lp2;
+    A.Lp3 = le->Lp3;
     A.extrapolate = le->p.extrapolate;
     A.hK = le->hK;
     A.hM = le->hM;
@@ -1360,7 +1380,7 @@ static int adj_step(TopoLE *le, bool capturing) {
     launch_sens(le, 0);
     count_launch();
     k_adj_advance<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->DLc, le->DDLc, le->Lp1, le->DLp1, le->DDLp1,
-                                                      le->Lp2, le->st);
+                                                      le->Lp2, le->Lp3);
     count_launch();
     k_step_add<<<1, 1, 0, s>>>(le->st, -1);
     return TOPO_OK;
@@ -1541,6 +1561,7 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
     CK(cudaMemsetAsync(le->DLp1, 0, sizeof(double) * nd, s));
     CK(cudaMemsetAsync(le->DDLp1, 0, sizeof(double) * nd, s));
     CK(cudaMemsetAsync(le->Lp2, 0, sizeof(double) * nd, s));
+    CK(cudaMemsetAsync(le->Lp3, 0, sizeof(double) * nd, s));
     CK(cudaMemsetAsync(&le->st->nadj, 0, sizeof(int), s));
     CK(cudaMemsetAsync(&le->st->fx, 0, sizeof(double), s));
     for (int c = le->p.ncp - 1; c >= 0; c--) {

@@ -489,7 +489,9 @@ struct PolRhsFwd {
     double load_scale;                  // 1/(ny-1)
     int loadsignal;
     double cK[3], cM[3];                // combination coefficients of (u-, du-, ddu-)
-    double pred[3];                     // predictor coefficients
+    double pred[3];                     // predictor coefficients (u-, du-, ddu-)
+    double pred2[2];                    // with an older acceleration ddu--: (ddu-, ddu--)
+    int use_pred2;                      // 1: x0 = u- + dt du- + pred2 . (ddu-, ddu--) when ddu-- exists
     const StepCtx *st;
     double *b, *x0;
     Partials<1> part;
@@ -521,13 +523,25 @@ struct PolRhsFwd {
     __device__ void epilogue(long long n, int, int, int, const T y[3], double *) const {
         const double *u, *du, *ddu;
         prev(u, du, ddu);
+        // acceleration one step further back: history slot j-2, or the block
+        // start state for j = 1; none for j = 0
+        const double *ddu2 = nullptr;
+        if (use_pred2 && st->j >= 2)
+            ddu2 = DDUh + (long long)(st->j - 2) * ndof;
+        else if (use_pred2 && st->j == 1)
+            ddu2 = cp + (long long)st->block * 3 * ndof + 2 * ndof;
         int t = st->tsc * st->block + st->j + 1;
         double s = load_signal(loadsignal, t * st->dt) * load_scale;
         uint8_t f = fixed[n];
         for (int c = 0; c < 3; c++) {
             bool fx = (f >> c) & 1;
             b[3 * n + c] = fx ? 0.0 : (rhs0[3 * n + c] * s + todbl(y[c]));
-            x0[3 * n + c] = fx ? 0.0 : (pred[0] * u[3 * n + c] + pred[1] * du[3 * n + c] + pred[2] * ddu[3 * n + c]);
+            double xv = pred[0] * u[3 * n + c] + pred[1] * du[3 * n + c];
+            if (ddu2)
+                xv += pred2[0] * ddu[3 * n + c] + pred2[1] * ddu2[3 * n + c];
+            else
+                xv += pred[2] * ddu[3 * n + c];
+            x0[3 * n + c] = fx ? 0.0 : xv;
         }
     }
     __device__ void finish(const double *) const {}

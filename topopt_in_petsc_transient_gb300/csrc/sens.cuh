@@ -20,7 +20,7 @@ struct AdjCombine {
     const uint8_t *fixed;
     const double *KL, *ML;        // K L+ and M L+ (unmasked element sums, masked input)
     const double *Lp1, *DLp1, *DDLp1;
-    const double *Lp2;            // lambda two steps later (initial-guess extrapolation)
+    const double *Lp2, *Lp3;      // lambda two and three steps later (initial-guess extrapolation)
     int extrapolate;
     const double *hK, *hM;        // product-form objective gradients (or null)
     const float *cntP;            // per node sum of P over adjacent elements
@@ -50,6 +50,7 @@ static __global__ void k_adj_combine(AdjCombine A) {
         ddu = A.DDUstate + off;
     }
     const double *a = A.a;
+    const int nadj = A.st->nadj;  // adjoint steps done: lambda+, ++, +++ valid when nadj >= 1, 2, 3
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
         uint8_t f = A.fixed[n];
         double cnt = A.cntP[n];
@@ -88,7 +89,12 @@ static __global__ void k_adj_combine(AdjCombine A) {
                 // the reference solves (N A N + I - N) L = R1 with A = -Keff
                 // (LinearElasticity.cc:1022-1026, :924): Keff L = -R1 on free DOFs
                 A.b[i] = fx ? 0.0 : -R1;
-                A.x0[i] = fx ? 0.0 : (A.extrapolate ? 2.0 * A.Lp1[i] - A.Lp2[i] : A.Lp1[i]);
+                double g = A.Lp1[i];
+                if (A.extrapolate >= 2 && nadj >= 3)
+                    g = 3.0 * (A.Lp1[i] - A.Lp2[i]) + A.Lp3[i];
+                else if (A.extrapolate >= 1 && nadj >= 2)
+                    g = 2.0 * A.Lp1[i] - A.Lp2[i];
+                A.x0[i] = fx ? 0.0 : g;
             }
         }
     }
@@ -109,15 +115,15 @@ static __global__ void k_count_region(GridDesc g, const double *__restrict__ P, 
     }
 }
 
-// after the adjoint solve of step j: L++ <- L+ (lambda_j after the first
-// step of the sweep, so that the extrapolated guess of the next step is
-// lambda_j itself), L+ <- lambda_j, DL+ <- DL_j, DDL+ <- DDL_j
+// after the adjoint solve of step j: L+++ <- L++, L++ <- L+, L+ <- lambda_j,
+// DL+ <- DL_j, DDL+ <- DDL_j (k_adj_combine uses the older lambdas only once
+// the sweep has produced them)
 static __global__ void k_adj_advance(long long ndof, const double *__restrict__ lam, const double *__restrict__ DL,
                               const double *__restrict__ DDL, double *Lp1, double *DLp1, double *DDLp1, double *Lp2,
-                              const StepCtx *st) {
-    const bool first = st->nadj == 0;
+                              double *Lp3) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
-        Lp2[i] = first ? lam[i] : Lp1[i];
+        Lp3[i] = Lp2[i];
+        Lp2[i] = Lp1[i];
         Lp1[i] = lam[i];
         DLp1[i] = DL[i];
         DDLp1[i] = DDL[i];

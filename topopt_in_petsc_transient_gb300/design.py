@@ -65,7 +65,7 @@ class TopOpt:
     inner_tol: float = 1e-5
     inner_maxit: int = 40
     adaptive_kappa: float = 40.0
-    extrapolate: bool = True
+    extrapolate: int = 2
     mass_precond: int = 2
     mass_precond_smooth: int = 0
     # state

@@ -77,7 +77,7 @@ class LinearElasticity:
         if adaptive_kappa is not None:
             p.adaptive_kappa = adaptive_kappa
         if extrapolate is not None:
-            p.extrapolate = int(bool(extrapolate))
+            p.extrapolate = int(extrapolate)
         if mass_precond is not None:
             p.mass_precond = int(mass_precond)
         if mass_precond_share is not None:
