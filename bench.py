@@ -28,6 +28,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "forward+adjoint design iters/s on 1 GB300: mixed vs plain FP64 at equal obj. error"
+
+# DRAM bytes (read + write) per launch from ncu captures summarised under
+# profiles/, keyed by (mesh, kernel name); absent pairs report null
+TRAFFIC = {}
 UNIT = "design_iter/s"
 
 
@@ -205,39 +209,54 @@ def run_gb300(args):
     if args.e2e_steps > 0:
         e2e = run_e2e(args, wl, flush_l2)
 
-    # ---- roofline of the dominant kernel, timed in the solve ----
-    # The fine-level FP32 Chebyshev smoothing step k_tile<float,PolCheb> is
-    # the top kernel of the mixed path.  One extra design iteration (outside
-    # the timed region, same kernels launched directly instead of from CUDA
-    # graphs) brackets each of its launches with CUDA events on the library
+    # ---- roofline of the dominant kernels, timed in the solve ----
+    # One extra design iteration per kernel class (outside the timed region,
+    # the same kernels launched directly instead of from CUDA graphs)
+    # brackets each launch of that class with CUDA events on the library
     # stream; achieved = algorithmic bytes per launch / mean launch time.
     import ctypes as C
     nel = opt.nel
     nn = (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1)
     probe = TopOpt(mixed=True, **dict(wl, use_graphs=False)).setup()
-    design_iteration(probe)
-    _lib.check(L.topo_le_smoother_timing(probe.physics._h, 1, None, None), "smoother_timing")
-    design_iteration(probe)
-    tot_ms, nlaunch = C.c_double(), C.c_longlong()
-    _lib.check(L.topo_le_smoother_timing(probe.physics._h, 0, C.byref(tot_ms), C.byref(nlaunch)), "smoother_timing")
-    ms_launch = tot_ms.value / nlaunch.value if nlaunch.value > 0 else float("nan")
+    for _ in range(args.warmup):
+        design_iteration(probe)
+    peaks = load_peaks()
+    # algorithmic bytes per launch (FP32 vectors of 3 nn values, 1-byte
+    # clamp mask per node, FP32 element factors kf, mf):
+    #   PQ32: stage z and p_prev, write p and q (4 x 12 B/node), mask, kf/mf
+    #   Kronecker pass: read and write one vector (24 B/node); the last of the
+    #     three passes also reads r, q, mask and node scaling (+29 B/node)
+    #   smoothing step: x, b, 1/diag, d read, d and x written (72 B/node), mask, kf/mf
+    classes = [(1, "k_tile<float,PolPQ32> (FCG operator product q = A p with p = z + beta p_prev, FP32)",
+                49.0 * nn + 8.0 * nel),
+               (2, "k_kron_pass<float> (one axis pass of the Kronecker mass inverse, 17-tap stencil, FP32)",
+                (24.0 + 24.0 + 53.0) / 3.0 * nn),
+               (0, "k_tile<float,PolCheb> (FP32 Chebyshev-Jacobi smoothing step)", 73.0 * nn + 8.0 * nel)]
+    kern = []
+    for cls, name, nbytes in classes:
+        _lib.check(L.topo_le_kernel_timing(probe.physics._h, cls, 1, None, None), "kernel_timing")
+        design_iteration(probe)
+        tot_ms, nlaunch = C.c_double(), C.c_longlong()
+        _lib.check(L.topo_le_kernel_timing(probe.physics._h, cls, 0, C.byref(tot_ms), C.byref(nlaunch)),
+                   "kernel_timing")
+        if nlaunch.value == 0:
+            continue
+        ms_launch = tot_ms.value / nlaunch.value
+        ach = nbytes / (ms_launch * 1e-3) / 1e9
+        kern.append({"kernel": name, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach / peaks["hbm_gbs"], "ms_per_launch": ms_launch, "launches_timed": nlaunch.value,
+                     "ms_per_design_iter": tot_ms.value, "algorithmic_bytes": nbytes})
     ms_fp64 = C.c_double()
     _lib.check(L.topo_le_time_apply(probe.physics._h, 0, 5, 50, C.byref(ms_fp64)), "time_apply")
     del probe
-    peaks = load_peaks()
-    # per launch: stage x (3 nn f32), read b, 1/diag, the previous update d
-    # (absent in the first post-smoothing step, 1 of the 5 fine-level launches
-    # of a V-cycle), write d and the new iterate (3 nn f32 each), the clamp
-    # mask (1 byte/node) and the two element factors (2 nel f32)
-    bytes_cheb = (3 * 4 * (4 * 6 + 1 * 5) / 5 + 1) * nn + 2 * 4 * nel
-    achieved = bytes_cheb / (ms_launch * 1e-3) / 1e9
-    roof = {"kernel": "k_tile<float,PolCheb> (fine-level FP32 Chebyshev-Jacobi smoothing step, matrix-free hex8)",
-            "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / peaks["hbm_gbs"], "traffic": args.traffic, "peak_source": peaks["source"],
-            "ms_per_launch": ms_launch, "launches_timed": nlaunch.value, "algorithmic_bytes": bytes_cheb,
-            "timing": "CUDA events around every launch of one design iteration, library stream",
-            "fp64_apply": {"kernel": "k_tile<double,PolResid>", "ms_per_launch": ms_fp64.value,
-                           "achieved_gbs": (3 * nn * 3 * 8 + 2 * nel * 8 + nn) / (ms_fp64.value * 1e-3) / 1e9}}
+    kern.sort(key=lambda k: -k["ms_per_design_iter"])
+    roof = dict(kern[0]) if kern else {"kernel": None}
+    roof.update({"traffic": TRAFFIC.get((args.mesh, (roof.get("kernel") or "").split(" ")[0])),
+                 "peak_source": peaks["source"],
+                 "timing": "CUDA events around every launch of the class in one design iteration, library stream",
+                 "other_kernels": kern[1:],
+                 "fp64_apply": {"kernel": "k_tile<double,PolResid>", "ms_per_launch": ms_fp64.value,
+                                "achieved_gbs": (3 * nn * 3 * 8 + 2 * nel * 8 + nn) / (ms_fp64.value * 1e-3) / 1e9}})
 
     cpu = None
     if rank == 0 and args.cpu_sample and ws == 1:
@@ -294,7 +313,8 @@ def run_e2e(args, wl, flush_l2):
     fscale = None
     h2d = d2h = 0
     times = []
-    for k in range(args.e2e_steps + 1):
+    nwarm = max(1, args.warmup)  # the first pass also captures the CUDA graphs
+    for k in range(nwarm + args.e2e_steps):
         flush_l2()
         t0 = time.perf_counter()
         ph.CompleteInitialState(xP, o.Emin, o.Emax, o.Rmin, o.Rmax, o.penalK, o.penalM)
@@ -310,7 +330,7 @@ def run_e2e(args, wl, flush_l2):
         mma.DesignChange(x, xold)
         filt.FilterProject(x, xT, xP, False, o.beta, o.eta)
         t1 = time.perf_counter()
-        if k > 0:  # first pass captures the CUDA graphs
+        if k >= nwarm:  # the same design iterations as the headline
             times.append(t1 - t0)
     b = 8 * n
     h2d = b * (1 + 0 + 1 + 3 + 1 + 1 + 5 + 2 + 1)
@@ -434,7 +454,6 @@ def main():
     ap.add_argument("--plain-steps", dest="plain_steps", type=int, default=1)
     ap.add_argument("--e2e-steps", dest="e2e_steps", type=int, default=2)
     ap.add_argument("--no-cpu", dest="cpu_sample", action="store_false")
-    ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per launch of the FP32 apply")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -150,13 +150,17 @@ int topo_le_get_stats(topo_le *le, topo_le_stats *out);
  * passes of the mixed path), 3 = FP32 Chebyshev smoothing step;
  * `reps` back-to-back launches after `warmup`; returns mean ms per launch */
 int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double *ms_per_launch);
-/* in-solve timing of the fine-level FP32 Chebyshev smoothing kernel (the
- * dominant kernel of the mixed path): enable = 1 arms CUDA events around each
- * of its direct launches on the object's stream (launches replayed from CUDA
- * graphs are not seen: create the object with use_graphs = 0); enable = 0
- * disarms, waits for the stream and returns the summed launch time (ms) and
- * the number of timed launches.  One armed object per process. */
-int topo_le_smoother_timing(topo_le *le, int enable, double *ms_total, long long *launches);
+/* in-solve timing of one fine-grid kernel class: enable = 1 arms CUDA events
+ * around each direct launch of that class on the object's stream (launches
+ * replayed from CUDA graphs are not seen: create the object with
+ * use_graphs = 0); enable = 0 disarms, waits for the stream and returns the
+ * summed launch time (ms) and the number of timed launches.  One armed object
+ * per process. */
+#define TOPO_KT_SMOOTH 0  /* FP32 Chebyshev-Jacobi smoothing step (tile kernel) */
+#define TOPO_KT_PQ32 1    /* FP32 FCG operator product q = A p, p.q (tile)    */
+#define TOPO_KT_KRON 2    /* one stencil pass of the Kronecker mass inverse   */
+#define TOPO_KT_REPLACE 3 /* FP64-accurate residual replacement (tile)        */
+int topo_le_kernel_timing(topo_le *le, int kclass, int enable, double *ms_total, long long *launches);
 /* 24x24 box element matrices (E = 1, unit density) as applied by the
  * matrix-free kernels, in the local node order of DMDAGetElements_3D
  * (LinearElasticity.cc:3067-3074), row-major: the Hex8IsoparametricKE/ME

@@ -56,7 +56,7 @@ EXPORTS = [
     "topo_le_compute_objective_sensitivities", "topo_le_compute_objective_sensitivities_dev",
     "topo_le_volume_constraint", "topo_le_volume_constraint_dev",
     "topo_le_get_state", "topo_le_apply_km", "topo_le_get_stats", "topo_le_time_apply",
-    "topo_le_smoother_timing", "topo_volume_constraint_noalloc_dev",
+    "topo_le_kernel_timing", "topo_volume_constraint_noalloc_dev",
     "topo_box_element_matrices",
     "topo_pdefilt_create", "topo_pdefilt_destroy", "topo_pdefilt_filter_project", "topo_pdefilt_filter_project_dev",
     "topo_filter_project", "topo_filter_project_dev", "topo_filter_gradients", "topo_filter_gradients_dev",
@@ -98,7 +98,7 @@ def load(path=None):
         "topo_le_apply_km": (ip, [vp, vp, vp, vp]),
         "topo_le_get_stats": (ip, [vp, C.POINTER(LEStats)]),
         "topo_le_time_apply": (ip, [vp, ip, ip, ip, dp]),
-        "topo_le_smoother_timing": (ip, [vp, ip, dp, C.POINTER(C.c_longlong)]),
+        "topo_le_kernel_timing": (ip, [vp, ip, ip, dp, C.POINTER(C.c_longlong)]),
         "topo_volume_constraint_noalloc_dev": (ip, [C.c_longlong, dp, vp, vp, d]),
         "topo_box_element_matrices": (None, [d, d, d, d, vp, vp]),
         "topo_pdefilt_create": (ip, [pp, ip, ip, ip, d, d, d, d, d, ip]),

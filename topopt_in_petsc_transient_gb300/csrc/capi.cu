@@ -225,9 +225,9 @@ int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double 
     return le_time_apply(le->impl, precision, warmup, reps, ms_per_launch);
 }
 
-int topo_le_smoother_timing(topo_le *le, int enable, double *ms_total, long long *launches) {
+int topo_le_kernel_timing(topo_le *le, int kclass, int enable, double *ms_total, long long *launches) {
     if (!le) return TOPO_ERR_ARG;
-    return le_smoother_timing(le->impl, enable, ms_total, launches);
+    return le_kernel_timing(le->impl, kclass, enable, ms_total, launches);
 }
 
 void topo_box_element_matrices(double hx, double hy, double hz, double nu, double *KE, double *ME) {

@@ -70,74 +70,125 @@ struct KronBand {
     }
 };
 
-// t = S N r (masked, node-scaled input of the x pass).  In the mixed FCG it
-// also re-forms r32 = sigma r after a residual replacement (S->rescale).
-template <class T, class R>
-static __global__ void __launch_bounds__(256) k_kron_prep(GridDesc g, const uint8_t *__restrict__ fixed, R *r,
-                                                          const double *__restrict__ r64, const SolveScalars *S,
-                                                          const T *__restrict__ scale, T *t) {
-    const unsigned nd = 3u * (unsigned)g.nn();
-    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nd) return;
-    const unsigned n = q / 3u, c = q - 3u * n;
-    R rv;
-    if (S && S->rescale) {
-        rv = (R)(S->sigma * r64[q]);
-        r[q] = rv;
-    } else {
-        rv = r[q];
-    }
-    t[q] = ((fixed[n] >> c) & 1) ? T(0) : (T)rv * scale[n];
-}
-
-// one axis pass: out_q = sum_{|d| <= KRON_B} tap[pos][d] in_{q + d stride},
-// flat grid over the 3 nn DOFs (32-bit index arithmetic: 3 nn < 2^32).
-// Positions at least KRON_B from both ends read their taps' inputs directly;
-// the others clamp indices past the line end (their taps are zero).  AXIS 2
-// finishes P^-1: out = S x on free DOFs, r on clamped ones; with DOT it also
-// forms the FCG dot products z.r and z.q of its output (the role of
-// k_mfcg_dot).
+// The three axis passes stage whole grid lines in shared memory: each input
+// value is read from global memory once per pass and the 17 taps read the
+// staged line.  Pass outputs: out_q = sum_{|d| <= KRON_B} tap[pos][d] v_{pos+d}
+// with indices past a line end clamped (their taps are zero).
 struct KronDot {
     const float *q32;
     SolveScalars *S;
     Partials<2> part;
 };
 
-template <class T, class R, int AXIS, bool DOT>
-static __global__ void __launch_bounds__(256) k_kron_pass(GridDesc g, const uint8_t *__restrict__ fixed,
-                                                          const R *__restrict__ r, const T *__restrict__ scale,
-                                                          KronBand<T> B, const T *__restrict__ in, T *out, KronDot kd) {
-    const unsigned nd = 3u * (unsigned)g.nn();
-    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
-    double red[2] = {0.0, 0.0};
-    if (q < nd) {
-        const unsigned n = q / 3u, c = q - 3u * n;
-        const unsigned nx = (unsigned)g.nx, nxy = nx * (unsigned)g.ny;
-        const unsigned k = n / nxy, rem = n - k * nxy, j = rem / nx, i = rem - j * nx;
-        const int pos = AXIS == 0 ? (int)i : (AXIS == 1 ? (int)j : (int)k);
-        const int len = AXIS == 0 ? g.nx : (AXIS == 1 ? g.ny : g.nz);
-        const int stride = AXIS == 0 ? 3 : (AXIS == 1 ? 3 * (int)nx : 3 * (int)nxy);
-        const T *tap = B.row(AXIS, (int)c, pos);
-        const T *src = in + q;
+// x pass: KX_LINES x-lines (3 nx consecutive values each) per CTA.  The
+// staged input is the masked, node-scaled residual t = S N r; in the mixed
+// FCG the staging also re-forms r32 = sigma r after a residual replacement
+// (S->rescale).
+constexpr int KX_LINES = 4;
+constexpr int KRON_THREADS = 256;
+
+template <class T, class R>
+static __global__ void __launch_bounds__(KRON_THREADS)
+    k_kron_x(GridDesc g, const uint8_t *__restrict__ fixed, R *r, const double *__restrict__ r64,
+             const SolveScalars *S, const T *__restrict__ scale, KronBand<T> B, T *out) {
+    extern __shared__ __align__(16) unsigned char kron_smem[];
+    T *tile = reinterpret_cast<T *>(kron_smem);  // [KX_LINES][3 nx]
+    const int row = 3 * g.nx;
+    const long long nlines = (long long)g.ny * g.nz;
+    const long long line0 = (long long)blockIdx.x * KX_LINES;
+    const int nl = (int)(nlines - line0 < KX_LINES ? nlines - line0 : KX_LINES);
+    const bool rs = S != nullptr && S->rescale != 0;
+    const double sg = rs ? S->sigma : 1.0;
+    for (int t = threadIdx.x; t < nl * row; t += blockDim.x) {
+        const int l = t / row, w = t - l * row, c = w % 3;
+        const long long q = (line0 + l) * row + w;
+        const long long n = (line0 + l) * g.nx + w / 3;
+        R rv;
+        if (rs) {
+            rv = (R)(sg * r64[q]);
+            r[q] = rv;
+        } else {
+            rv = r[q];
+        }
+        tile[t] = ((fixed[n] >> c) & 1) ? T(0) : (T)rv * scale[n];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nl * row; t += blockDim.x) {
+        const int l = t / row, w = t - l * row, i = w / 3, c = w - 3 * i;
+        const T *tap = B.row(0, c, i);
+        const T *v = tile + l * row + c;
         T acc = T(0);
-        if (pos >= KRON_B && pos < len - KRON_B) {
+        if (i >= KRON_B && i < g.nx - KRON_B) {
 #pragma unroll
-            for (int d = -KRON_B; d <= KRON_B; d++) acc += tap[d + KRON_B] * src[d * stride];
+            for (int d = -KRON_B; d <= KRON_B; d++) acc += tap[d + KRON_B] * v[3 * (i + d)];
         } else {
 #pragma unroll
             for (int d = -KRON_B; d <= KRON_B; d++) {
-                int p = pos + d;
-                p = p < 0 ? 0 : (p > len - 1 ? len - 1 : p);
-                acc += tap[d + KRON_B] * src[(p - pos) * stride];
+                int p = i + d;
+                p = p < 0 ? 0 : (p > g.nx - 1 ? g.nx - 1 : p);
+                acc += tap[d + KRON_B] * v[3 * p];
             }
         }
+        out[(line0 + l) * row + w] = acc;
+    }
+}
+
+// y pass (AXIS 1) and z pass (AXIS 2): a CTA stages a chunk of KW values of
+// one x-row (consecutive in memory) at every position along the line.  The
+// z pass finishes P^-1: out = S x on free DOFs, r on clamped ones; with DOT it
+// also forms the FCG dot products z.r and z.q of its output.
+constexpr int KW = 32;
+
+__host__ inline unsigned kron_yz_blocks(const GridDesc &g, int axis) {
+    const int nchunk = (3 * g.nx + KW - 1) / KW;
+    return (unsigned)nchunk * (unsigned)(axis == 1 ? g.nz : g.ny);
+}
+
+template <class T, class R, int AXIS, bool DOT>
+static __global__ void __launch_bounds__(KRON_THREADS)
+    k_kron_yz(GridDesc g, const uint8_t *__restrict__ fixed, const R *__restrict__ r, const T *__restrict__ scale,
+              KronBand<T> B, const T *__restrict__ in, T *out, KronDot kd) {
+    extern __shared__ __align__(16) unsigned char kron_smem[];
+    T *tile = reinterpret_cast<T *>(kron_smem);  // [len][KW]
+    const int row = 3 * g.nx;
+    const int nchunk = (row + KW - 1) / KW;
+    const int chunk = blockIdx.x % nchunk, other = blockIdx.x / nchunk;
+    const int w0 = chunk * KW, wn = (row - w0 < KW) ? row - w0 : KW;
+    const int len = AXIS == 1 ? g.ny : g.nz;
+    const long long S = AXIS == 1 ? (long long)row : (long long)row * g.ny;
+    const long long base = AXIS == 1 ? (long long)other * row * g.ny + w0 : (long long)other * row + w0;
+    for (int t = threadIdx.x; t < len * KW; t += blockDim.x) {
+        const int p = t / KW, w = t - p * KW;
+        if (w < wn) tile[t] = in[base + p * S + w];
+    }
+    __syncthreads();
+    double red[2] = {0.0, 0.0};
+    for (int t = threadIdx.x; t < len * KW; t += blockDim.x) {
+        const int p = t / KW, w = t - p * KW;
+        if (w >= wn) continue;
+        const int c = (w0 + w) % 3;
+        const T *tap = B.row(AXIS, c, p);
+        const T *v = tile + w;
+        T acc = T(0);
+        if (p >= KRON_B && p < len - KRON_B) {
+#pragma unroll
+            for (int d = -KRON_B; d <= KRON_B; d++) acc += tap[d + KRON_B] * v[(p + d) * KW];
+        } else {
+#pragma unroll
+            for (int d = -KRON_B; d <= KRON_B; d++) {
+                int pp = p + d;
+                pp = pp < 0 ? 0 : (pp > len - 1 ? len - 1 : pp);
+                acc += tap[d + KRON_B] * v[pp * KW];
+            }
+        }
+        const long long q = base + p * S + w;
         if (AXIS == 2) {
-            const bool fx = (fixed[n] >> c) & 1;
-            const T z = fx ? (T)r[q] : scale[n] * acc;
+            const long long n = q / 3;
+            const T z = ((fixed[n] >> c) & 1) ? (T)r[q] : scale[n] * acc;
             out[q] = z;
             if (DOT) {
-                red[0] = (double)((float)z * (float)r[q]);
-                red[1] = (double)((float)z * kd.q32[q]);
+                red[0] += (double)((float)z * (float)r[q]);
+                red[1] += (double)((float)z * kd.q32[q]);
             }
         } else {
             out[q] = acc;
@@ -145,7 +196,7 @@ static __global__ void __launch_bounds__(256) k_kron_pass(GridDesc g, const uint
     }
     if constexpr (DOT) {
         double tot[2];
-        if (grid_reduce<256, 2>(red, kd.part, tot)) {
+        if (grid_reduce<KRON_THREADS, 2>(red, kd.part, tot)) {
             SolveScalars *S = kd.S;
             S->rho = tot[0];
             S->gam = tot[1];

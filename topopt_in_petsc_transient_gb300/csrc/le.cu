@@ -207,16 +207,46 @@ struct Arena {
         if (rc_) return rc_;                     \
     } while (0)
 
-// In-solve timing of the fine-level FP32 Chebyshev smoothing kernel, the
-// kernel that dominates the mixed path: when armed, every direct launch of it
-// on the grid `nn` is bracketed by a pair of CUDA events on its stream.
-// Launches recorded into a CUDA graph are not timed.
+// In-solve timing of one kernel class on the fine grid (`nn` nodes): when
+// armed, every direct launch of that class is bracketed by a pair of CUDA
+// events on its stream.  Launches recorded into a CUDA graph are not timed.
+// Classes: TOPO_KT_SMOOTH (PolCheb / PolChebDot in FP32), TOPO_KT_PQ32,
+// TOPO_KT_KRON (each Kronecker stencil pass), TOPO_KT_REPLACE (the residual
+// replacement pass, FP64-accurate).
 struct LaunchTimer {
+    int cls = -1;
     long long nn = -1;
     std::vector<cudaEvent_t> ev;
     size_t used = 0;
 };
 static LaunchTimer *g_timer = nullptr;
+
+static bool timer_begin(int cls, long long nn, cudaStream_t s) {
+    if (!g_timer || g_timer->cls != cls || g_timer->nn != nn) return false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cs);
+    if (cs != cudaStreamCaptureStatusNone) return false;
+    while (g_timer->ev.size() < g_timer->used + 2) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return false;
+        g_timer->ev.push_back(e);
+    }
+    cudaEventRecord(g_timer->ev[g_timer->used], s);
+    return true;
+}
+static void timer_end(bool timed, cudaStream_t s) {
+    if (!timed) return;
+    cudaEventRecord(g_timer->ev[g_timer->used + 1], s);
+    g_timer->used += 2;
+}
+
+template <class T, class Pol>
+constexpr int tile_class() {
+    return (std::is_same<Pol, PolCheb<float>>::value || std::is_same<Pol, PolChebDot>::value) ? TOPO_KT_SMOOTH
+           : std::is_same<Pol, PolPQ32>::value                                                 ? TOPO_KT_PQ32
+           : std::is_same<Pol, PolReplace<T>>::value                                           ? TOPO_KT_REPLACE
+                                                                                               : -1;
+}
 
 template <class T, class Pol>
 static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, cudaStream_t s) {
@@ -226,30 +256,10 @@ static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol
         cudaFuncSetAttribute(k_tile<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         attr = true;
     }
-    bool timed = false;
-    if ((std::is_same<Pol, PolCheb<float>>::value || std::is_same<Pol, PolChebDot>::value) && g_timer &&
-        g.nn() == g_timer->nn) {
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        cudaStreamIsCapturing(s, &cs);
-        timed = cs == cudaStreamCaptureStatusNone;
-        if (timed) {
-            while (g_timer->ev.size() < g_timer->used + 2) {
-                cudaEvent_t e;
-                if (cudaEventCreate(&e) != cudaSuccess) {
-                    timed = false;
-                    break;
-                }
-                g_timer->ev.push_back(e);
-            }
-        }
-        if (timed) cudaEventRecord(g_timer->ev[g_timer->used], s);
-    }
+    const bool timed = tile_class<T, Pol>() >= 0 && timer_begin(tile_class<T, Pol>(), g.nn(), s);
     count_launch();
     k_tile<T, Pol><<<tile_grid(g), TILE_THREADS, sm, s>>>(g, C, pol);
-    if (timed) {
-        cudaEventRecord(g_timer->ev[g_timer->used + 1], s);
-        g_timer->used += 2;
-    }
+    timer_end(timed, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -470,7 +480,7 @@ int le_alloc(TopoLE *le) {
     {
         // per-CTA partials: tile kernels (<= 4 sums per CTA) and the
         // Kronecker pass with the fused dot products (2 sums per CTA)
-        const long long kron_blocks = (3LL * p.nx * p.ny * p.nz + 255) / 256;
+        const long long kron_blocks = (long long)((3 * p.nx + KW - 1) / KW) * std::max(p.ny, p.nz);
         AG(le->part, std::max(4LL * 65536, 2 * kron_blocks));
     }
     AG(le->counter, 4);
@@ -717,7 +727,10 @@ static int setup_operator(TopoLE *le, int o) {
             memcpy(&ratio, &hb, sizeof(ratio));
             op.share = op.sK / op.sM * ratio * le->mu_KM;
         }
-        op.kron = le->p.mass_precond == 1 || (le->p.mass_precond == 2 && op.share <= le->p.mass_precond_share);
+        // the line-staging passes hold whole grid lines in shared memory (FP64: 8 bytes a value)
+        const size_t stage = 8 * std::max((size_t)KX_LINES * 3 * l0.g.nx, (size_t)KW * std::max(l0.g.ny, l0.g.nz));
+        op.kron = stage <= 100 * 1024 &&
+                  (le->p.mass_precond == 1 || (le->p.mass_precond == 2 && op.share <= le->p.mass_precond_share));
     }
     // adaptive depth: stop at the first level whose Jacobi-scaled operator is
     // well conditioned (bound hi/lo <= adaptive_kappa); a full-spectrum
@@ -903,25 +916,41 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     const GridDesc &g = l0.g;
     KronBand<T> B{kron_fac<T>(le), le->kron_nmax};
     const T *sc = kron_scale<T>(le->ops[o]);
-    const unsigned grid = (unsigned)((3 * g.nn() + 255) / 256);
     const bool mixed = fz && std::is_same<T, float>::value;
+    const long long nlines = (long long)g.ny * g.nz;
+    const size_t smx = sizeof(T) * KX_LINES * 3 * g.nx, smy = sizeof(T) * KW * g.ny, smz = sizeof(T) * KW * g.nz;
+    static bool attr = false;
+    if (!attr) {  // lines of up to 1024 nodes
+        cudaFuncSetAttribute(k_kron_x<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        cudaFuncSetAttribute(k_kron_yz<T, T, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        cudaFuncSetAttribute(k_kron_yz<T, T, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        cudaFuncSetAttribute(k_kron_yz<T, T, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        attr = true;
+    }
+    bool t;
     count_launch();
-    k_kron_prep<T, T><<<grid, 256, 0, s>>>(g, l0.fixed, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc,
-                                            w.xa);
+    t = timer_begin(TOPO_KT_KRON, g.nn(), s);
+    k_kron_x<T, T><<<(unsigned)((nlines + KX_LINES - 1) / KX_LINES), KRON_THREADS, smx, s>>>(
+        g, l0.fixed, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
+    timer_end(t, s);
     count_launch();
-    k_kron_pass<T, T, 0, false><<<grid, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb, KronDot{});
+    t = timer_begin(TOPO_KT_KRON, g.nn(), s);
+    k_kron_yz<T, T, 1, false><<<kron_yz_blocks(g, 1), KRON_THREADS, smy, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb,
+                                                                             KronDot{});
+    timer_end(t, s);
     count_launch();
-    k_kron_pass<T, T, 1, false><<<grid, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xb, w.xa, KronDot{});
-    count_launch();
+    t = timer_begin(TOPO_KT_KRON, g.nn(), s);
     if (mixed && le->p.mass_precond_smooth <= 0) {
-        k_kron_pass<T, T, 2, true><<<grid, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb,
-                                                        KronDot{fz->q32, fz->S, fz->part});
+        k_kron_yz<T, T, 2, true><<<kron_yz_blocks(g, 2), KRON_THREADS, smz, s>>>(g, l0.fixed, r, sc, B, w.xb, w.xa,
+                                                                                KronDot{fz->q32, fz->S, fz->part});
         fz->dotted = true;
     } else {
-        k_kron_pass<T, T, 2, false><<<grid, 256, 0, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb, KronDot{});
+        k_kron_yz<T, T, 2, false><<<kron_yz_blocks(g, 2), KRON_THREADS, smz, s>>>(g, l0.fixed, r, sc, B, w.xb, w.xa,
+                                                                                 KronDot{});
     }
+    timer_end(t, s);
     if (mixed) fz->scaled = true;
-    return w.xb;
+    return w.xa;
 }
 
 // Chebyshev-Jacobi steps over the full spectrum of Dinv A after the
@@ -1681,16 +1710,21 @@ int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms) {
     *ms = (double)t / reps;
     return TOPO_OK;
 }
-int le_smoother_timing(TopoLE *le, int enable, double *ms_total, long long *launches) {
+int le_kernel_timing(TopoLE *le, int kclass, int enable, double *ms_total, long long *launches) {
     static LaunchTimer timer;
     if (enable) {
+        if (kclass < TOPO_KT_SMOOTH || kclass > TOPO_KT_REPLACE) {
+            set_error("unknown kernel class " + std::to_string(kclass));
+            return TOPO_ERR_ARG;
+        }
+        timer.cls = kclass;
         timer.nn = le->L[0].g.nn();
         timer.used = 0;
         g_timer = &timer;
         return TOPO_OK;
     }
     if (g_timer != &timer) {
-        set_error("smoother timing was not armed");
+        set_error("kernel timing was not armed");
         return TOPO_ERR_STATE;
     }
     g_timer = nullptr;

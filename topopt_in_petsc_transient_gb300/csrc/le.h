@@ -28,7 +28,7 @@ long long le_nel(const TopoLE *le);
 long long le_ndof(const TopoLE *le);
 void *le_stream(TopoLE *le);
 int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms);
-int le_smoother_timing(TopoLE *le, int enable, double *ms_total, long long *launches);
+int le_kernel_timing(TopoLE *le, int kclass, int enable, double *ms_total, long long *launches);
 void box_element_matrices(double hx, double hy, double hz, double nu, double *KE, double *ME);
 
 }  // namespace topo
