@@ -44,6 +44,8 @@ def lib():
         L.oracle_le_total_cg_iterations.argtypes = [C.c_void_p]
         L.oracle_le_total_cg_iterations.restype = C.c_long
         L.oracle_le_apply_KM.argtypes = [C.c_void_p, dp, dp, dp]
+        L.oracle_le_reduced_objective_sensitivities.argtypes = [C.c_void_p, dp, C.c_int, C.c_double, dp, dp, dp, dp,
+                                                                dp]
         L.oracle_load_signal.argtypes = [C.c_int, C.c_double]
         L.oracle_load_signal.restype = C.c_double
         L.oracle_hex8_ke_me.argtypes = [C.c_double] * 4 + [dp, dp]
@@ -134,6 +136,19 @@ class LinearElasticity:
         rc |= self.GenerateCheckPoints()
         rc2, fx, df = self.ComputeObjectiveSensitivities(xPhys)
         return rc | rc2, fx, df
+
+    def reduced_objective_sensitivities(self, xPhys, basis, omega0):
+        """SOMMG reduced path (SOMMG.cc:40-265 + the reduction branches of
+        LinearElasticity.cc): returns rc, fx, dfdx, Q (basis x ndof), Kr, Mr."""
+        x = _f64(xPhys)
+        fx = np.zeros(1)
+        df = np.zeros(self.nel)
+        Q = np.zeros((basis, self.ndof))
+        Kr = np.zeros((basis, basis))
+        Mr = np.zeros((basis, basis))
+        rc = lib().oracle_le_reduced_objective_sensitivities(self._h, _p(x), int(basis), float(omega0), _p(fx), _p(df),
+                                                             _p(Q), _p(Kr), _p(Mr))
+        return rc, float(fx[0]), df, Q, Kr, Mr
 
     def vectors(self):
         N = np.zeros(self.ndof); P = np.zeros(self.nel); R = np.zeros(self.ndof)

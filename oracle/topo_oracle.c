@@ -1351,3 +1351,251 @@ void oracle_mma_get_state(const topo_oracle_mma *mm, double *L, double *U, doubl
     memcpy(U, mm->U, sizeof(double) * mm->n);
     memcpy(lam, mm->lam, sizeof(double) * mm->m);
 }
+
+/* ------------------------------------------------------------------ */
+/* SOMMG reduced-order path: SOMMG::ConstructBasis (SOMMG.cc:40-265) and   */
+/* the reduction branches of LinearElasticity.cc (:404-458, :993-1008,     */
+/* :1089-1107, :1225-1243, :1683-1774, :1850-1868, :2318-2336).            */
+/* ------------------------------------------------------------------ */
+
+/* P0 = K - om^2 M with Dirichlet rows: N P0 N + (I - N) (SOMMG.cc:58-72) */
+typedef struct {
+    topo_oracle *o;
+    double om2;
+} p0ctx;
+static void op_p0(void *vctx, const double *x, double *y) {
+    p0ctx *c = (p0ctx *)vctx;
+    topo_oracle *o = c->o;
+    int nd = o->ndof;
+    double *xm = o->t3, *kx = o->t4;
+    for (int i = 0; i < nd; i++) xm[i] = o->N[i] * x[i];
+    st_mult(&o->K, xm, kx);
+    st_mult(&o->M, xm, y);
+    for (int i = 0; i < nd; i++) y[i] = o->N[i] * (kx[i] - c->om2 * y[i]) + (1.0 - o->N[i]) * x[i];
+}
+
+/* dense k x k solve A x = b, LU with partial pivoting (stands in for the
+ * reference's PCLU on the SeqDense reduced matrices, SetUpSolver2) */
+static void dense_solve(int k, const double *A, const double *b, double *x) {
+    double *LU = (double *)malloc(sizeof(double) * k * k);
+    int *piv = (int *)malloc(sizeof(int) * k);
+    memcpy(LU, A, sizeof(double) * k * k);
+    for (int i = 0; i < k; i++) piv[i] = i;
+    for (int c = 0; c < k; c++) {
+        int pr = c;
+        for (int r = c + 1; r < k; r++)
+            if (fabs(LU[r * k + c]) > fabs(LU[pr * k + c])) pr = r;
+        if (pr != c) {
+            for (int j = 0; j < k; j++) {
+                double t = LU[c * k + j];
+                LU[c * k + j] = LU[pr * k + j];
+                LU[pr * k + j] = t;
+            }
+            int t = piv[c];
+            piv[c] = piv[pr];
+            piv[pr] = t;
+        }
+        for (int r = c + 1; r < k; r++) {
+            double f = LU[r * k + c] / LU[c * k + c];
+            LU[r * k + c] = f;
+            for (int j = c + 1; j < k; j++) LU[r * k + j] -= f * LU[c * k + j];
+        }
+    }
+    for (int i = 0; i < k; i++) {
+        double s = b[piv[i]];
+        for (int j = 0; j < i; j++) s -= LU[i * k + j] * x[j];
+        x[i] = s;
+    }
+    for (int i = k - 1; i >= 0; i--) {
+        double s = x[i];
+        for (int j = i + 1; j < k; j++) s -= LU[i * k + j] * x[j];
+        x[i] = s / LU[i * k + i];
+    }
+    free(LU);
+    free(piv);
+}
+static void dgemv_k(int k, const double *A, const double *x, double *y) {
+    for (int i = 0; i < k; i++) {
+        double s = 0.0;
+        for (int j = 0; j < k; j++) s += A[i * k + j] * x[j];
+        y[i] = s;
+    }
+}
+/* full = sum_k r[k] Q_k (the VecAXPY lifts of LinearElasticity.cc:1089-1107) */
+static void lift(const topo_oracle *o, int k, const double *Q, const double *r, double *full) {
+    int nd = o->ndof;
+    memset(full, 0, sizeof(double) * nd);
+    for (int b = 0; b < k; b++)
+        for (int i = 0; i < nd; i++) full[i] += r[b] * Q[(size_t)b * nd + i];
+}
+
+int oracle_le_reduced_objective_sensitivities(topo_oracle *o, const double *xPhys, int k, double omega0, double *fx,
+                                              double *dfdx, double *Qout, double *Kr_out, double *Mr_out) {
+    const topo_oracle_params *p = &o->p;
+    int nd = o->ndof, Ts = o->Ts, rc = 0;
+    double *a = o->a, dt = o->dt, al = p->dalpha, be = p->dbeta;
+    rc |= oracle_le_complete_initial_state(o, xPhys); /* AssembleMass/Stiffness with xPhys */
+    /* ---- ConstructBasis (SOMMG.cc:40-214) ---- */
+    double *Q = vnew((size_t)k * nd), *Pv = vnew(nd), *f = vnew(nd), *mq = vnew(nd), *dinv = vnew(nd);
+    double *Ut = vnew((size_t)k * k);
+    double om2 = omega0 * omega0;
+    for (int i = 0; i < nd; i++) Pv[i] = o->N[i] * o->RHS0[i]; /* VecPointwiseMult(P, P, N), :75 */
+    {
+        double *dk = o->t1, *dm = o->t2;
+        st_diag(&o->K, dk);
+        st_diag(&o->M, dm);
+        for (int i = 0; i < nd; i++) dinv[i] = 1.0 / (o->N[i] * (dk[i] - om2 * dm[i]) + (1.0 - o->N[i]));
+    }
+    p0ctx pc = {o, om2};
+    for (int j = 0; j < k; j++) {
+        double *Qj = Q + (size_t)j * nd;
+        if (j == 0) {
+            rc |= pcg(op_p0, &pc, dinv, nd, Pv, Qj, p->rtol, p->maxit, &o->cg_iters); /* :78-80 */
+        } else {
+            /* fvec = 2 om M Q_{j-1} (:109-111) with M diagonally scaled by N (:68);
+             * the moment-matching correction (:113-176) is scaled by the comma
+             * expression (-1,0) == 0 at :176 and so contributes nothing */
+            const double *Qm = Q + (size_t)(j - 1) * nd;
+            for (int i = 0; i < nd; i++) mq[i] = o->N[i] * Qm[i];
+            st_mult(&o->M, mq, f);
+            for (int i = 0; i < nd; i++) f[i] = o->N[i] * (2.0 * omega0 * o->N[i] * f[i]); /* :181 */
+            rc |= pcg(op_p0, &pc, dinv, nd, f, Qj, p->rtol, p->maxit, &o->cg_iters);       /* :185 */
+            /* modified Gram-Schmidt against the accepted vectors (:195-202) */
+            for (int i = 0; i < j; i++) {
+                const double *Qi = Q + (size_t)i * nd;
+                double u = vdot(nd, Qi, Qj);
+                Ut[i * k + j] = u;
+                for (int q = 0; q < nd; q++) Qj[q] -= u * Qi[q];
+            }
+        }
+        double nrm = sqrt(vdot(nd, Qj, Qj)); /* :92, :206 */
+        Ut[j * k + j] = nrm;
+        for (int q = 0; q < nd; q++) Qj[q] /= nrm;
+    }
+    /* ---- reduced matrices and load (SOMMG.cc:228-252); Q vanishes on clamped
+     * DOFs, so the masked and unmasked products agree ---- */
+    double *Kr = vnew((size_t)k * k), *Mr = vnew((size_t)k * k), *Cr = vnew((size_t)k * k), *Pr = vnew(k);
+    double *kq = vnew(nd), *mqq = vnew(nd);
+    for (int j = 0; j < k; j++) {
+        const double *Qj = Q + (size_t)j * nd;
+        st_mult(&o->K, Qj, kq);
+        for (int i = 0; i < nd; i++) mq[i] = o->N[i] * Qj[i];
+        st_mult(&o->M, mq, mqq);
+        for (int i = 0; i < nd; i++) mqq[i] *= o->N[i];
+        for (int i = 0; i < k; i++) {
+            const double *Qi = Q + (size_t)i * nd;
+            Kr[i * k + j] = vdot(nd, Qi, kq);
+            Mr[i * k + j] = vdot(nd, Qi, mqq);
+        }
+    }
+    for (int i = 0; i < k * k; i++) Cr[i] = al * Mr[i] + be * Kr[i]; /* C = alpha M + beta K, :2605-2619 */
+    for (int i = 0; i < k; i++) Pr[i] = vdot(nd, Pv, Q + (size_t)i * nd);
+    if (Qout) memcpy(Qout, Q, sizeof(double) * k * nd);
+    if (Kr_out) memcpy(Kr_out, Kr, sizeof(double) * k * k);
+    if (Mr_out) memcpy(Mr_out, Mr, sizeof(double) * k * k);
+    /* ---- reduced Newmark (N = 1, :1000-1002), dense operators ---- */
+    double *Ke = vnew((size_t)k * k), *B1 = vnew((size_t)k * k), *B2 = vnew((size_t)k * k), *B3 = vnew((size_t)k * k);
+    for (int i = 0; i < k * k; i++) {
+        Ke[i] = Kr[i] + a[5] * Mr[i] + a[2] * Cr[i];
+        B1[i] = a[5] * Mr[i] + a[2] * Cr[i];
+        B2[i] = a[3] * Mr[i] - a[0] * Cr[i];
+        B3[i] = a[4] * Mr[i] - a[1] * Cr[i];
+    }
+    size_t hs = (size_t)Ts * k;
+    double *Ur = vnew(hs), *DUr = vnew(hs), *DDUr = vnew(hs), *Lr = vnew(hs), *DLr = vnew(hs), *DDLr = vnew(hs);
+    double *v1 = vnew(k), *v2 = vnew(k), *v3 = vnew(k), *rr = vnew(k);
+    /* CompleteInitialState: U0 = DU0 = 0, M DDU0 = f(0) - C DU0 - K U0 (:1049-1078) */
+    double s0 = oracle_load_signal(p->loadsignal, 0.0) / (o->ny - 1);
+    for (int i = 0; i < k; i++) rr[i] = Pr[i] * s0;
+    dense_solve(k, Mr, rr, DDUr);
+    for (int t = 1; t < Ts; t++) { /* SolveStateBlock (:1298-1397) */
+        const double *u = Ur + (size_t)(t - 1) * k, *du = DUr + (size_t)(t - 1) * k, *ddu = DDUr + (size_t)(t - 1) * k;
+        double st = oracle_load_signal(p->loadsignal, t * dt) / (o->ny - 1);
+        dgemv_k(k, B1, u, v1);
+        dgemv_k(k, B2, du, v2);
+        dgemv_k(k, B3, ddu, v3);
+        for (int i = 0; i < k; i++) rr[i] = Pr[i] * st + v1[i] + v2[i] + v3[i];
+        double *un = Ur + (size_t)t * k;
+        dense_solve(k, Ke, rr, un);
+        for (int i = 0; i < k; i++) {
+            double d = un[i] - u[i];
+            DUr[(size_t)t * k + i] = a[0] * du[i] + a[1] * ddu[i] + a[2] * d;
+            DDUr[(size_t)t * k + i] = -a[3] * du[i] - a[4] * ddu[i] + a[5] * d;
+        }
+    }
+    /* ---- objective on the lifted states, every step including t = 0 (:1778-1802) ---- */
+    double *uf = vnew(nd), *duf = vnew(nd), *dduf = vnew(nd), *lf = vnew(nd);
+    double *ubf = vnew(nd), *dubf = vnew(nd), *ddubf = vnew(nd);
+    double fsum = 0.0;
+    for (int t = 0; t < Ts; t++) {
+        lift(o, k, Q, Ur + (size_t)t * k, uf);
+        lift(o, k, Q, DUr + (size_t)t * k, duf);
+        lift(o, k, Q, DDUr + (size_t)t * k, dduf);
+        fsum += objective_loop(o, uf, duf, dduf);
+    }
+    /* ---- adjoint in reduced space with projected state gradients (:2318-2336) ---- */
+    double *h1 = vnew(k), *h2 = vnew(k), *h3 = vnew(k), *Lp = vnew(k), *DLp = vnew(k), *DDLp = vnew(k);
+    for (int t = Ts - 1; t >= 1; t--) {
+        lift(o, k, Q, Ur + (size_t)t * k, uf);
+        lift(o, k, Q, DUr + (size_t)t * k, duf);
+        lift(o, k, Q, DDUr + (size_t)t * k, dduf);
+        gradient_objective_loop(o, uf, duf, dduf);
+        for (int i = 0; i < k; i++) {
+            h1[i] = vdot(nd, o->HDU, Q + (size_t)i * nd);
+            h2[i] = vdot(nd, o->HDDU, Q + (size_t)i * nd);
+            h3[i] = vdot(nd, o->HDDDU, Q + (size_t)i * nd);
+        }
+        double *Lt = Lr + (size_t)t * k, *DLt = DLr + (size_t)t * k, *DDLt = DDLr + (size_t)t * k;
+        if (t == Ts - 1) { /* :864-889 */
+            for (int i = 0; i < k; i++) {
+                DLt[i] = -h2[i];
+                DDLt[i] = -h3[i];
+                rr[i] = h1[i] - a[2] * DLt[i] - a[5] * DDLt[i]; /* -r1: -Keff L = r1 */
+            }
+        } else { /* :892-924 */
+            dgemv_k(k, B1, Lp, v1);
+            dgemv_k(k, B2, Lp, v2);
+            dgemv_k(k, B3, Lp, v3);
+            for (int i = 0; i < k; i++) {
+                DLt[i] = -(h2[i] + v2[i] - a[0] * DLp[i] + a[3] * DDLp[i]);
+                DDLt[i] = -(h3[i] + v3[i] + a[4] * DDLp[i]);
+                double v = -(h1[i] + v1[i] + a[2] * DLp[i] + a[5] * DDLp[i]) + a[2] * DLt[i] + a[5] * DDLt[i];
+                rr[i] = -v;
+            }
+        }
+        dense_solve(k, Ke, rr, Lt);
+        memcpy(Lp, Lt, sizeof(double) * k);
+        memcpy(DLp, DLt, sizeof(double) * k);
+        memcpy(DDLp, DDLt, sizeof(double) * k);
+    }
+    /* ---- sensitivities on the lifted states and adjoints (:1804-1840) ---- */
+    memset(dfdx, 0, sizeof(double) * o->nel);
+    for (int t = 1; t < Ts; t++) {
+        lift(o, k, Q, Ur + (size_t)t * k, uf);
+        lift(o, k, Q, DUr + (size_t)t * k, duf);
+        lift(o, k, Q, Lr + (size_t)t * k, lf);
+        lift(o, k, Q, Ur + (size_t)(t - 1) * k, ubf);
+        lift(o, k, Q, DUr + (size_t)(t - 1) * k, dubf);
+        lift(o, k, Q, DDUr + (size_t)(t - 1) * k, ddubf);
+        sens_loop_n(o, dfdx, uf, duf, lf, ubf, dubf, ddubf);
+    }
+    /* ---- SolveLagrange0 (:678-804) and the t = 0 sensitivities ---- */
+    lift(o, k, Q, Ur, o->U0);
+    lift(o, k, Q, DUr, o->DU0);
+    lift(o, k, Q, DDUr, o->DDU0);
+    gradient_objective_loop(o, o->U0, o->DU0, o->DDU0);
+    for (int i = 0; i < k; i++) h3[i] = vdot(nd, o->HDDDU, Q + (size_t)i * nd);
+    dgemv_k(k, B3, Lp, v3);
+    for (int i = 0; i < k; i++) rr[i] = -(h3[i] + v3[i] - a[1] * DLp[i] + a[4] * DDLp[i]);
+    double *ddl0 = vnew(k);
+    dense_solve(k, Mr, rr, ddl0);
+    lift(o, k, Q, ddl0, o->DDL0);
+    sens_loop_0(o, dfdx);
+    *fx = fsum;
+    free(Q); free(Pv); free(f); free(mq); free(dinv); free(Ut); free(Kr); free(Mr); free(Cr); free(Pr);
+    free(kq); free(mqq); free(Ke); free(B1); free(B2); free(B3); free(Ur); free(DUr); free(DDUr);
+    free(Lr); free(DLr); free(DDLr); free(v1); free(v2); free(v3); free(rr); free(uf); free(duf); free(dduf);
+    free(lf); free(ubf); free(dubf); free(ddubf); free(h1); free(h2); free(h3); free(Lp); free(DLp); free(DDLp);
+    free(ddl0);
+    return rc;
+}

@@ -62,6 +62,12 @@ void oracle_le_get_initial_state(const topo_oracle *o, double *U0, double *DU0, 
 void oracle_le_get_last_block(const topo_oracle *o, int j, double *U, double *DU, double *DDU);
 void oracle_le_get_adjoint0(const topo_oracle *o, double *L1, double *DDL0);
 long oracle_le_total_cg_iterations(const topo_oracle *o);
+/* SOMMG reduced-order path (SOMMG.cc:40-265 and the reduction branches of
+ * LinearElasticity.cc): basis of k vectors at expansion frequency omega0,
+ * reduced Newmark forward/adjoint, objective and sensitivities on lifted
+ * fields.  Q (k x ndof), Kr, Mr (k x k) are returned when non-null. */
+int oracle_le_reduced_objective_sensitivities(topo_oracle *o, const double *xPhys, int k, double omega0, double *fx,
+                                              double *dfdx, double *Q, double *Kr, double *Mr);
 /* y = kfac-weighted K x and mfac-weighted M x (assembled, no masking) */
 void oracle_le_apply_KM(const topo_oracle *o, const double *x, double *Kx, double *Mx);
 double oracle_load_signal(int which, double t);

@@ -217,3 +217,22 @@ def test_golden_fixtures_reproduce():
     KE, ME = O.hex8_ke_me()
     np.testing.assert_allclose(KE, g["KE"], rtol=0, atol=1e-15)
     np.testing.assert_allclose(O.pde_filter(4, 2, 2, x, 2.0), g["xfilt"], rtol=1e-11)
+
+
+def test_sommg_basis_and_reduced_matrices():
+    # SOMMG.cc:40-252: orthonormal basis from P0 = K - om^2 M solves, reduced
+    # matrices Kr = Q'KQ, Mr = Q'MQ symmetric; Kr matches Q'(K Q) formed here
+    n = (8, 4, 4)
+    kw = dict(ncp=1, tsc=6, t1=0.12, objective=3, loadsignal=1, dalpha=1e-3, dbeta=1e-3, rtol=1e-13)
+    rng = np.random.default_rng(3)
+    x = 0.3 + 0.1 * (2 * rng.random(np.prod(n)) - 1)
+    le = O.LinearElasticity(*n, **kw)
+    rc, fx, df, Q, Kr, Mr = le.reduced_objective_sensitivities(x, 4, 0.01)
+    assert rc == 0 and np.isfinite(fx) and np.all(np.isfinite(df))
+    assert np.abs(Q @ Q.T - np.eye(4)).max() < 1e-12
+    assert np.abs(Kr - Kr.T).max() < 1e-12 * np.abs(Kr).max()
+    assert np.abs(Mr - Mr.T).max() < 1e-12 * np.abs(Mr).max()
+    N, P, R = le.vectors()
+    assert np.abs(Q[:, N == 0.0]).max() == 0.0  # the basis vanishes on clamped DOFs
+    KQ = np.stack([le.apply_KM(q)[0] for q in Q])
+    assert np.abs(Q @ KQ.T - Kr).max() < 1e-12 * np.abs(Kr).max()
