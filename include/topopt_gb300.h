@@ -90,6 +90,9 @@ typedef struct topo_le_params {
                                 applied after the Kronecker solve; they remove
                                 the error of its density scaling where the
                                 design varies sharply                             */
+    int reduction;           /* 1: SOMMG reduced-order path (-reduction)            */
+    int basis;               /* basis vectors of the reduction, 1..32 (-basis)      */
+    double omega0;           /* expansion frequency om of P0 = K - om^2 M (-omega0) */
 } topo_le_params;
 
 typedef struct topo_le_stats {
@@ -161,6 +164,11 @@ int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double 
 #define TOPO_KT_KRON 2    /* one stencil pass of the Kronecker mass inverse   */
 #define TOPO_KT_REPLACE 3 /* FP64-accurate residual replacement (tile)        */
 int topo_le_kernel_timing(topo_le *le, int kclass, int enable, double *ms_total, long long *launches);
+/* SOMMG reduced system of the current design (the public members QQ, Kr,
+ * Mr, Pr of SOMMG, SOMMG.h:21-22): Q (basis x 3*nn, row b = basis vector b),
+ * Kr, Mr (basis x basis, row-major), Pr (basis); any pointer may be NULL.
+ * Requires reduction = 1 and CompleteInitialState. */
+int topo_le_reduced_system(topo_le *le, double *Q, double *Kr, double *Mr, double *Pr);
 /* 24x24 box element matrices (E = 1, unit density) as applied by the
  * matrix-free kernels, in the local node order of DMDAGetElements_3D
  * (LinearElasticity.cc:3067-3074), row-major: the Hex8IsoparametricKE/ME

@@ -125,6 +125,29 @@ def test_fp32_sensitivities_every_objective(gpu, objective):
     assert _rel(df, df_r) < 1e-5
 
 
+@pytest.mark.parametrize("objective,mixed", [(3, False), (0, False), (4, True), (6, True), (5, False)])
+def test_sommg_reduced_path_matches_oracle(gpu, objective, mixed):
+    # SOMMG basis (SOMMG.cc:40-252) from FCG solves with P0 = K - om^2 M,
+    # reduced Newmark forward/adjoint, sensitivities from the accumulated
+    # reduced outer products; the oracle lifts every step to the full grid
+    # as the reference does (LinearElasticity.cc:1683-1868)
+    n = (8, 4, 4)
+    kw = dict(ncp=2, tsc=6, t1=0.24, objective=objective, loadsignal=1, dalpha=1e-3, dbeta=1e-3)
+    rng = np.random.default_rng(3)
+    x = 0.3 + 0.1 * (2 * rng.random(np.prod(n)) - 1)
+    le = _le(n, nlvls=2, mixed=mixed, rtol=1e-13, reduction=True, basis=4, omega0=0.01, **kw)
+    fx, df = _run_gpu(le, x)
+    Q, Kr, Mr, Pr = le.reduced_system()
+    ref = O.LinearElasticity(*n, rtol=1e-13, **kw)
+    rc, fx_r, df_r, Q_r, Kr_r, Mr_r = ref.reduced_objective_sensitivities(x, 4, 0.01)
+    assert rc == 0
+    assert _rel(Q, Q_r) < 1e-8
+    assert _rel(Kr, Kr_r) < 1e-8 and _rel(Mr, Mr_r) < 1e-8
+    assert abs(fx - fx_r) <= 1e-8 * abs(fx_r)
+    assert _rel(df, df_r) < 1e-7
+    assert np.all(np.isfinite(le.state(0, kw["tsc"] - 1)))
+
+
 def test_reference_pulse_and_defaults(gpu):
     # reference defaults: Emax 1e3, Rmax 4.1667e-4, reference load pulse, dt = 0.4
     n = (8, 4, 4)

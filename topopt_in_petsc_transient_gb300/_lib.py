@@ -40,7 +40,7 @@ class LEParams(C.Structure):
         ("coarse_dense_max", C.c_int), ("coarse_smooth", C.c_int), ("sens_fp32", C.c_int),
         ("inner_tol", C.c_double), ("inner_maxit", C.c_int), ("adaptive_kappa", C.c_double),
         ("extrapolate", C.c_int), ("mass_precond", C.c_int), ("mass_precond_share", C.c_double),
-        ("mass_precond_smooth", C.c_int),
+        ("mass_precond_smooth", C.c_int), ("reduction", C.c_int), ("basis", C.c_int), ("omega0", C.c_double),
     ]
 
 
@@ -56,7 +56,7 @@ EXPORTS = [
     "topo_le_compute_objective_sensitivities", "topo_le_compute_objective_sensitivities_dev",
     "topo_le_volume_constraint", "topo_le_volume_constraint_dev",
     "topo_le_get_state", "topo_le_apply_km", "topo_le_get_stats", "topo_le_time_apply",
-    "topo_le_kernel_timing", "topo_volume_constraint_noalloc_dev",
+    "topo_le_kernel_timing", "topo_volume_constraint_noalloc_dev", "topo_le_reduced_system",
     "topo_box_element_matrices",
     "topo_pdefilt_create", "topo_pdefilt_destroy", "topo_pdefilt_filter_project", "topo_pdefilt_filter_project_dev",
     "topo_filter_project", "topo_filter_project_dev", "topo_filter_gradients", "topo_filter_gradients_dev",
@@ -99,6 +99,7 @@ def load(path=None):
         "topo_le_get_stats": (ip, [vp, C.POINTER(LEStats)]),
         "topo_le_time_apply": (ip, [vp, ip, ip, ip, dp]),
         "topo_le_kernel_timing": (ip, [vp, ip, ip, dp, C.POINTER(C.c_longlong)]),
+        "topo_le_reduced_system": (ip, [vp, vp, vp, vp, vp]),
         "topo_volume_constraint_noalloc_dev": (ip, [C.c_longlong, dp, vp, vp, d]),
         "topo_box_element_matrices": (None, [d, d, d, d, vp, vp]),
         "topo_pdefilt_create": (ip, [pp, ip, ip, ip, d, d, d, d, d, ip]),

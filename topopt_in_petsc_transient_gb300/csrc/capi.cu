@@ -105,6 +105,9 @@ void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz) {
     p->mass_precond = 2;
     p->mass_precond_share = 0.25;
     p->mass_precond_smooth = 0;
+    p->reduction = 0;
+    p->basis = 5;
+    p->omega0 = 1.0;
 }
 
 int topo_le_create(topo_le **out, const topo_le_params *p) {
@@ -223,6 +226,11 @@ int topo_le_get_stats(topo_le *le, topo_le_stats *out) {
 int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double *ms_per_launch) {
     if (!le || !ms_per_launch || reps < 1 || warmup < 0 || precision < 0 || precision > 3) return TOPO_ERR_ARG;
     return le_time_apply(le->impl, precision, warmup, reps, ms_per_launch);
+}
+
+int topo_le_reduced_system(topo_le *le, double *Q, double *Kr, double *Mr, double *Pr) {
+    if (!le) return TOPO_ERR_ARG;
+    return le_reduced_system(le->impl, Q, Kr, Mr, Pr);
 }
 
 int topo_le_kernel_timing(topo_le *le, int kclass, int enable, double *ms_total, long long *launches) {

@@ -132,11 +132,14 @@ static __global__ void k_bounds(long long nel, const double *__restrict__ kf, co
     const double dK[3] = {dK0, dK1, dK2};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
         double ck = kf ? sK * kf[e] : 0.0, cm = sM * mf[e];
+        // a negative mass coefficient (the shifted operator K - om^2 M) takes
+        // the mass bounds in the opposite order
+        const double mhi = cm >= 0.0 ? lamMhi : lamMlo, mlo = cm >= 0.0 ? lamMlo : lamMhi;
         for (int c = 0; c < 3; c++) {
             double den = ck * dK[c] + cm * dM;
             if (den <= 0.0) continue;
-            hi = fmax(hi, (ck * lamK * dK[c] + cm * lamMhi * dM) / den);
-            lo = fmin(lo, (cm * lamMlo * dM) / den);
+            hi = fmax(hi, (ck * lamK * dK[c] + cm * mhi * dM) / den);
+            lo = fmin(lo, (cm * mlo * dM) / den);
         }
     }
     for (int o = 16; o > 0; o >>= 1) {

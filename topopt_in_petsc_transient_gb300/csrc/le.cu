@@ -23,7 +23,7 @@
 
 #include "le.h"
 #include "kron.cuh"
-#include "sens.cuh"
+#include "sommg.cuh"
 
 namespace topo {
 
@@ -315,7 +315,14 @@ struct TopoLE {
     double dt = 0.0, a[6] = {0};
     int nlev = 1;
     std::vector<Level> L;
-    Operator ops[2];  // 0: Newmark effective operator, 1: mass
+    Operator ops[3];  // 0: Newmark effective operator, 1: mass, 2: SOMMG P0 = K - om^2 M
+    int nops = 2;
+    // SOMMG reduced path (reduction = 1): basis Q [kb][ndof]; reduced
+    // matrices Kr, Mr, Kp, Mp, Gc, Ut [kb*kb each], Pr [kb], fx; reduced
+    // history [Ts][3][kb]; accumulators S [4][kb*kb]; Phi [4][kb][ndof]
+    int kb = 0;
+    double *Q = nullptr, *red = nullptr, *rhist = nullptr, *Sacc = nullptr, *Phi = nullptr, *mdpart = nullptr;
+    int *rstatus = nullptr;
     Arena arena;
     cudaStream_t stream = nullptr;
 
@@ -395,6 +402,11 @@ int le_create(TopoLE **out, const LEParams *pp) {
         set_error("invalid LinearElasticity parameters");
         return TOPO_ERR_ARG;
     }
+    if (p.reduction && (p.basis < 1 || p.basis > KB_MAX || !(p.omega0 > 0.0))) {
+        set_error("SOMMG reduction needs 1 <= basis <= " + std::to_string(KB_MAX) +
+                  " and omega0 > 0 (the basis recursion scales by omega0)");
+        return TOPO_ERR_ARG;
+    }
     // multigrid divisibility (TopOpt::SetUpMESH, TopOpt.cc:200-219)
     int div = 1 << (p.nlvls - 1);
     if ((p.nx - 1) % div || (p.ny - 1) % div || (p.nz - 1) % div) {
@@ -445,9 +457,11 @@ int le_alloc(TopoLE *le) {
     AG(le->mfx, ne);
     AG(le->cntP, nn);
     AG(le->cp, (size_t)(p.ncp + 1) * 3 * nd);
-    AG(le->Uh, (size_t)p.tsc * nd);
-    AG(le->DUh, (size_t)p.tsc * nd);
-    AG(le->DDUh, (size_t)p.tsc * nd);
+    // the reduced path keeps its history in reduced coordinates
+    const size_t hsteps = p.reduction ? 1 : (size_t)p.tsc;
+    AG(le->Uh, hsteps * nd);
+    AG(le->DUh, hsteps * nd);
+    AG(le->DDUh, hsteps * nd);
     AG(le->Lp1, nd);
     AG(le->DLp1, nd);
     AG(le->DDLp1, nd);
@@ -571,7 +585,8 @@ int le_alloc(TopoLE *le) {
         double KE[576], ME[576];
         box_element_matrices(p.hx, p.hy, p.hz, p.nu, KE, ME);
         le->mu_KM = mass_scaled_lmax(KE, ME);
-        for (int o = 0; o < 2; o++) {
+        le->nops = p.reduction ? 3 : 2;
+        for (int o = 0; o < le->nops; o++) {
             AG(le->ops[o].kscale_d, nn);
             AG(le->ops[o].kscale_f, nn);
         }
@@ -647,7 +662,21 @@ int le_alloc(TopoLE *le) {
     le->ops[0].sM = le->a[5] + le->a[2] * p.dalpha;
     le->ops[1].sK = 0.0;
     le->ops[1].sM = 1.0;
-    for (int o = 0; o < 2; o++) {
+    // SOMMG basis operator P0 = K - om^2 M (SOMMG.cc:58-59)
+    le->ops[2].sK = 1.0;
+    le->ops[2].sM = -p.omega0 * p.omega0;
+    if (p.reduction) {
+        le->kb = p.basis;
+        const int kb = le->kb;
+        AG(le->Q, (size_t)kb * nd);
+        AG(le->red, (size_t)6 * kb * kb + kb + 1);
+        AG(le->rhist, (size_t)le->Ts * 3 * kb);
+        AG(le->Sacc, (size_t)4 * kb * kb);
+        AG(le->Phi, (size_t)4 * kb * nd);
+        AG(le->mdpart, (size_t)kb * MD_CHUNKS);
+        AG(le->rstatus, 1);
+    }
+    for (int o = 0; o < le->nops; o++) {
         Operator &op = le->ops[o];
         op.lv.resize(le->nlev);
         for (int l = 0; l < le->nlev; l++) {
@@ -729,7 +758,7 @@ static int setup_operator(TopoLE *le, int o) {
         }
         // the line-staging passes hold whole grid lines in shared memory (FP64: 8 bytes a value)
         const size_t stage = 8 * std::max((size_t)KX_LINES * 3 * l0.g.nx, (size_t)KW * std::max(l0.g.ny, l0.g.nz));
-        op.kron = stage <= 100 * 1024 &&
+        op.kron = stage <= 100 * 1024 && op.sM > 0.0 && op.sK >= 0.0 &&
                   (le->p.mass_precond == 1 || (le->p.mass_precond == 2 && op.share <= le->p.mass_precond_share));
     }
     // adaptive depth: stop at the first level whose Jacobi-scaled operator is
@@ -1506,6 +1535,223 @@ __global__ void k_init_accel_rhs(long long nn, const uint8_t *fixed, const doubl
 // ---------------------------------------------------------------------------
 // public operations
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// SOMMG reduced path (SOMMG.cc:40-265, reduction branches of
+// LinearElasticity.cc): basis, reduced system, reduced sweeps
+// ---------------------------------------------------------------------------
+// out[b * ostride] = Q_b . y for b < kb (Q_b = Qbase + b ndof)
+static void multidot(TopoLE *le, const double *Qbase, int kb, const double *y, double *out, int ostride) {
+    cudaStream_t s = le->stream;
+    count_launch();
+    k_md_partial<<<dim3(MD_CHUNKS, kb), 256, 0, s>>>(le->ndof, Qbase, kb, y, le->mdpart);
+    count_launch();
+    k_md_final<<<1, 32, 0, s>>>(kb, MD_CHUNKS, le->mdpart, out, ostride);
+}
+
+enum { RED_KR = 0, RED_MR = 1, RED_KP = 2, RED_MP = 3, RED_GC = 4, RED_UT = 5 };
+static double *red_mat(TopoLE *le, int which) { return le->red + (size_t)which * le->kb * le->kb; }
+static double *red_pr(TopoLE *le) { return le->red + (size_t)6 * le->kb * le->kb; }
+static double *red_fx(TopoLE *le) { return red_pr(le) + le->kb; }
+
+// ConstructBasis (SOMMG.cc:40-210): Qb_0 = P0^-1 N P; Qb_j = P0^-1 N 2 om M Q_{j-1}
+// (the moment-matching correction of :113-176 is scaled by the comma
+// expression (-1,0) == 0 at :176 and so contributes nothing); modified
+// Gram-Schmidt against the accepted vectors and normalisation
+static int sommg_basis(TopoLE *le) {
+    cudaStream_t s = le->stream;
+    const long long nd = le->ndof, nn = le->nn;
+    const int kb = le->kb;
+    const uint8_t *fixed = le->L[0].fixed;
+    double *Ut = red_mat(le, RED_UT), *Pv = le->hM;
+    count_launch();
+    k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->rhs0, 1.0, Pv);  // VecPointwiseMult(P, P, N), :75
+    for (int j = 0; j < kb; j++) {
+        double *Qj = le->Q + (size_t)j * nd;
+        if (j == 0) {
+            CK(cudaMemcpyAsync(le->sb, Pv, sizeof(double) * nd, cudaMemcpyDeviceToDevice, s));
+        } else {
+            product<false, true>(le, le->Q + (size_t)(j - 1) * nd, le->ML, nullptr, 0.0, 1.0);
+            count_launch();
+            k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->ML, 2.0 * le->p.omega0, le->sb);  // :109-111, :181
+        }
+        CK(cudaMemsetAsync(le->sx, 0, sizeof(double) * nd, s));
+        int rc = solve(le, 2, le->sb, false);  // :78-80, :185
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(Qj, le->sx, sizeof(double) * nd, cudaMemcpyDeviceToDevice, s));
+        for (int i = 0; i < j; i++) {  // :195-202
+            const double *Qi = le->Q + (size_t)i * nd;
+            multidot(le, Qi, 1, Qj, Ut + (size_t)i * kb + j, 1);
+            count_launch();
+            k_axpy_dev<<<ew_blocks(nd), EW, 0, s>>>(nd, Qj, Qi, Ut + (size_t)i * kb + j);
+        }
+        multidot(le, Qj, 1, Qj, Ut + (size_t)j * kb + j, 1);  // :92, :206
+        count_launch();
+        k_normalise<<<ew_blocks(nd), EW, 0, s>>>(nd, Qj, Ut + (size_t)j * kb + j);
+        count_launch();
+        k_sqrt1<<<1, 1, 0, s>>>(Ut + (size_t)j * kb + j);
+    }
+    CK(cudaGetLastError());
+    return TOPO_OK;
+}
+
+// reduced matrices (SOMMG.cc:228-252) and the objective projections of the
+// reduced state gradients (LinearElasticity.cc:2318-2336): column j of each is
+// Q' (A Q_j); Q vanishes on clamped DOFs, so masked and unmasked products agree
+static int sommg_reduce(TopoLE *le) {
+    cudaStream_t s = le->stream;
+    const long long nd = le->ndof, nn = le->nn;
+    const int kb = le->kb, ob = le->p.objective;
+    const uint8_t *fixed = le->L[0].fixed;
+    double *tmp = le->sp;
+    for (int j = 0; j < kb; j++) {
+        const double *Qj = le->Q + (size_t)j * nd;
+        product<true, false>(le, Qj, le->KL, nullptr, 1.0, 0.0);
+        multidot(le, le->Q, kb, le->KL, red_mat(le, RED_KR) + j, kb);
+        product<false, true>(le, Qj, le->ML, nullptr, 0.0, 1.0);
+        count_launch();
+        k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->ML, 1.0, tmp);
+        multidot(le, le->Q, kb, tmp, red_mat(le, RED_MR) + j, kb);
+        if (ob == 3 || ob == 5 || ob == 6) {
+            product<true, false>(le, Qj, le->KL, le->P, 1.0, 0.0);
+            multidot(le, le->Q, kb, le->KL, red_mat(le, RED_KP) + j, kb);
+        }
+        if (ob == 4 || ob == 5 || ob == 6) {
+            product<false, true>(le, Qj, le->ML, le->P, 0.0, 1.0);
+            multidot(le, le->Q, kb, le->ML, red_mat(le, RED_MP) + j, kb);
+        }
+        if (ob <= 2) {
+            count_launch();
+            k_cnt_mul<<<ew_blocks(nn), EW, 0, s>>>(nn, le->cntP, Qj, tmp);
+            multidot(le, le->Q, kb, tmp, red_mat(le, RED_GC) + j, kb);
+        }
+    }
+    multidot(le, le->Q, kb, le->hM, red_pr(le), 1);  // Pr = Q' N P
+    CK(cudaGetLastError());
+    return TOPO_OK;
+}
+
+static RedSys red_sys(TopoLE *le) {
+    const LEParams &p = le->p;
+    const int ob = p.objective;
+    RedSys R;
+    memset(&R, 0, sizeof(R));
+    R.kb = le->kb;
+    R.Ts = le->Ts;
+    R.objective = ob;
+    R.loadsignal = p.loadsignal;
+    memcpy(R.a, le->a, sizeof(R.a));
+    R.dt = le->dt;
+    R.alpha = p.dalpha;
+    R.beta = p.dbeta;
+    R.load_scale = 1.0 / (p.ny - 1);
+    R.Kr = red_mat(le, RED_KR);
+    R.Mr = red_mat(le, RED_MR);
+    R.Kp = (ob == 3 || ob == 5 || ob == 6) ? red_mat(le, RED_KP) : nullptr;
+    R.Mp = (ob == 4 || ob == 5 || ob == 6) ? red_mat(le, RED_MP) : nullptr;
+    R.Gc = ob <= 2 ? red_mat(le, RED_GC) : nullptr;
+    R.Pr = red_pr(le);
+    R.hist = le->rhist;
+    R.S = le->Sacc;
+    R.fx = red_fx(le);
+    R.status = le->rstatus;
+    return R;
+}
+
+static int red_status(TopoLE *le) {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, le->rstatus, sizeof(int), cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaStreamSynchronize(le->stream));
+    if (h) {
+        set_error("SOMMG: singular reduced matrix (basis vectors linearly dependent?)");
+        return h;
+    }
+    return TOPO_OK;
+}
+
+static void red_attributes() {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_red_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)red_smem_bytes(KB_MAX));
+        cudaFuncSetAttribute(k_red_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)red_smem_bytes(KB_MAX));
+        attr = true;
+    }
+}
+
+// CompleteInitialState of the reduced path (LinearElasticity.cc:993-1078)
+static int sommg_initial_state(TopoLE *le) {
+    cudaStream_t s = le->stream;
+    int rc = setup_operator(le, 2);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(le->red, 0, sizeof(double) * (6 * le->kb * le->kb + le->kb + 1), s));
+    CK(cudaMemsetAsync(le->rstatus, 0, sizeof(int), s));
+    rc = sommg_basis(le);
+    if (rc) return rc;
+    rc = sommg_reduce(le);
+    if (rc) return rc;
+    red_attributes();
+    count_launch();
+    k_red_forward<<<1, 256, red_smem_bytes(le->kb), s>>>(red_sys(le));
+    CK(cudaGetLastError());
+    rc = check_err(le);
+    if (rc) return rc;
+    return red_status(le);
+}
+
+// ComputeObjectiveSensitivities of the reduced path: reduced adjoint sweep,
+// then one element pass over the accumulated S matrices
+static int sommg_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev) {
+    cudaStream_t s = le->stream;
+    const long long nd = le->ndof;
+    const int kb = le->kb, ob = le->p.objective;
+    red_attributes();
+    count_launch();
+    k_red_adjoint<<<1, 256, red_smem_bytes(kb), s>>>(red_sys(le));
+    CK(cudaGetLastError());
+    // Phi_s = Q S_s' for S_K, S_M and the objective terms in use
+    const bool useoK = ob == 3 || ob == 5 || ob == 6, useoM = ob >= 4;
+    const int ns = (useoK || useoM) ? 4 : 2;
+    count_launch();
+    k_red_phi<<<ew_blocks(nd), 256, 0, s>>>(nd, kb, le->Q, le->Sacc, ns, le->Phi);
+    RedSens A;
+    A.g = le->g;
+    A.kb = kb;
+    A.Q = le->Q;
+    A.phiK = le->Phi;
+    A.phiM = le->Phi + (size_t)kb * nd;
+    A.phioK = useoK ? le->Phi + (size_t)2 * kb * nd : nullptr;
+    A.phioM = useoM ? le->Phi + (size_t)3 * kb * nd : nullptr;
+    A.dkf = le->dkf;
+    A.dmf = le->dmf;
+    A.P = le->P;
+    A.df = le->df;
+    count_launch();
+    k_red_sens<<<red_blocks(le->nel), EW, 0, s>>>(A, le->L[0].Cd);
+    CK(cudaGetLastError());
+    if (dfdx_dev) CK(cudaMemcpyAsync(dfdx_dev, le->df, sizeof(double) * le->nel, cudaMemcpyDeviceToDevice, s));
+    double h = 0.0;
+    CK(cudaMemcpyAsync(&h, red_fx(le), sizeof(double), cudaMemcpyDeviceToHost, s));
+    int rc = red_status(le);
+    if (rc) return rc;
+    *fx = h;
+    le->stats.last_fx = h;
+    return TOPO_OK;
+}
+
+int le_reduced_system(TopoLE *le, double *Q, double *Kr, double *Mr, double *Pr) {
+    if (!le->kb || !le->design_ready) {
+        set_error("reduced_system needs reduction = 1 and CompleteInitialState");
+        return TOPO_ERR_STATE;
+    }
+    cudaStream_t s = le->stream;
+    const size_t k2 = (size_t)le->kb * le->kb;
+    if (Q) CK(cudaMemcpyAsync(Q, le->Q, sizeof(double) * le->kb * le->ndof, cudaMemcpyDeviceToHost, s));
+    if (Kr) CK(cudaMemcpyAsync(Kr, red_mat(le, RED_KR), sizeof(double) * k2, cudaMemcpyDeviceToHost, s));
+    if (Mr) CK(cudaMemcpyAsync(Mr, red_mat(le, RED_MR), sizeof(double) * k2, cudaMemcpyDeviceToHost, s));
+    if (Pr) CK(cudaMemcpyAsync(Pr, red_pr(le), sizeof(double) * le->kb, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return TOPO_OK;
+}
+
 int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, double Emax, double Rmin, double Rmax,
                               double penalK, double penalM) {
     cudaStream_t s = le->stream;
@@ -1520,6 +1766,13 @@ int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, 
         k_coarsen<<<ew_blocks(le->L[l].g.nel()), EW, 0, s>>>(le->L[l - 1].g, le->L[l].g, le->L[l - 1].kfd,
                                                              le->L[l - 1].mfd, le->L[l].kfd, le->L[l].mfd,
                                                              le->L[l].kff, le->L[l].mff);
+    }
+    if (le->kb) {
+        int rc = sommg_initial_state(le);
+        if (rc) return rc;
+        le->design_ready = 1;
+        le->last_block_resident = le->p.ncp - 1;
+        return TOPO_OK;
     }
     int rc = setup_operator(le, 0);
     if (rc) return rc;
@@ -1561,7 +1814,7 @@ int le_generate_checkpoints(TopoLE *le) {
         set_error("GenerateCheckPoints called before CompleteInitialState");
         return TOPO_ERR_STATE;
     }
-    if (le->p.ncp <= 1) return TOPO_OK;
+    if (le->p.ncp <= 1 || le->kb) return TOPO_OK;  // the reduced history is complete after CompleteInitialState
     long long nd = le->ndof;
     int tsc = le->p.tsc;
     for (int c = 0; c < le->p.ncp; c++) {
@@ -1583,6 +1836,7 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
         set_error("ComputeObjectiveSensitivities called before CompleteInitialState");
         return TOPO_ERR_STATE;
     }
+    if (le->kb) return sommg_objective_sensitivities(le, fx, dfdx_dev);
     cudaStream_t s = le->stream;
     long long nd = le->ndof;
     CK(cudaMemsetAsync(le->df, 0, sizeof(double) * le->nel, s));
@@ -1619,6 +1873,15 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
 int le_get_state(TopoLE *le, int which, int j, double *out) {
     if (which < 0 || which > 2 || j < -1 || j >= le->p.tsc) return TOPO_ERR_ARG;
     long long nd = le->ndof;
+    if (le->kb) {  // lift the reduced state (LinearElasticity.cc:1225-1243)
+        const int t = le->p.tsc * (le->p.ncp - 1) + j + 1;
+        count_launch();
+        k_lift<<<ew_blocks(nd), EW, 0, le->stream>>>(nd, le->kb, le->Q,
+                                                       le->rhist + ((size_t)t * 3 + which) * le->kb, le->sp);
+        CK(cudaMemcpyAsync(out, le->sp, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
+        CK(cudaStreamSynchronize(le->stream));
+        return TOPO_OK;
+    }
     const double *src;
     if (j < 0) {
         int blk = le->last_block_resident < 0 ? 0 : le->last_block_resident;

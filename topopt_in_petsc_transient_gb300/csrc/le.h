@@ -29,6 +29,7 @@ long long le_ndof(const TopoLE *le);
 void *le_stream(TopoLE *le);
 int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms);
 int le_kernel_timing(TopoLE *le, int kclass, int enable, double *ms_total, long long *launches);
+int le_reduced_system(TopoLE *le, double *Q, double *Kr, double *Mr, double *Pr);
 void box_element_matrices(double hx, double hy, double hz, double nu, double *KE, double *ME);
 
 }  // namespace topo

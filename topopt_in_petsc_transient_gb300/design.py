@@ -67,6 +67,9 @@ class TopOpt:
     adaptive_kappa: float = 40.0
     extrapolate: int = 2
     mass_precond: int = 2
+    reduction: bool = False  # TopOpt.cc:157-159
+    basis: int = 5
+    omega0: float = 1.0
     mass_precond_smooth: int = 0
     # state
     fscale: float = 1.0
@@ -111,7 +114,8 @@ class TopOpt:
             coarse_dense_max=self.coarse_dense_max, coarse_smooth=self.coarse_smooth, sens_fp32=self.sens_fp32,
             inner_tol=self.inner_tol, inner_maxit=self.inner_maxit, adaptive_kappa=self.adaptive_kappa,
             extrapolate=self.extrapolate, mass_precond=self.mass_precond,
-            mass_precond_smooth=self.mass_precond_smooth)
+            mass_precond_smooth=self.mass_precond_smooth, reduction=self.reduction, basis=self.basis,
+            omega0=self.omega0)
         self.filt = Filter(self.nelx, self.nely, self.nelz, self.filter, self.rmin, h=self.h, rtol=self.filter_rtol)
         self.mma = MMA(n, self.m, self.x)
         self.mma.SetAsymptotes(0.1, 0.6, 1.05)  # main.cc:58

@@ -51,8 +51,6 @@ class LinearElasticity:
                  coarse_dense_max=None, coarse_smooth=None, sens_fp32=None, inner_tol=None, inner_maxit=None,
                  adaptive_kappa=None, extrapolate=None, mass_precond=None, mass_precond_share=None,
                  mass_precond_smooth=None):
-        if reduction:
-            raise TopoError(1, "LinearElasticity", "the SOMMG reduced-order path is not part of this build")
         L = _lib.load()
         p = LEParams()
         L.topo_le_default_params(C.byref(p), nelx, nely, nelz)
@@ -62,6 +60,7 @@ class LinearElasticity:
         p.objective, p.sInt, p.mInt = objective, stiffnessInterpolation, massInterpolation
         p.boundaries, p.loadloc, p.optregion, p.loadsignal = boundaries, loadloc, optimizationRegion, loadsignal
         p.dalpha, p.dbeta = dalpha, dbeta
+        p.reduction, p.basis, p.omega0 = int(bool(reduction)), int(basis), float(omega0)
         p.mixed, p.rtol, p.maxit, p.smooth = int(bool(mixed)), rtol, maxit, smooth
         p.cheb_ratio, p.use_graphs = cheb_ratio, int(bool(use_graphs))
         if coarse_dense_max is not None:
@@ -137,6 +136,18 @@ class LinearElasticity:
         f = L.topo_le_volume_constraint_dev if dev1 else L.topo_le_volume_constraint
         check(f(self._h, C.byref(gx), a, b, volfrac), "VolumeConstraint")
         return gx.value
+
+    def reduced_system(self):
+        """SOMMG's QQ, Kr, Mr, Pr (SOMMG.h:21-22) of the current design, as numpy arrays."""
+        L = _lib.load()
+        kb, nd = self.params.basis, self.ndof
+        Q = np.zeros((kb, nd))
+        Kr = np.zeros((kb, kb))
+        Mr = np.zeros((kb, kb))
+        Pr = np.zeros(kb)
+        check(L.topo_le_reduced_system(self._h, Q.ctypes.data, Kr.ctypes.data, Mr.ctypes.data, Pr.ctypes.data),
+              "reduced_system")
+        return Q, Kr, Mr, Pr
 
     # -- inspection --------------------------------------------------------
     def state(self, which, j):
