@@ -321,6 +321,7 @@ struct TopoLE {
     // matrices Kr, Mr, Kp, Mp, Gc, Ut [kb*kb each], Pr [kb], fx; reduced
     // history [Ts][3][kb]; accumulators S [4][kb*kb]; Phi [4][kb][ndof]
     int kb = 0;
+    bool fp64_solves = false;  // the SOMMG basis solves run the FP64 FCG in either mode
     double *Q = nullptr, *red = nullptr, *rhist = nullptr, *Sacc = nullptr, *Phi = nullptr, *mdpart = nullptr;
     int *rstatus = nullptr;
     Arena arena;
@@ -1035,17 +1036,20 @@ __global__ void k_solve_check(const SolveScalars *S, int *err) {
 }
 
 static const double *&cur_b(TopoLE *le);
+// mixed-precision FCG for this solve (FP64 FCG for the plain path and for
+// solves that set fp64_solves)
+static bool mixed_fcg(const TopoLE *le) { return le->p.mixed && !le->fp64_solves; }
 template <class A>
 static void solve_init_t(TopoLE *le, int o, const double *b, cudaGraphConditionalHandle cond, int has_cond) {
     Level &l0 = le->L[0];
     Operator &op = le->ops[o];
     Weights<A> wt = fine_weights<A>(le, op.sK != 0.0, true, nullptr, op.sK, op.sM);
-    PolInitResid<A> pi{l0.fixed, wt, le->sx, b, le->sr, le->p.mixed ? le->sr32 : nullptr, le->S, cond, has_cond, P2(le)};
+    PolInitResid<A> pi{l0.fixed, wt, le->sx, b, le->sr, mixed_fcg(le) ? le->sr32 : nullptr, le->S, cond, has_cond, P2(le)};
     launch_tile<A>(l0.g, fine_const<A>(le), pi, le->stream);
 }
 static void solve_init(TopoLE *le, int o, const double *b, cudaGraphConditionalHandle cond, int has_cond) {
     cur_b(le) = b;
-    if (le->p.mixed)
+    if (mixed_fcg(le))
         solve_init_t<df>(le, o, b, cond, has_cond);
     else
         solve_init_t<double>(le, o, b, cond, has_cond);
@@ -1064,7 +1068,7 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
     Operator &op = le->ops[o];
     long long nd = le->ndof;
     unsigned nb = ew_blocks(nd);
-    if (le->p.mixed) {
+    if (mixed_fcg(le)) {
         // reliable-update mixed precision: FP32 recurrence, FP64 replacements.
         // The rescaling of r32 and the dot products ride on the first and
         // last fine-level smoothing steps, the direction update on PolPQ32.
@@ -1106,7 +1110,7 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
     PolPQ<double> pq{l0.fixed, wt, le->sp, le->sq, le->S, P1(le)};
     launch_tile<double>(l0.g, l0.Cd, pq, s);
     count_launch();
-    k_fcg_update<<<red_blocks(nd), EW, 0, s>>>(nd, le->sx, le->sr, le->p.mixed ? le->sr32 : nullptr, le->sp, le->sq, le->S,
+    k_fcg_update<<<red_blocks(nd), EW, 0, s>>>(nd, le->sx, le->sr, mixed_fcg(le) ? le->sr32 : nullptr, le->sp, le->sq, le->S,
                                    P1(le), cond, has_cond);
 }
 
@@ -1563,6 +1567,11 @@ static int sommg_basis(TopoLE *le) {
     const int kb = le->kb;
     const uint8_t *fixed = le->L[0].fixed;
     double *Ut = red_mat(le, RED_UT), *Pv = le->hM;
+    struct Fp64Solves {  // FP64 FCG for the basis solves, restored on every exit
+        TopoLE *le;
+        explicit Fp64Solves(TopoLE *l) : le(l) { le->fp64_solves = true; }
+        ~Fp64Solves() { le->fp64_solves = false; }
+    } fp64(le);
     count_launch();
     k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->rhs0, 1.0, Pv);  // VecPointwiseMult(P, P, N), :75
     for (int j = 0; j < kb; j++) {
