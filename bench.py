@@ -43,12 +43,14 @@ def workload(args):
                 objective=3, boundaries=1, loadloc=1, optimizationRegion=2, projectionFilter=False,
                 loadsignal=1, movlim=0.2, smooth=args.smooth, cheb_ratio=args.cheb_ratio, rtol=args.rtol,
                 coarse_dense_max=args.coarse_dense_max, coarse_smooth=args.coarse_smooth, sens_fp32=args.sens_fp32,
-                inner_tol=args.inner_tol, inner_maxit=args.inner_maxit, use_graphs=not args.no_graphs)
+                inner_tol=args.inner_tol, inner_maxit=args.inner_maxit, use_graphs=not args.no_graphs,
+                reduction=args.reduction, basis=args.basis, omega0=args.omega0)
 
 
 def workload_name(args):
-    return ("cantilever %s hex8, %d Newmark steps dt=%g, %d-level GMG, PDE filter r=2, MMA; objective 3"
-            % (args.mesh, args.nsteps, args.dt, args.nlvls))
+    red = (", SOMMG reduction: %d basis vectors at omega0=%g" % (args.basis, args.omega0)) if args.reduction else ""
+    return ("cantilever %s hex8, %d Newmark steps dt=%g, %d-level GMG, PDE filter r=2, MMA; objective 3%s"
+            % (args.mesh, args.nsteps, args.dt, args.nlvls, red))
 
 
 class ClockSampler:
@@ -297,7 +299,8 @@ def run_e2e(args, wl, flush_l2):
                           dalpha=o.dalpha, dbeta=o.dbeta, loadsignal=o.loadsignal, mixed=True, rtol=o.rtol,
                           smooth=o.smooth, cheb_ratio=o.cheb_ratio, use_graphs=o.use_graphs,
                           coarse_dense_max=o.coarse_dense_max, coarse_smooth=o.coarse_smooth, sens_fp32=o.sens_fp32,
-                          inner_tol=o.inner_tol, inner_maxit=o.inner_maxit)
+                          inner_tol=o.inner_tol, inner_maxit=o.inner_maxit, reduction=o.reduction, basis=o.basis,
+                          omega0=o.omega0)
     filt = Filter(o.nelx, o.nely, o.nelz, 2, o.rmin)
     mma = MMA(n, 1)
     mma.SetAsymptotes(0.1, 0.6, 1.05)
@@ -449,6 +452,10 @@ def main():
                     help="FP64 element math in the sensitivity kernel of the mixed path (default FP32)")
     ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-5)
     ap.add_argument("--inner-maxit", dest="inner_maxit", type=int, default=40)
+    ap.add_argument("--reduction", action="store_true", help="SOMMG reduced-order path")
+    ap.add_argument("--basis", type=int, default=8, help="SOMMG basis vectors (with --reduction)")
+    ap.add_argument("--omega0", type=float, default=1e-4,
+                    help="SOMMG expansion frequency; below the first eigenfrequency for an SPD P0")
     ap.add_argument("--no-graphs", dest="no_graphs", action="store_true",
                     help="launch every kernel directly (profilers see each launch); same kernels")
     ap.add_argument("--plain-steps", dest="plain_steps", type=int, default=1)
