@@ -71,21 +71,66 @@ struct KronBand {
 };
 
 // The three axis passes stage whole grid lines in shared memory: each input
-// value is read from global memory once per pass and the 17 taps read the
-// staged line.  Pass outputs: out_q = sum_{|d| <= KRON_B} tap[pos][d] v_{pos+d}
-// with indices past a line end clamped (their taps are zero).
+// value is read from global memory once per pass.  A thread computes KRON_MP
+// consecutive outputs of one line from a register window of KRON_MP + 2 KRON_B
+// staged values (3 shared-memory reads per output instead of 17).  Positions
+// at least KRON_B from both line ends use the interior taps, staged once per
+// CTA (the interior rows of the exact inverse agree with them to
+// 0.268^(2 KRON_B) relative); the others use their exact rows, which are zero
+// past the line end, so the window clamps indices there.
 struct KronDot {
     const float *q32;
     SolveScalars *S;
     Partials<2> part;
 };
 
+constexpr int KRON_THREADS = 256;
+constexpr int KRON_MP = 8;                      // outputs per thread along a line
+constexpr int KRON_WIN = KRON_MP + 2 * KRON_B;  // register window
+
+// interior taps of one axis for the three components: the exact row at the
+// middle of the line (lines shorter than 2 KRON_B + 1 have no interior)
+template <class T>
+__device__ __forceinline__ void kron_stage_interior(const KronBand<T> &B, int axis, int len, T *tint) {
+    for (int t = threadIdx.x; t < 3 * KRON_W; t += blockDim.x) {
+        const int c = t / KRON_W, d = t - c * KRON_W;
+        tint[t] = B.row(axis, c, len / 2)[d];
+    }
+}
+
+// KRON_MP outputs at positions p0.. of a staged line (value at position p is
+// src[p * sstride]); outputs past the line end are computed but not used
+template <class T>
+__device__ __forceinline__ void kron_line(const T *src, int sstride, int len, int p0, const T *tint,
+                                          const KronBand<T> &B, int axis, int c, T out[KRON_MP]) {
+    T win[KRON_WIN];
+#pragma unroll
+    for (int k = 0; k < KRON_WIN; k++) {
+        int p = p0 - KRON_B + k;
+        p = p < 0 ? 0 : (p > len - 1 ? len - 1 : p);
+        win[k] = src[p * sstride];
+    }
+#pragma unroll
+    for (int k = 0; k < KRON_MP; k++) {
+        const int pos = p0 + k;
+        const T *tp = (pos >= KRON_B && pos < len - KRON_B) ? tint + c * KRON_W
+                                                            : B.row(axis, c, pos < len ? pos : len - 1);
+        T acc = T(0);
+#pragma unroll
+        for (int d = 0; d < KRON_W; d++) acc += tp[d] * win[k + d];
+        out[k] = acc;
+    }
+}
+
 // x pass: KX_LINES x-lines (3 nx consecutive values each) per CTA.  The
 // staged input is the masked, node-scaled residual t = S N r; in the mixed
 // FCG the staging also re-forms r32 = sigma r after a residual replacement
 // (S->rescale).
-constexpr int KX_LINES = 4;
-constexpr int KRON_THREADS = 256;
+constexpr int KX_LINES = 8;
+
+__host__ inline size_t kron_x_smem(const GridDesc &g, size_t elem) {
+    return elem * ((size_t)KX_LINES * 3 * g.nx + 3 * KRON_W);
+}
 
 template <class T, class R>
 static __global__ void __launch_bounds__(KRON_THREADS)
@@ -93,16 +138,18 @@ static __global__ void __launch_bounds__(KRON_THREADS)
              const SolveScalars *S, const T *__restrict__ scale, KronBand<T> B, T *out) {
     extern __shared__ __align__(16) unsigned char kron_smem[];
     T *tile = reinterpret_cast<T *>(kron_smem);  // [KX_LINES][3 nx]
+    T *tint = tile + KX_LINES * 3 * g.nx;        // [3][KRON_W]
     const int row = 3 * g.nx;
     const long long nlines = (long long)g.ny * g.nz;
     const long long line0 = (long long)blockIdx.x * KX_LINES;
     const int nl = (int)(nlines - line0 < KX_LINES ? nlines - line0 : KX_LINES);
     const bool rs = S != nullptr && S->rescale != 0;
     const double sg = rs ? S->sigma : 1.0;
+    kron_stage_interior(B, 0, g.nx, tint);
     for (int t = threadIdx.x; t < nl * row; t += blockDim.x) {
-        const int l = t / row, w = t - l * row, c = w % 3;
+        const int l = t / row, w = t - l * row, i = w / 3, c = w - 3 * i;
         const long long q = (line0 + l) * row + w;
-        const long long n = (line0 + l) * g.nx + w / 3;
+        const long long n = (line0 + l) * g.nx + i;
         R rv;
         if (rs) {
             rv = (R)(sg * r64[q]);
@@ -113,23 +160,16 @@ static __global__ void __launch_bounds__(KRON_THREADS)
         tile[t] = ((fixed[n] >> c) & 1) ? T(0) : (T)rv * scale[n];
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < nl * row; t += blockDim.x) {
-        const int l = t / row, w = t - l * row, i = w / 3, c = w - 3 * i;
-        const T *tap = B.row(0, c, i);
-        const T *v = tile + l * row + c;
-        T acc = T(0);
-        if (i >= KRON_B && i < g.nx - KRON_B) {
+    const int ngrp = (g.nx + KRON_MP - 1) / KRON_MP;
+    for (int t = threadIdx.x; t < nl * 3 * ngrp; t += blockDim.x) {
+        const int l = t / (3 * ngrp), rem = t - l * 3 * ngrp, c = rem / ngrp, grp = rem - c * ngrp;
+        const int p0 = grp * KRON_MP;
+        T o[KRON_MP];
+        kron_line(tile + l * row + c, 3, g.nx, p0, tint, B, 0, c, o);
+        T *dst = out + (line0 + l) * row + c;
 #pragma unroll
-            for (int d = -KRON_B; d <= KRON_B; d++) acc += tap[d + KRON_B] * v[3 * (i + d)];
-        } else {
-#pragma unroll
-            for (int d = -KRON_B; d <= KRON_B; d++) {
-                int p = i + d;
-                p = p < 0 ? 0 : (p > g.nx - 1 ? g.nx - 1 : p);
-                acc += tap[d + KRON_B] * v[3 * p];
-            }
-        }
-        out[(line0 + l) * row + w] = acc;
+        for (int k = 0; k < KRON_MP; k++)
+            if (p0 + k < g.nx) dst[3 * (p0 + k)] = o[k];
     }
 }
 
@@ -143,55 +183,55 @@ __host__ inline unsigned kron_yz_blocks(const GridDesc &g, int axis) {
     const int nchunk = (3 * g.nx + KW - 1) / KW;
     return (unsigned)nchunk * (unsigned)(axis == 1 ? g.nz : g.ny);
 }
+__host__ inline size_t kron_yz_smem(const GridDesc &g, int axis, size_t elem) {
+    return elem * ((size_t)KW * (axis == 1 ? g.ny : g.nz) + 3 * KRON_W);
+}
 
 template <class T, class R, int AXIS, bool DOT>
 static __global__ void __launch_bounds__(KRON_THREADS)
     k_kron_yz(GridDesc g, const uint8_t *__restrict__ fixed, const R *__restrict__ r, const T *__restrict__ scale,
               KronBand<T> B, const T *__restrict__ in, T *out, KronDot kd) {
     extern __shared__ __align__(16) unsigned char kron_smem[];
+    const int len = AXIS == 1 ? g.ny : g.nz;
     T *tile = reinterpret_cast<T *>(kron_smem);  // [len][KW]
+    T *tint = tile + (size_t)len * KW;           // [3][KRON_W]
     const int row = 3 * g.nx;
     const int nchunk = (row + KW - 1) / KW;
     const int chunk = blockIdx.x % nchunk, other = blockIdx.x / nchunk;
     const int w0 = chunk * KW, wn = (row - w0 < KW) ? row - w0 : KW;
-    const int len = AXIS == 1 ? g.ny : g.nz;
     const long long S = AXIS == 1 ? (long long)row : (long long)row * g.ny;
     const long long base = AXIS == 1 ? (long long)other * row * g.ny + w0 : (long long)other * row + w0;
+    kron_stage_interior(B, AXIS, len, tint);
     for (int t = threadIdx.x; t < len * KW; t += blockDim.x) {
         const int p = t / KW, w = t - p * KW;
         if (w < wn) tile[t] = in[base + p * S + w];
     }
     __syncthreads();
     double red[2] = {0.0, 0.0};
-    for (int t = threadIdx.x; t < len * KW; t += blockDim.x) {
-        const int p = t / KW, w = t - p * KW;
+    const int ngrp = (len + KRON_MP - 1) / KRON_MP;
+    for (int t = threadIdx.x; t < ngrp * KW; t += blockDim.x) {
+        const int grp = t / KW, w = t - grp * KW;
         if (w >= wn) continue;
-        const int c = (w0 + w) % 3;
-        const T *tap = B.row(AXIS, c, p);
-        const T *v = tile + w;
-        T acc = T(0);
-        if (p >= KRON_B && p < len - KRON_B) {
+        const int i3 = w0 + w, i = i3 / 3, c = i3 - 3 * i;
+        const int p0 = grp * KRON_MP;
+        T o[KRON_MP];
+        kron_line(tile + w, KW, len, p0, tint, B, AXIS, c, o);
 #pragma unroll
-            for (int d = -KRON_B; d <= KRON_B; d++) acc += tap[d + KRON_B] * v[(p + d) * KW];
-        } else {
-#pragma unroll
-            for (int d = -KRON_B; d <= KRON_B; d++) {
-                int pp = p + d;
-                pp = pp < 0 ? 0 : (pp > len - 1 ? len - 1 : pp);
-                acc += tap[d + KRON_B] * v[pp * KW];
+        for (int k = 0; k < KRON_MP; k++) {
+            const int p = p0 + k;
+            if (p >= len) break;
+            const long long q = base + p * S + w;
+            if (AXIS == 2) {
+                const long long n = i + (long long)g.nx * (other + (long long)g.ny * p);
+                const T z = ((fixed[n] >> c) & 1) ? (T)r[q] : scale[n] * o[k];
+                out[q] = z;
+                if (DOT) {
+                    red[0] += (double)((float)z * (float)r[q]);
+                    red[1] += (double)((float)z * kd.q32[q]);
+                }
+            } else {
+                out[q] = o[k];
             }
-        }
-        const long long q = base + p * S + w;
-        if (AXIS == 2) {
-            const long long n = q / 3;
-            const T z = ((fixed[n] >> c) & 1) ? (T)r[q] : scale[n] * acc;
-            out[q] = z;
-            if (DOT) {
-                red[0] += (double)((float)z * (float)r[q]);
-                red[1] += (double)((float)z * kd.q32[q]);
-            }
-        } else {
-            out[q] = acc;
         }
     }
     if constexpr (DOT) {

@@ -758,7 +758,7 @@ static int setup_operator(TopoLE *le, int o) {
             op.share = op.sK / op.sM * ratio * le->mu_KM;
         }
         // the line-staging passes hold whole grid lines in shared memory (FP64: 8 bytes a value)
-        const size_t stage = 8 * std::max((size_t)KX_LINES * 3 * l0.g.nx, (size_t)KW * std::max(l0.g.ny, l0.g.nz));
+        const size_t stage = std::max(kron_x_smem(l0.g, 8), std::max(kron_yz_smem(l0.g, 1, 8), kron_yz_smem(l0.g, 2, 8)));
         op.kron = stage <= 100 * 1024 && op.sM > 0.0 && op.sK >= 0.0 &&
                   (le->p.mass_precond == 1 || (le->p.mass_precond == 2 && op.share <= le->p.mass_precond_share));
     }
@@ -948,7 +948,7 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     const T *sc = kron_scale<T>(le->ops[o]);
     const bool mixed = fz && std::is_same<T, float>::value;
     const long long nlines = (long long)g.ny * g.nz;
-    const size_t smx = sizeof(T) * KX_LINES * 3 * g.nx, smy = sizeof(T) * KW * g.ny, smz = sizeof(T) * KW * g.nz;
+    const size_t smx = kron_x_smem(g, sizeof(T)), smy = kron_yz_smem(g, 1, sizeof(T)), smz = kron_yz_smem(g, 2, sizeof(T));
     static bool attr = false;
     if (!attr) {  // lines of up to 1024 nodes
         cudaFuncSetAttribute(k_kron_x<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
