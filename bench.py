@@ -40,17 +40,38 @@ def workload(args):
     return dict(nelx=nel[0], nely=nel[1], nelz=nel[2], nlvls=args.nlvls, volfrac=0.12, V0=0.12, rmin=2.0,
                 penalK=3.0, penalM=1.0, Emax=1.0, Ef=1e-9, Rmax=1.0, Rf=1e-3, filter=2, sInt=1, mInt=0, ti=1,
                 t1=args.dt * args.nsteps, ncp=args.ncp, tsc=args.nsteps // args.ncp, dalpha=0.0, dbeta=1e-3,
-                objective=3, boundaries=1, loadloc=1, optimizationRegion=2, projectionFilter=False,
+                objective=args.objective, boundaries=1, loadloc=1, optimizationRegion=2, projectionFilter=False,
                 loadsignal=1, movlim=0.2, smooth=args.smooth, cheb_ratio=args.cheb_ratio, rtol=args.rtol,
                 coarse_dense_max=args.coarse_dense_max, coarse_smooth=args.coarse_smooth, sens_fp32=args.sens_fp32,
                 inner_tol=args.inner_tol, inner_maxit=args.inner_maxit, use_graphs=not args.no_graphs,
-                reduction=args.reduction, basis=args.basis, omega0=args.omega0)
+                reduction=args.reduction, basis=args.basis, omega0=args.omega0, 
+                noise=args.noise, **load2(args))
+
+
+def load2(args):
+    """Second point load of the extended workload: a seeded free node in the
+    outer half of the beam and a seeded phase (generator seed 0x7A11)."""
+    if not args.load2:
+        return {}
+    import numpy as np
+    nel = [int(v) for v in args.mesh.split("x")]
+    rng = np.random.default_rng(0x7A11)
+    i = int(rng.integers(nel[0] // 2, nel[0] + 1))
+    j = int(rng.integers(0, nel[1] + 1))
+    k = int(rng.integers(0, nel[2] + 1))
+    node = i + (nel[0] + 1) * (j + (nel[1] + 1) * k)
+    return {"load2_node": node, "load2_phase": float(rng.uniform(0.0, 2.0 * np.pi))}
 
 
 def workload_name(args):
     red = (", SOMMG reduction: %d basis vectors at omega0=%g" % (args.basis, args.omega0)) if args.reduction else ""
-    return ("cantilever %s hex8, %d Newmark steps dt=%g, %d-level GMG, PDE filter r=2, MMA; objective 3%s"
-            % (args.mesh, args.nsteps, args.dt, args.nlvls, red))
+    ext = ""
+    if args.noise > 0:
+        ext += ", density noise U(-%g,%g) seed 0x7A11" % (args.noise, args.noise)
+    if args.load2:
+        ext += ", second point load (node %(load2_node)d, phase %(load2_phase).4f)" % load2(args)
+    return ("cantilever %s hex8, %d Newmark steps dt=%g, %d-level GMG, PDE filter r=2, MMA; objective %d%s%s"
+            % (args.mesh, args.nsteps, args.dt, args.nlvls, args.objective, red, ext))
 
 
 class ClockSampler:
@@ -300,11 +321,13 @@ def run_e2e(args, wl, flush_l2):
                           smooth=o.smooth, cheb_ratio=o.cheb_ratio, use_graphs=o.use_graphs,
                           coarse_dense_max=o.coarse_dense_max, coarse_smooth=o.coarse_smooth, sens_fp32=o.sens_fp32,
                           inner_tol=o.inner_tol, inner_maxit=o.inner_maxit, reduction=o.reduction, basis=o.basis,
-                          omega0=o.omega0)
+                          omega0=o.omega0, load2_node=o.load2_node, load2_phase=o.load2_phase, out_dof=o.out_dof)
     filt = Filter(o.nelx, o.nely, o.nelz, 2, o.rmin)
     mma = MMA(n, 1)
     mma.SetAsymptotes(0.1, 0.6, 1.05)
     x = np.full(n, o.V0)
+    if o.noise > 0.0:
+        x += np.random.default_rng(o.seed).uniform(-o.noise, o.noise, n)
     xT = np.zeros(n)
     xP = np.zeros(n)
     xold = x.copy()
@@ -452,6 +475,9 @@ def main():
                     help="FP64 element math in the sensitivity kernel of the mixed path (default FP32)")
     ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-5)
     ap.add_argument("--inner-maxit", dest="inner_maxit", type=int, default=40)
+    ap.add_argument("--objective", type=int, default=3, help="0..6 reference objectives, 7 output-DOF displacement")
+    ap.add_argument("--noise", type=float, default=0.0, help="seeded U(-a, a) noise on the initial design")
+    ap.add_argument("--load2", action="store_true", help="seeded second point load with a seeded phase")
     ap.add_argument("--reduction", action="store_true", help="SOMMG reduced-order path")
     ap.add_argument("--basis", type=int, default=8, help="SOMMG basis vectors (with --reduction)")
     ap.add_argument("--omega0", type=float, default=1e-4,

@@ -93,6 +93,14 @@ typedef struct topo_le_params {
     int reduction;           /* 1: SOMMG reduced-order path (-reduction)            */
     int basis;               /* basis vectors of the reduction, 1..32 (-basis)      */
     double omega0;           /* expansion frequency om of P0 = K - om^2 M (-omega0) */
+    /* workload extensions with no counterpart in the reference options:
+     * a second point load in z at node load2_node (-1: none), signal
+     * sin(2 pi t + load2_phase) for t < 0.5 scaled like the line load;
+     * objective 7 = sum_t dt/2 u_out^2 of one output DOF (out_dof, -1: the z
+     * DOF of the tip-centre node).  Neither combines with reduction = 1. */
+    int load2_node;
+    double load2_phase;
+    int out_dof;
 } topo_le_params;
 
 typedef struct topo_le_stats {

@@ -19,6 +19,7 @@ class Params(C.Structure):
         ("Emin", C.c_double), ("Emax", C.c_double), ("Rmin", C.c_double), ("Rmax", C.c_double),
         ("penalK", C.c_double), ("penalM", C.c_double), ("dalpha", C.c_double), ("dbeta", C.c_double),
         ("rtol", C.c_double), ("maxit", C.c_int),
+        ("load2_node", C.c_int), ("load2_phase", C.c_double), ("out_dof", C.c_int),
     ]
 
 
@@ -93,7 +94,8 @@ def load_signal(which, t):
 
 DEFAULTS = dict(hx=1.0, hy=1.0, hz=1.0, nu=0.3, ncp=1, tsc=10, t1=0.1, ti=1, objective=3, sInt=1, mInt=0,
                 boundaries=1, loadloc=1, optregion=2, loadsignal=0, Emin=1e-9, Emax=1.0, Rmin=1e-3, Rmax=1.0,
-                penalK=3.0, penalM=1.0, dalpha=0.0, dbeta=1e-3, rtol=1e-13, maxit=100000)
+                penalK=3.0, penalM=1.0, dalpha=0.0, dbeta=1e-3, rtol=1e-13, maxit=100000, load2_node=-1,
+                load2_phase=0.0, out_dof=-1)
 
 
 class LinearElasticity:

@@ -467,6 +467,14 @@ void oracle_le_destroy(topo_oracle *o) {
 static void load(topo_oracle *o, double t) {
     double s = oracle_load_signal(o->p.loadsignal, t) / (o->ny - 1);
     for (int i = 0; i < o->ndof; i++) o->RHS[i] = o->RHS0[i] * s;
+    /* second point load (workload extension, not in the reference) */
+    if (o->p.load2_node >= 0 && o->N[3 * o->p.load2_node + 2] != 0.0)
+        o->RHS[3 * o->p.load2_node + 2] += ((t < 0.5) ? sin(2.0 * M_PI * t + o->p.load2_phase) : 0.0) / (o->ny - 1);
+}
+/* output DOF of objective 7: the z DOF of the tip-centre node by default */
+static int out_dof(const topo_oracle *o) {
+    if (o->p.out_dof >= 0) return o->p.out_dof;
+    return 3 * (o->nx - 1 + o->nx * ((o->ny - 1) / 2 + o->ny * ((o->nz - 1) / 2))) + 2;
 }
 
 /* Keff x with Keff = K + a5 M + a2 C (= -A before masking), C = alpha M + beta K,
@@ -641,6 +649,10 @@ static double eval_objective_gradient(int obj, double dt, double dkfac, double u
 /* ComputeObjectiveElementLoop, LinearElasticity.cc:2359-2452 */
 static double objective_loop(topo_oracle *o, const double *up, const double *dup, const double *ddup) {
     const topo_oracle_params *p = &o->p;
+    if (p->objective == 7) { /* extension: dt/2 u_out^2 */
+        double v = up[out_dof(o)];
+        return o->dt * 0.5 * v * v;
+    }
     double *he = vnew(o->nel);
 #pragma omp parallel for schedule(static)
     for (int e = 0; e < o->nel; e++) {
@@ -676,6 +688,10 @@ static void gradient_objective_loop(topo_oracle *o, const double *up, const doub
     memset(o->HDDU, 0, sizeof(double) * nd);
     memset(o->HDDDU, 0, sizeof(double) * nd);
     double dt = o->dt;
+    if (p->objective == 7) {
+        o->HDU[out_dof(o)] = dt * up[out_dof(o)];
+        return;
+    }
     for (int color = 0; color < 8; color++) {
         int ci = color & 1, cj = (color >> 1) & 1, ck = (color >> 2) & 1;
 #pragma omp parallel for collapse(2) schedule(static)

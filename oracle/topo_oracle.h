@@ -40,6 +40,13 @@ typedef struct {
     double Emin, Emax, Rmin, Rmax, penalK, penalM, dalpha, dbeta;
     double rtol;             /* relative residual for every CG solve                 */
     int maxit;
+    /* workload extensions (not in the reference): a second point load in z at
+     * node load2_node (-1: none) with signal sin(2 pi t + load2_phase) for
+     * t < 0.5, scaled like the line load; objective 7 = time-integrated
+     * dt/2 u^2 of one output DOF (out_dof, -1: z DOF of the tip-centre node) */
+    int load2_node;
+    double load2_phase;
+    int out_dof;
 } topo_oracle_params;
 
 typedef struct topo_oracle topo_oracle;

@@ -148,6 +148,26 @@ def test_sommg_reduced_path_matches_oracle(gpu, objective, mixed):
     assert np.all(np.isfinite(le.state(0, kw["tsc"] - 1)))
 
 
+@pytest.mark.parametrize("objective,mixed", [(7, False), (7, True), (3, True)])
+def test_extended_workload_load_and_output_objective(gpu, objective, mixed):
+    # the extended workloads: a second point load at a seeded node with a
+    # seeded phase, and objective 7 (dt/2 u^2 of the tip-centre z DOF)
+    n = (12, 6, 6)
+    rng = np.random.default_rng(0x7A11)
+    node = int(rng.integers(0, 13 * 7 * 7))
+    phase = float(rng.uniform(0.0, 2.0 * np.pi))
+    kw = dict(ncp=2, tsc=5, t1=0.2, objective=objective, loadsignal=1, dalpha=1e-3, dbeta=1e-3, load2_node=node,
+              load2_phase=phase)
+    x = 0.3 + 0.02 * (2 * rng.random(np.prod(n)) - 1)
+    le = _le(n, nlvls=2, mixed=mixed, rtol=1e-12, sens_fp32=False, **kw)
+    fx, df = _run_gpu(le, x)
+    ref = O.LinearElasticity(*n, **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert rc == 0
+    assert abs(fx - fx_r) <= 1e-9 * abs(fx_r)
+    assert _rel(df, df_r) < 1e-8
+
+
 def test_reference_pulse_and_defaults(gpu):
     # reference defaults: Emax 1e3, Rmax 4.1667e-4, reference load pulse, dt = 0.4
     n = (8, 4, 4)

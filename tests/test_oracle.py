@@ -141,10 +141,14 @@ def test_mma_converges_on_separable_problem():
     np.testing.assert_allclose(x, np.clip(c - lam / (2 * n), 0, 1), atol=2e-3)
 
 
-@pytest.mark.parametrize("objective", range(7))
+@pytest.mark.parametrize("objective", range(8))
 def test_adjoint_sensitivities_match_finite_differences(objective):
+    # objective 7 (output-DOF displacement) and the second point load are the
+    # extended workloads' additions; the second load rides along on objective 7
     kw = dict(ncp=2, tsc=4, t1=0.8, objective=objective, loadsignal=1, dalpha=0.01, dbeta=0.01,
               mInt=1 if objective == 4 else 0)
+    if objective == 7:
+        kw.update(load2_node=7, load2_phase=0.7)
     le = O.LinearElasticity(4, 2, 2, **kw)
     rng = np.random.default_rng(objective)
     x = 0.3 + 0.4 * rng.random(le.nel)

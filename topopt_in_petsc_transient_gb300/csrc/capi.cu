@@ -108,6 +108,9 @@ void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz) {
     p->reduction = 0;
     p->basis = 5;
     p->omega0 = 1.0;
+    p->load2_node = -1;
+    p->load2_phase = 0.0;
+    p->out_dof = -1;
 }
 
 int topo_le_create(topo_le **out, const topo_le_params *p) {

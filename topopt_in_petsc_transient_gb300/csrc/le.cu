@@ -320,6 +320,7 @@ struct TopoLE {
     // SOMMG reduced path (reduction = 1): basis Q [kb][ndof]; reduced
     // matrices Kr, Mr, Kp, Mp, Gc, Ut [kb*kb each], Pr [kb], fx; reduced
     // history [Ts][3][kb]; accumulators S [4][kb*kb]; Phi [4][kb][ndof]
+    long long out_dof = -1;    // objective 7 output DOF
     int kb = 0;
     bool fp64_solves = false;  // the SOMMG basis solves run the FP64 FCG in either mode
     double *Q = nullptr, *red = nullptr, *rhist = nullptr, *Sacc = nullptr, *Phi = nullptr, *mdpart = nullptr;
@@ -399,8 +400,13 @@ int le_create(TopoLE **out, const LEParams *pp) {
     *out = nullptr;
     const LEParams &p = *pp;
     if (p.nx < 2 || p.ny < 2 || p.nz < 2 || p.ncp < 1 || p.tsc < 1 || p.nlvls < 1 || p.hx <= 0 || p.hy <= 0 ||
-        p.hz <= 0 || p.t1 <= 0 || p.objective < 0 || p.objective > 6) {
+        p.hz <= 0 || p.t1 <= 0 || p.objective < 0 || p.objective > 7 ||
+        p.load2_node >= (long long)p.nx * p.ny * p.nz || p.out_dof >= 3LL * p.nx * p.ny * p.nz) {
         set_error("invalid LinearElasticity parameters");
+        return TOPO_ERR_ARG;
+    }
+    if (p.reduction && (p.objective == 7 || p.load2_node >= 0)) {
+        set_error("the SOMMG reduction does not take the output-DOF objective or the second point load");
         return TOPO_ERR_ARG;
     }
     if (p.reduction && (p.basis < 1 || p.basis > KB_MAX || !(p.omega0 > 0.0))) {
@@ -422,6 +428,8 @@ int le_create(TopoLE **out, const LEParams *pp) {
     le->ndof = 3 * le->nn;
     // constructor, LinearElasticity.cc:93-97; SetUpTimeIntegration :185-219
     le->Ts = p.ncp * p.tsc + 1;
+    le->out_dof = p.out_dof >= 0 ? p.out_dof
+                                 : 3 * ((p.nx - 1) + (long long)p.nx * ((p.ny - 1) / 2 + (long long)p.ny * ((p.nz - 1) / 2))) + 2;
     le->dt = p.t1 / (le->Ts - 1);
     double dt = le->dt;
     if (p.ti == 0) {
@@ -1206,6 +1214,8 @@ static void fwd_rhs_t(TopoLE *le) {
     pr.rhs0 = le->rhs0;
     pr.load_scale = 1.0 / (p.ny - 1);
     pr.loadsignal = p.loadsignal;
+    pr.load2_dof = p.load2_node >= 0 ? 3LL * p.load2_node + 2 : -1;
+    pr.load2_phase = p.load2_phase;
     // B1 u- + B2 du- + B3 ddu- = M (cM . s-) + K (cK . s-)  (LinearElasticity.cc:1028-1044)
     pr.cM[0] = a[5] + a[2] * p.dalpha;
     pr.cM[1] = a[3] - a[0] * p.dalpha;
@@ -1288,7 +1298,7 @@ __global__ void k_select_state(long long ndof, const StepCtx *st, const double *
 
 static void objective_products(TopoLE *le, int t0mode) {
     int obj = le->p.objective;
-    if (obj < 3) return;
+    if (obj < 3 || obj == 7) return;
     double dt = le->dt;
     // stage the needed state vectors into the solver scratch (sp, sq are free here)
     bool needU = (obj == 3 || obj == 5), needDU = (obj >= 4);
@@ -1327,6 +1337,8 @@ static AdjCombine adj_args(TopoLE *le, int t0mode) {
     A.cp = le->cp;
     A.ndof = le->ndof;
     A.objective = p.objective;
+    A.out_dof = le->out_dof;
+    A.fx = &le->st->fx;
     A.t0mode = t0mode;
     A.dt = le->dt;
     memcpy(A.a, a, sizeof(A.a));
@@ -1425,6 +1437,7 @@ static void launch_sens(TopoLE *le, int t0mode) {
     case 3: launch_sens_obj<3>(le, S); break;
     case 4: launch_sens_obj<4>(le, S); break;
     case 5: launch_sens_obj<5>(le, S); break;
+    case 7: launch_sens_obj<7>(le, S); break;
     default: launch_sens_obj<6>(le, S); break;
     }
 }
@@ -1525,13 +1538,13 @@ static int check_err(TopoLE *le) {
     return TOPO_OK;
 }
 
-__global__ void k_init_accel_rhs(long long nn, const uint8_t *fixed, const double *rhs0, double s, const double *Ku,
-                                 const double *Cdu, double *b) {
+__global__ void k_init_accel_rhs(long long nn, const uint8_t *fixed, const double *rhs0, double s, long long load2_dof,
+                                 double s2, const double *Ku, const double *Cdu, double *b) {
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
         uint8_t f = fixed[n];
         for (int c = 0; c < 3; c++) {
             long long i = 3 * n + c;
-            b[i] = ((f >> c) & 1) ? 0.0 : (rhs0[i] * s - Cdu[i] - Ku[i]);
+            b[i] = ((f >> c) & 1) ? 0.0 : (rhs0[i] * s + (i == load2_dof ? s2 : 0.0) - Cdu[i] - Ku[i]);
         }
     }
 }
@@ -1805,7 +1818,11 @@ int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, 
         s0 /= (p.ny - 1);
     }
     count_launch();
-    k_init_accel_rhs<<<ew_blocks(le->nn), EW, 0, s>>>(le->nn, le->L[0].fixed, le->rhs0, s0, le->KL, le->ML, le->sb);
+    // second point load at t = 0 (workload extension)
+    const long long l2 = p.load2_node >= 0 ? 3LL * p.load2_node + 2 : -1;
+    const double s2 = l2 >= 0 ? sin(p.load2_phase) / (p.ny - 1) : 0.0;
+    k_init_accel_rhs<<<ew_blocks(le->nn), EW, 0, s>>>(le->nn, le->L[0].fixed, le->rhs0, s0, l2, s2, le->KL, le->ML,
+                                                      le->sb);
     CK(cudaMemsetAsync(le->sx, 0, sizeof(double) * nd, s));
     rc = solve(le, 1, le->sb, false);
     if (rc) return rc;

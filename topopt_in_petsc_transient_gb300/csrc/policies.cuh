@@ -468,6 +468,11 @@ struct StepCtx {   // device-resident time-stepping state
     double fx;     // objective accumulator
 };
 
+// second point load of the extended workloads: sin(2 pi t + phase) for t < 0.5
+__device__ __forceinline__ double load2_signal(double phase, double t) {
+    return (t < 0.5) ? sin(2.0 * 3.14159265358979323846 * t + phase) : 0.0;
+}
+
 __device__ __forceinline__ double load_signal(int which, double t) {
     if (which == 1) return (t < 0.5) ? sin(2.0 * 3.14159265358979323846 * t) : 0.0;
     // LinearElasticity.cc:597-606
@@ -488,6 +493,8 @@ struct PolRhsFwd {
     const double *rhs0;                 // RHSLocation (LoadLocation, LinearElasticity.cc:616-675)
     double load_scale;                  // 1/(ny-1)
     int loadsignal;
+    long long load2_dof;                // z DOF of the second point load (-1: none)
+    double load2_phase;
     double cK[3], cM[3];                // combination coefficients of (u-, du-, ddu-)
     double pred[3];                     // predictor coefficients (u-, du-, ddu-)
     double pred2[2];                    // with an older acceleration ddu--: (ddu-, ddu--)
@@ -535,7 +542,8 @@ struct PolRhsFwd {
         uint8_t f = fixed[n];
         for (int c = 0; c < 3; c++) {
             bool fx = (f >> c) & 1;
-            b[3 * n + c] = fx ? 0.0 : (rhs0[3 * n + c] * s + todbl(y[c]));
+            const double f2 = (3 * n + c == load2_dof) ? load2_signal(load2_phase, t * st->dt) * load_scale : 0.0;
+            b[3 * n + c] = fx ? 0.0 : (rhs0[3 * n + c] * s + f2 + todbl(y[c]));
             double xv = pred[0] * u[3 * n + c] + pred[1] * du[3 * n + c];
             if (ddu2)
                 xv += pred2[0] * ddu[3 * n + c] + pred2[1] * ddu2[3 * n + c];

@@ -28,6 +28,8 @@ struct AdjCombine {
     const double *cp;             // checkpoints (for j < 0: t = 0 state)
     long long ndof;
     int objective;
+    long long out_dof;            // objective 7: the output DOF
+    double *fx;                   // objective accumulator (objective 7 adds its value here)
     int t0mode;                   // 1: SolveLagrange0 right-hand side R3
     double dt;
     double a[6];
@@ -66,6 +68,12 @@ static __global__ void k_adj_combine(AdjCombine A) {
             case 5:
                 hu = A.hK[i];
                 hdu = A.hM[i];
+                break;
+            case 7:  // extension: dt/2 u_out^2, gradient dt u_out at the output DOF
+                if (i == A.out_dof) {
+                    hu = A.dt * u[i];
+                    *A.fx += 0.5 * A.dt * u[i] * u[i];  // the one thread of this DOF
+                }
                 break;
             default: hdu = A.hK[i]; break;
             }
@@ -309,7 +317,9 @@ static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const Elem
         double t3 = dkfe * (double)sK + dmfe * (double)sM;
         // objective value h0 and its explicit density derivative dfx0
         double h0 = 0.0, dfx0 = 0.0;
-        if (OBJ == 0 || OBJ == 1 || OBJ == 2) {
+        if (OBJ == 7) {
+            // the output-DOF objective has no element part (k_adj_combine adds it)
+        } else if (OBJ == 0 || OBJ == 1 || OBJ == 2) {
             if (A.with_objective) {
                 const double *s = (OBJ == 0) ? u : (OBJ == 1 ? du : ddu);
                 double acc = 0.0;

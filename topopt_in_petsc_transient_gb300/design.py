@@ -70,6 +70,11 @@ class TopOpt:
     reduction: bool = False  # TopOpt.cc:157-159
     basis: int = 5
     omega0: float = 1.0
+    load2_node: int = -1  # workload extensions (second point load, objective 7 output DOF)
+    load2_phase: float = 0.0
+    out_dof: int = -1
+    noise: float = 0.0  # initial design V0 + U(-noise, noise) from a generator seeded with seed
+    seed: int = 0x7A11
     mass_precond_smooth: int = 0
     # state
     fscale: float = 1.0
@@ -98,9 +103,13 @@ class TopOpt:
         n = self.nel
         f64 = dict(dtype=torch.float64, device=device)
         self.x = torch.full((n,), V0, **f64)
+        if self.noise > 0.0:
+            import numpy as np
+            rng = np.random.default_rng(self.seed)
+            self.x += torch.tensor(rng.uniform(-self.noise, self.noise, n), **f64)
         self.xTilde = torch.full((n,), V0, **f64)
         self.xPhys = torch.full((n,), V0, **f64)
-        self.xold = torch.full((n,), V0, **f64)
+        self.xold = self.x.clone()
         self.dfdx = torch.zeros(n, **f64)
         self.dgdx = torch.zeros(self.m * n, **f64)
         self.xmin = torch.zeros(n, **f64)
@@ -115,7 +124,7 @@ class TopOpt:
             inner_tol=self.inner_tol, inner_maxit=self.inner_maxit, adaptive_kappa=self.adaptive_kappa,
             extrapolate=self.extrapolate, mass_precond=self.mass_precond,
             mass_precond_smooth=self.mass_precond_smooth, reduction=self.reduction, basis=self.basis,
-            omega0=self.omega0)
+            omega0=self.omega0, load2_node=self.load2_node, load2_phase=self.load2_phase, out_dof=self.out_dof)
         self.filt = Filter(self.nelx, self.nely, self.nelz, self.filter, self.rmin, h=self.h, rtol=self.filter_rtol)
         self.mma = MMA(n, self.m, self.x)
         self.mma.SetAsymptotes(0.1, 0.6, 1.05)  # main.cc:58
