@@ -321,6 +321,11 @@ struct TopoLE {
     // matrices Kr, Mr, Kp, Mp, Gc, Ut [kb*kb each], Pr [kb], fx; reduced
     // history [Ts][3][kb]; accumulators S [4][kb*kb]; Phi [4][kb][ndof]
     long long out_dof = -1;    // objective 7 output DOF
+    // K, M products of the two previous adjoint iterates (initial residual of
+    // the adjoint solves without an operator pass); ax0_pending: the next
+    // solve takes (N A N + I - N) x0 from ax0 (= sq)
+    double *KLh1 = nullptr, *MLh1 = nullptr, *KLh2 = nullptr, *MLh2 = nullptr;
+    bool ax0_pending = false;
     int kb = 0;
     bool fp64_solves = false;  // the SOMMG basis solves run the FP64 FCG in either mode
     double *Q = nullptr, *red = nullptr, *rhist = nullptr, *Sacc = nullptr, *Phi = nullptr, *mdpart = nullptr;
@@ -387,6 +392,12 @@ template <>
 Weights<df> fine_weights<df>(TopoLE *le, bool hk, bool hm, const double *P, double sK, double sM) {
     return Weights<df>{hk ? le->kfx : nullptr, hm ? le->mfx : nullptr, P, df(sK), df(sM)};
 }
+template <>
+Weights<float> fine_weights<float>(TopoLE *le, bool hk, bool hm, const double *P, double sK, double sM) {
+    return Weights<float>{hk ? le->L[0].kff : nullptr, hm ? le->L[0].mff : nullptr, P, (float)sK, (float)sM};
+}
+template <>
+const ElemConst<float> &fine_const<float>(TopoLE *le) { return le->L[0].Cf; }
 template <>
 const ElemConst<double> &fine_const<double>(TopoLE *le) { return le->L[0].Cd; }
 template <>
@@ -476,6 +487,12 @@ int le_alloc(TopoLE *le) {
     AG(le->DDLp1, nd);
     AG(le->Lp2, nd);
     AG(le->Lp3, nd);
+    if (!p.reduction) {
+        AG(le->KLh1, nd);
+        AG(le->MLh1, nd);
+        AG(le->KLh2, nd);
+        AG(le->MLh2, nd);
+    }
     AG(le->DLc, nd);
     AG(le->DDLc, nd);
     AG(le->KL, nd);
@@ -1057,6 +1074,13 @@ static void solve_init_t(TopoLE *le, int o, const double *b, cudaGraphConditiona
 }
 static void solve_init(TopoLE *le, int o, const double *b, cudaGraphConditionalHandle cond, int has_cond) {
     cur_b(le) = b;
+    if (le->ax0_pending) {  // the caller formed (N A N + I - N) x0 in sq
+        le->ax0_pending = false;
+        count_launch();
+        k_init_pointwise<<<red_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, b, le->sq, le->sr, le->S,
+                                                                       mixed_fcg(le) ? 1 : 0, cond, has_cond, P2(le));
+        return;
+    }
     if (mixed_fcg(le))
         solve_init_t<df>(le, o, b, cond, has_cond);
     else
@@ -1353,6 +1377,15 @@ static AdjCombine adj_args(TopoLE *le, int t0mode) {
     A.DDL = le->DDLc;
     A.b = le->sb;
     A.x0 = le->sx;
+    if (le->KLh1) {
+        A.ax0 = le->sq;
+        A.KLh1 = le->KLh1;
+        A.MLh1 = le->MLh1;
+        A.KLh2 = le->KLh2;
+        A.MLh2 = le->MLh2;
+        A.sK = t0mode ? le->ops[1].sK : le->ops[0].sK;
+        A.sM = t0mode ? le->ops[1].sM : le->ops[0].sM;
+    }
     return A;
 }
 
@@ -1442,20 +1475,33 @@ static void launch_sens(TopoLE *le, int t0mode) {
     }
 }
 
+// K L+: its part in the B terms and in A x0 is scaled by the stiffness share
+// of the operator, so when that share is tiny an FP32 product is accurate to
+// well below the solver tolerance (share 1e-4: FP32 rounding 6e-8 x 1e-4)
+static void adj_kl(TopoLE *le) {
+    if (le->p.mixed && le->ops[0].share <= 1e-4)
+        product_t<float, true, false>(le, le->Lp1, le->KL, nullptr, 1.0, 0.0);
+    else
+        product<true, false>(le, le->Lp1, le->KL, nullptr, 1.0, 0.0);
+}
+
 static int adj_step(TopoLE *le, bool capturing) {
     cudaStream_t s = le->stream;
     // K L+ and M L+ (the B1..B3 products of LinearElasticity.cc:897-899)
-    product<true, false>(le, le->Lp1, le->KL, nullptr, 1.0, 0.0);
+    adj_kl(le);
     product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
     objective_products(le, 0);
     count_launch();
     k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 0));
+    le->ax0_pending = le->KLh1 != nullptr;
     int rc = solve(le, 0, le->sb, capturing);
+    le->ax0_pending = false;
     if (rc) return rc;
     launch_sens(le, 0);
     count_launch();
     k_adj_advance<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->DLc, le->DDLc, le->Lp1, le->DLp1, le->DDLp1,
-                                                      le->Lp2, le->Lp3);
+                                                      le->Lp2, le->Lp3,
+                                                      KMHist{le->KL, le->ML, le->KLh1, le->MLh1, le->KLh2, le->MLh2});
     count_launch();
     k_step_add<<<1, 1, 0, s>>>(le->st, -1);
     return TOPO_OK;
@@ -1463,12 +1509,14 @@ static int adj_step(TopoLE *le, bool capturing) {
 
 static int lagrange0(TopoLE *le) {
     cudaStream_t s = le->stream;
-    product<true, false>(le, le->Lp1, le->KL, nullptr, 1.0, 0.0);
+    adj_kl(le);
     product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
     objective_products(le, 1);
     count_launch();
     k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 1));
+    le->ax0_pending = le->KLh1 != nullptr;
     int rc = solve(le, 1, le->sb, false);
+    le->ax0_pending = false;
     if (rc) return rc;
     launch_sens(le, 1);
     count_launch();

@@ -53,6 +53,28 @@ struct Weights {
     }
 };
 
+// solver state after the initial residual (t[0] = b.b, t[1] = r.r)
+__device__ __forceinline__ void init_finish(SolveScalars *S, const double t[2], bool has_r32,
+                                            cudaGraphConditionalHandle cond, int has_cond) {
+    S->bb = t[0];
+    S->rr = t[1];
+    S->it = 0;
+    S->status = 0;
+    S->zero_x = (t[0] == 0.0);
+    S->done = (t[0] == 0.0) || (t[1] <= S->tol2 * t[0]);
+    S->need_replace = 0;
+    S->restart = 1;
+    S->inner_it = 0;
+    S->sigma = (t[1] > 0.0) ? sqrt(S->ndof / t[1]) : 1.0;
+    S->rr_ref = t[1] * S->sigma * S->sigma;
+    S->rescale = has_r32;
+    if (!isfinite(t[1])) {
+        S->status = TOPO_ERR_NAN;
+        S->done = 1;
+    }
+    if (has_cond) cudaGraphSetConditional(cond, S->done ? 0u : 1u);
+}
+
 // ---------------------------------------------------------------------------
 // FCG initial residual: r = b - (N A N + I - N) x0, reductions b.b and r.r
 // ---------------------------------------------------------------------------
@@ -87,25 +109,7 @@ struct PolInitResid {
             red[1] += rv * rv;
         }
     }
-    __device__ void finish(const double t[2]) const {
-        S->bb = t[0];
-        S->rr = t[1];
-        S->it = 0;
-        S->status = 0;
-        S->zero_x = (t[0] == 0.0);
-        S->done = (t[0] == 0.0) || (t[1] <= S->tol2 * t[0]);
-        S->need_replace = 0;
-        S->restart = 1;
-        S->inner_it = 0;
-        S->sigma = (t[1] > 0.0) ? sqrt(S->ndof / t[1]) : 1.0;
-        S->rr_ref = t[1] * S->sigma * S->sigma;
-        S->rescale = (r32 != nullptr);
-        if (!isfinite(t[1])) {
-            S->status = TOPO_ERR_NAN;
-            S->done = 1;
-        }
-        if (has_cond) cudaGraphSetConditional(cond, S->done ? 0u : 1u);
-    }
+    __device__ void finish(const double t[2]) const { init_finish(S, t, r32 != nullptr, cond, has_cond); }
 };
 
 // ---------------------------------------------------------------------------

@@ -36,6 +36,14 @@ struct AdjCombine {
     double cM[3], cK[3];          // B1..B3 coefficients
     const StepCtx *st;
     double *DL, *DDL, *b, *x0;
+    // optional: the masked operator applied to the initial guess,
+    // (N A N + I - N) x0, from the K and M products of the last adjoint
+    // iterates (KL, ML = K L+, M L+; KLh1, MLh1 = K L++, M L++; KLh2, MLh2 =
+    // K L+++, M L+++), so that the solve needs no operator pass for its
+    // initial residual
+    double *ax0;
+    const double *KLh1, *MLh1, *KLh2, *MLh2;
+    double sK, sM;  // A = sK K + sM M
 };
 
 static __global__ void k_adj_combine(AdjCombine A) {
@@ -87,7 +95,8 @@ static __global__ void k_adj_combine(AdjCombine A) {
                 // SolveLagrange0 R3 (LinearElasticity.cc:753-758)
                 double r3 = -(hddu + B3 - a[1] * dlp + a[4] * ddlp);
                 A.b[i] = fx ? 0.0 : r3;
-                A.x0[i] = fx ? 0.0 : 0.0;
+                A.x0[i] = 0.0;
+                if (A.ax0) A.ax0[i] = 0.0;
             } else {
                 double DL = -(hdu + B2 - a[0] * dlp + a[3] * ddlp);
                 double DDL = -(hddu + B3 + a[4] * ddlp);
@@ -97,12 +106,32 @@ static __global__ void k_adj_combine(AdjCombine A) {
                 // the reference solves (N A N + I - N) L = R1 with A = -Keff
                 // (LinearElasticity.cc:1022-1026, :924): Keff L = -R1 on free DOFs
                 A.b[i] = fx ? 0.0 : -R1;
-                double g = A.Lp1[i];
-                if (A.extrapolate >= 2 && nadj >= 3)
-                    g = 3.0 * (A.Lp1[i] - A.Lp2[i]) + A.Lp3[i];
-                else if (A.extrapolate >= 1 && nadj >= 2)
-                    g = 2.0 * A.Lp1[i] - A.Lp2[i];
+                // x0 = w1 L+ + w2 L++ + w3 L+++
+                double w1 = 1.0, w2 = 0.0, w3 = 0.0;
+                if (A.extrapolate >= 2 && nadj >= 3) {
+                    w1 = 3.0;
+                    w2 = -3.0;
+                    w3 = 1.0;
+                } else if (A.extrapolate >= 1 && nadj >= 2) {
+                    w1 = 2.0;
+                    w2 = -1.0;
+                }
+                double g = w1 * A.Lp1[i];
+                if (w2 != 0.0) g += w2 * A.Lp2[i];
+                if (w3 != 0.0) g += w3 * A.Lp3[i];
                 A.x0[i] = fx ? 0.0 : g;
+                if (A.ax0) {
+                    double kx = w1 * A.KL[i], mx = w1 * A.ML[i];
+                    if (w2 != 0.0) {
+                        kx += w2 * A.KLh1[i];
+                        mx += w2 * A.MLh1[i];
+                    }
+                    if (w3 != 0.0) {
+                        kx += w3 * A.KLh2[i];
+                        mx += w3 * A.MLh2[i];
+                    }
+                    A.ax0[i] = fx ? 0.0 : A.sK * kx + A.sM * mx;
+                }
             }
         }
     }
@@ -126,16 +155,43 @@ static __global__ void k_count_region(GridDesc g, const double *__restrict__ P, 
 // after the adjoint solve of step j: L+++ <- L++, L++ <- L+, L+ <- lambda_j,
 // DL+ <- DL_j, DDL+ <- DDL_j (k_adj_combine uses the older lambdas only once
 // the sweep has produced them)
+struct KMHist {
+    const double *KL, *ML;
+    double *KLh1, *MLh1, *KLh2, *MLh2;  // null: not kept
+};
 static __global__ void k_adj_advance(long long ndof, const double *__restrict__ lam, const double *__restrict__ DL,
                               const double *__restrict__ DDL, double *Lp1, double *DLp1, double *DDLp1, double *Lp2,
-                              double *Lp3) {
+                              double *Lp3, KMHist H) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        if (H.KLh1) {  // K, M products follow their lambdas: K L++ <- K L+, ...
+            H.KLh2[i] = H.KLh1[i];
+            H.MLh2[i] = H.MLh1[i];
+            H.KLh1[i] = H.KL[i];
+            H.MLh1[i] = H.ML[i];
+        }
         Lp3[i] = Lp2[i];
         Lp2[i] = Lp1[i];
         Lp1[i] = lam[i];
         DLp1[i] = DL[i];
         DDLp1[i] = DDL[i];
     }
+}
+
+// FCG initial residual from a precomputed (N A N + I - N) x0:
+// r = b - ax0, reductions b.b and r.r, then the same solver-state set-up as
+// the operator-pass initial residual (PolInitResid)
+static __global__ void k_init_pointwise(long long ndof, const double *__restrict__ b, const double *__restrict__ ax0,
+                                        double *r, SolveScalars *S, int has_r32, cudaGraphConditionalHandle cond,
+                                        int has_cond, Partials<2> part) {
+    double red[2] = {0.0, 0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        const double bv = b[i], rv = bv - ax0[i];
+        r[i] = rv;
+        red[0] += bv * bv;
+        red[1] += rv * rv;
+    }
+    double tot[2];
+    if (grid_reduce<EW, 2>(red, part, tot)) init_finish(S, tot, has_r32, cond, has_cond);
 }
 
 // ---------------------------------------------------------------------------
