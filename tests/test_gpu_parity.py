@@ -109,6 +109,31 @@ def test_mixed_default_fp32_sensitivities(gpu, nlvls, coarse_smooth):
     assert _rel(df, df_r) < 1e-5
 
 
+@pytest.mark.parametrize("ncp,tsc,uniform", [(1, 200, True), (2, 100, True), (2, 100, False)])
+def test_long_horizon_tracked_products(gpu, ncp, tsc, uniform):
+    # 200 steps, the load pulse ending at step 100: the mixed forward sweep
+    # forms its right-hand sides from tracked products A u, A du, A ddu
+    # (re-formed at block starts and every 32 steps); smooth free vibration
+    # lets the predictor reach the solve tolerance, so solves that stop at
+    # their initial guess are exercised too.  Default tolerance rtol 1e-10:
+    # objective within 1e-7 of the oracle, displacement and velocity of the
+    # resident block within 1e-6 (the acceleration carries the alternating
+    # high-frequency part of the solve error and is not compared).
+    n = (16, 8, 8)
+    kw = dict(ncp=ncp, tsc=tsc, t1=0.005 * ncp * tsc, objective=3, loadsignal=1, dalpha=0.0, dbeta=1e-3)
+    rng = np.random.default_rng(5)
+    x = np.full(np.prod(n), 0.12) if uniform else 0.1 + 0.2 * rng.random(np.prod(n))
+    le = _le(n, nlvls=3, mixed=True, rtol=1e-10, sens_fp32=False, **kw)
+    fx, df = _run_gpu(le, x)
+    ref = O.LinearElasticity(*n, **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert abs(fx - fx_r) <= 1e-7 * abs(fx_r)
+    assert _rel(df, df_r) < 1e-6
+    U, DU, DDU = ref.last_block_state(tsc - 1)
+    assert _rel(le.state(0, tsc - 1), U) < 1e-6
+    assert _rel(le.state(1, tsc - 1), DU) < 1e-6
+
+
 @pytest.mark.parametrize("objective", range(7))
 def test_fp32_sensitivities_every_objective(gpu, objective):
     # FP32 element math of the sensitivity kernel for every objective, on the

@@ -508,6 +508,24 @@ static __global__ void k_newmark(long long ndof, const double *__restrict__ x, c
     }
 }
 
+// after a forward solve: the tracked products of the new state,
+// A u = b - r (the solve's final residual), A du and A ddu by the Newmark
+// corrector applied to the tracked products; A ddu of the previous state
+// moves to AAp (free rows; clamped rows hold 0)
+static __global__ void k_track_products(long long ndof, const double *__restrict__ b, const double *__restrict__ r,
+                                        const SolveScalars *S, double *AU, double *AV, double *AA, double *AAp,
+                                        Newmark nm) {
+    const bool zx = S->zero_x != 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        const double aun = zx ? 0.0 : b[i] - r[i], d = aun - AU[i];
+        const double av = AV[i], aa = AA[i];
+        AAp[i] = aa;
+        AU[i] = aun;
+        AV[i] = nm.a[0] * av + nm.a[1] * aa + nm.a[2] * d;
+        AA[i] = -nm.a[3] * av - nm.a[4] * aa + nm.a[5] * d;
+    }
+}
+
 static __global__ void k_step_set(StepCtx *st, int block, int j) {
     st->block = block;
     st->j = j;

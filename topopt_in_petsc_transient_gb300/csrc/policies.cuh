@@ -55,13 +55,13 @@ struct Weights {
 
 // solver state after the initial residual (t[0] = b.b, t[1] = r.r)
 __device__ __forceinline__ void init_finish(SolveScalars *S, const double t[2], bool has_r32,
-                                            cudaGraphConditionalHandle cond, int has_cond) {
+                                            cudaGraphConditionalHandle cond, int has_cond, bool accept_x0 = true) {
     S->bb = t[0];
     S->rr = t[1];
     S->it = 0;
     S->status = 0;
     S->zero_x = (t[0] == 0.0);
-    S->done = (t[0] == 0.0) || (t[1] <= S->tol2 * t[0]);
+    S->done = (t[0] == 0.0) || (accept_x0 && t[1] <= S->tol2 * t[0]);
     S->need_replace = 0;
     S->restart = 1;
     S->inner_it = 0;
@@ -456,12 +456,7 @@ struct PolProduct {
 };
 
 // ---------------------------------------------------------------------------
-// Newmark right-hand side of one forward step (SolveStateBlock,
-// LinearElasticity.cc:1330-1356):
-//   b = N (f(t) + B1 u- + B2 du- + B3 ddu-),  B_i = N (cMi M + cKi K) N
-// staged as vK = sum cKi (u-,du-,ddu-)_i and vM = sum cMi (...)_i so that one
-// element pass gives K vK + M vM.  Also writes the Newmark predictor
-// u- + dt du- + (1/2 - beta) dt^2 ddu- as the Krylov initial guess.
+// forward time stepping (SolveStateBlock, LinearElasticity.cc:1317-1385)
 // ---------------------------------------------------------------------------
 struct StepCtx {   // device-resident time-stepping state
     int block;     // checkpoint block c
@@ -485,6 +480,13 @@ __device__ __forceinline__ double load_signal(int which, double t) {
     return exp(-(s * s) / ((2 * c) * (2 * c))) * cos(4.0 * s) * cos(5.0 * s) * cos(6.0 * s) * cos(7.0 * s);
 }
 
+// ---------------------------------------------------------------------------
+// Newmark right-hand side of one forward step (plain FP64 path):
+//   b = N (f(t) + B1 u- + B2 du- + B3 ddu-),  B_i = N (cMi M + cKi K) N
+// staged as vK = sum cKi (u-,du-,ddu-)_i and vM = sum cMi (...)_i so that one
+// element pass gives K vK + M vM.  Also writes the initial guess x0 (the
+// Newmark predictor, see PolRhsInit).
+// ---------------------------------------------------------------------------
 template <class T>
 struct PolRhsFwd {
     static constexpr int NIN = 2, NRED = 0;
@@ -557,6 +559,110 @@ struct PolRhsFwd {
         }
     }
     __device__ void finish(const double *) const {}
+};
+
+// ---------------------------------------------------------------------------
+// Forward step right-hand side and initial residual in one K-only pass.
+// With A = sK K + sM M the step operator and the tracked products
+// AS_i = A s_i of the previous state s = (u-, du-, ddu-) (exact: A u = b - r
+// of the previous solve, and A du, A ddu follow the Newmark corrector, which
+// is linear), M s_i = (AS_i - sK K s_i) / sM and
+//   b = f + sum_i B_i s_i = f + sum_i (cM_i / sM) AS_i + K (sum_i c'_i s_i),
+//   c'_i = cK_i - cM_i sK / sM
+// (SolveStateBlock, LinearElasticity.cc:1317-1361); the initial guess x0 is the
+// predictor and A x0 the same combination of the tracked products, so
+// r0 = b - A x0 needs no operator pass.  The pass also forms b.b and r.r and
+// sets up the FCG state.  Initial guess: the Newmark predictor
+// u- + dt du- + (1/2 - beta) dt^2 ddu- (pred), or with the acceleration
+// extrapolated linearly from ddu- and ddu-- (use_pred2, pred2).
+// ---------------------------------------------------------------------------
+template <class T>
+struct PolRhsInit {
+    static constexpr int NIN = 1, NRED = 2;
+    static constexpr bool HAS_K = true, HAS_M = false;
+    const uint8_t *fixed;
+    Weights<T> w;                       // kf, sK = 1
+    const double *cp, *Uh, *DUh, *DDUh;
+    long long ndof;
+    const double *rhs0;
+    double load_scale;
+    int loadsignal;
+    long long load2_dof;
+    double load2_phase;
+    double ck[3];                       // c'_i
+    double cA[3];                       // cM_i / sM
+    double pred[3], pred2[2];
+    int use_pred2;
+    const double *AU, *AV, *AA, *AAp;   // A u-, A du-, A ddu-, A ddu-- (free rows)
+    const StepCtx *st;
+    double *b, *x0, *r;
+    SolveScalars *S;
+    cudaGraphConditionalHandle cond;
+    int has_cond;
+    Partials<2> part;
+    __device__ __forceinline__ void prev(const double *&u, const double *&du, const double *&ddu) const {
+        int j = st->j;
+        if (j == 0) {
+            const double *base = cp + (long long)st->block * 3 * ndof;
+            u = base;
+            du = base + ndof;
+            ddu = base + 2 * ndof;
+        } else {
+            u = Uh + (long long)(j - 1) * ndof;
+            du = DUh + (long long)(j - 1) * ndof;
+            ddu = DDUh + (long long)(j - 1) * ndof;
+        }
+    }
+    __device__ void load(long long n, T v[1][3]) const {
+        const double *u, *du, *ddu;
+        prev(u, du, ddu);
+        for (int c = 0; c < 3; c++) {
+            const long long i = 3 * n + c;
+            v[0][c] = T(ck[0] * u[i] + ck[1] * du[i] + ck[2] * ddu[i]);
+        }
+        mask3(fixed[n], v[0]);
+    }
+    __device__ void coef(long long e, T &kc, T &mc) const { w.get(e, kc, mc); }
+    __device__ void epilogue(long long n, int, int, int, const T y[3], double red[2]) const {
+        const double *u, *du, *ddu;
+        prev(u, du, ddu);
+        const double *ddu2 = nullptr;
+        if (use_pred2 && st->j >= 2)
+            ddu2 = DDUh + (long long)(st->j - 2) * ndof;
+        else if (use_pred2 && st->j == 1)
+            ddu2 = cp + (long long)st->block * 3 * ndof + 2 * ndof;
+        const int t = st->tsc * st->block + st->j + 1;
+        const double s = load_signal(loadsignal, t * st->dt) * load_scale;
+        const uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) {
+            const long long i = 3 * n + c;
+            if ((f >> c) & 1) {
+                b[i] = 0.0;
+                x0[i] = 0.0;
+                r[i] = 0.0;
+                continue;
+            }
+            const double f2 = (i == load2_dof) ? load2_signal(load2_phase, t * st->dt) * load_scale : 0.0;
+            const double bv = rhs0[i] * s + f2 + cA[0] * AU[i] + cA[1] * AV[i] + cA[2] * AA[i] + todbl(y[c]);
+            double xv = pred[0] * u[i] + pred[1] * du[i], ax = pred[0] * AU[i] + pred[1] * AV[i];
+            if (ddu2) {
+                xv += pred2[0] * ddu[i] + pred2[1] * ddu2[i];
+                ax += pred2[0] * AA[i] + pred2[1] * AAp[i];
+            } else {
+                xv += pred[2] * ddu[i];
+                ax += pred[2] * AA[i];
+            }
+            const double rv = bv - ax;
+            b[i] = bv;
+            x0[i] = xv;
+            r[i] = rv;
+            red[0] += bv * bv;
+            red[1] += rv * rv;
+        }
+    }
+    // x0 is never accepted without a true residual: A u+ = b - r must hold
+    // for the stored u+, and r0 here rests on the tracked products
+    __device__ void finish(const double t[2]) const { init_finish(S, t, true, cond, has_cond, false); }
 };
 
 }  // namespace topo
