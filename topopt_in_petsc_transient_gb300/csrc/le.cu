@@ -1072,6 +1072,9 @@ __global__ void k_solve_check(const SolveScalars *S, int *err) {
 }
 
 static const double *&cur_b(TopoLE *le);
+// mixed path: tracked operator products (A u of the forward states, A lambda of
+// the adjoint iterates) in place of mass products
+static bool al_mode(const TopoLE *le) { return le->AUt != nullptr; }
 // mixed-precision FCG for this solve (FP64 FCG for the plain path and for
 // solves that set fp64_solves)
 static bool mixed_fcg(const TopoLE *le) { return le->p.mixed && !le->fp64_solves; }
@@ -1094,8 +1097,11 @@ static void solve_init(TopoLE *le, int o, const double *b, cudaGraphConditionalH
     if (le->ax0_pending) {  // the caller formed (N A N + I - N) x0 in sq
         le->ax0_pending = false;
         count_launch();
+        // AL mode: x0 is accepted only on a true residual, which keeps
+        // A lambda = b - r exact for the stored lambda
         k_init_pointwise<<<red_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, b, le->sq, le->sr, le->S,
-                                                                       mixed_fcg(le) ? 1 : 0, cond, has_cond, P2(le));
+                                                                       mixed_fcg(le) ? 1 : 0, al_mode(le) ? 0 : 1,
+                                                                       cond, has_cond, P2(le));
         return;
     }
     if (mixed_fcg(le))
@@ -1503,6 +1509,18 @@ static AdjCombine adj_args(TopoLE *le, int t0mode) {
         A.sK = t0mode ? le->ops[1].sK : le->ops[0].sK;
         A.sM = t0mode ? le->ops[1].sM : le->ops[0].sM;
     }
+    if (al_mode(le)) {
+        // the ML slots hold A L (A = sK K + sM M of the step operator):
+        // B_i L = cM_i M L + cK_i K L = (cM_i / sM) A L + (cK_i - cM_i sK / sM) K L,
+        // and (N A N + I - N) x0 = sum_w w A L directly
+        const double sK = le->ops[0].sK, sM = le->ops[0].sM;
+        for (int i = 0; i < 3; i++) {
+            A.cK[i] -= A.cM[i] * sK / sM;
+            A.cM[i] /= sM;
+        }
+        A.sK = 0.0;
+        A.sM = 1.0;
+    }
     return A;
 }
 
@@ -1606,7 +1624,7 @@ static int adj_step(TopoLE *le, bool capturing) {
     cudaStream_t s = le->stream;
     // K L+ and M L+ (the B1..B3 products of LinearElasticity.cc:897-899)
     adj_kl(le);
-    product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
+    if (!al_mode(le)) product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
     objective_products(le, 0);
     count_launch();
     k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 0));
@@ -1618,7 +1636,8 @@ static int adj_step(TopoLE *le, bool capturing) {
     count_launch();
     k_adj_advance<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->DLc, le->DDLc, le->Lp1, le->DLp1, le->DDLp1,
                                                       le->Lp2, le->Lp3,
-                                                      KMHist{le->KL, le->ML, le->KLh1, le->MLh1, le->KLh2, le->MLh2});
+                                                      KMHist{le->KL, le->ML, le->KLh1, le->MLh1, le->KLh2, le->MLh2,
+                                                             al_mode(le) ? le->sb : nullptr, le->sr, le->S});
     count_launch();
     k_step_add<<<1, 1, 0, s>>>(le->st, -1);
     return TOPO_OK;
@@ -1627,7 +1646,7 @@ static int adj_step(TopoLE *le, bool capturing) {
 static int lagrange0(TopoLE *le) {
     cudaStream_t s = le->stream;
     adj_kl(le);
-    product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
+    if (!al_mode(le)) product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
     objective_products(le, 1);
     count_launch();
     k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 1));
@@ -2041,6 +2060,7 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
     CK(cudaMemsetAsync(le->DDLp1, 0, sizeof(double) * nd, s));
     CK(cudaMemsetAsync(le->Lp2, 0, sizeof(double) * nd, s));
     CK(cudaMemsetAsync(le->Lp3, 0, sizeof(double) * nd, s));
+    if (al_mode(le)) CK(cudaMemsetAsync(le->ML, 0, sizeof(double) * nd, s));  // A L+ of L+ = 0
     CK(cudaMemsetAsync(&le->st->nadj, 0, sizeof(int), s));
     CK(cudaMemsetAsync(&le->st->fx, 0, sizeof(double), s));
     for (int c = le->p.ncp - 1; c >= 0; c--) {

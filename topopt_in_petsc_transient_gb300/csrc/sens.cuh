@@ -155,15 +155,26 @@ static __global__ void k_count_region(GridDesc g, const double *__restrict__ P, 
 // after the adjoint solve of step j: L+++ <- L++, L++ <- L+, L+ <- lambda_j,
 // DL+ <- DL_j, DDL+ <- DDL_j (k_adj_combine uses the older lambdas only once
 // the sweep has produced them)
+// Mixed path (AL set): the ML slots hold A L instead of M L (A = sK K + sM M,
+// the step operator).  A lambda_j = b - r of the solve just finished (its
+// final residual is FP64-accurate), so no mass product is formed; with x zeroed
+// by the solve (b = 0) A lambda_j = 0.
 struct KMHist {
-    const double *KL, *ML;
+    const double *KL;
+    double *ML;
     double *KLh1, *MLh1, *KLh2, *MLh2;  // null: not kept
+    const double *b, *r;                // AL mode: the adjoint solve's b and final r (else null)
+    const SolveScalars *S;
 };
 static __global__ void k_adj_advance(long long ndof, const double *__restrict__ lam, const double *__restrict__ DL,
                               const double *__restrict__ DDL, double *Lp1, double *DLp1, double *DDLp1, double *Lp2,
                               double *Lp3, KMHist H) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
-        if (H.KLh1) {  // K, M products follow their lambdas: K L++ <- K L+, ...
+        if (H.b) {  // AL mode: A L++ <- A L+, A L+ <- A lambda_j
+            H.MLh2[i] = H.MLh1[i];
+            H.MLh1[i] = H.ML[i];
+            H.ML[i] = H.S->zero_x ? 0.0 : H.b[i] - H.r[i];
+        } else if (H.KLh1) {  // K, M products follow their lambdas: K L++ <- K L+, ...
             H.KLh2[i] = H.KLh1[i];
             H.MLh2[i] = H.MLh1[i];
             H.KLh1[i] = H.KL[i];
@@ -181,8 +192,8 @@ static __global__ void k_adj_advance(long long ndof, const double *__restrict__ 
 // r = b - ax0, reductions b.b and r.r, then the same solver-state set-up as
 // the operator-pass initial residual (PolInitResid)
 static __global__ void k_init_pointwise(long long ndof, const double *__restrict__ b, const double *__restrict__ ax0,
-                                        double *r, SolveScalars *S, int has_r32, cudaGraphConditionalHandle cond,
-                                        int has_cond, Partials<2> part) {
+                                        double *r, SolveScalars *S, int has_r32, int accept_x0,
+                                        cudaGraphConditionalHandle cond, int has_cond, Partials<2> part) {
     double red[2] = {0.0, 0.0};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
         const double bv = b[i], rv = bv - ax0[i];
@@ -191,7 +202,7 @@ static __global__ void k_init_pointwise(long long ndof, const double *__restrict
         red[1] += rv * rv;
     }
     double tot[2];
-    if (grid_reduce<EW, 2>(red, part, tot)) init_finish(S, tot, has_r32, cond, has_cond);
+    if (grid_reduce<EW, 2>(red, part, tot)) init_finish(S, tot, has_r32, cond, has_cond, accept_x0 != 0);
 }
 
 // ---------------------------------------------------------------------------
