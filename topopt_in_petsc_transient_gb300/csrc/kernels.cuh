@@ -508,22 +508,89 @@ static __global__ void k_newmark(long long ndof, const double *__restrict__ x, c
     }
 }
 
-// after a forward solve: the tracked products of the new state,
-// A u = b - r (the solve's final residual), A du and A ddu by the Newmark
-// corrector applied to the tracked products; A ddu of the previous state
-// moves to AAp (free rows; clamped rows hold 0)
-static __global__ void k_track_products(long long ndof, const double *__restrict__ b, const double *__restrict__ r,
-                                        const SolveScalars *S, double *AU, double *AV, double *AA, double *AAp,
-                                        Newmark nm) {
+// ---------------------------------------------------------------------------
+// Mixed forward sweep: tracked products and next-step preparation.
+// With A = sK K + sM M the step operator and s = (u, du, ddu) a state, the
+// tracked products T = (A u, A du, A ddu) give the next step's
+//   KS = sum_i c'_i s_i              (the only operator input: b needs K KS)
+//   BT = sum_i cA_i T_i              (b = f + BT + K KS)
+//   X0 = predictor . s,  AX = predictor . T   (r0 = b - AX)
+// (c'_i = cK_i - cM_i sK/sM, cA_i = cM_i/sM; SolveStateBlock,
+// LinearElasticity.cc:1317-1361).  X0, BT and AX are written into the solver
+// vectors x, b and r of the next solve, which reads them in its first pass.
+// ---------------------------------------------------------------------------
+struct FwdPrep {
+    double ck[3], cA[3];   // c'_i and cA_i
+    double pred[3];        // predictor u + pred1 du + pred2 ddu (no older acceleration)
+    double pred2[2];       // with ddu--: u + pred1 du + pred2[0] ddu + pred2[1] ddu--
+    int use_pred2;
+    double *KS, *X0, *BT, *AX;
+};
+__device__ __forceinline__ void fwd_prep(long long i, double u, double du, double ddu, double ddu_prev, bool has_prev,
+                                         double au, double av, double aa, double aa_prev, const FwdPrep &P) {
+    P.KS[i] = P.ck[0] * u + P.ck[1] * du + P.ck[2] * ddu;
+    P.BT[i] = P.cA[0] * au + P.cA[1] * av + P.cA[2] * aa;
+    double x = P.pred[0] * u + P.pred[1] * du, ax = P.pred[0] * au + P.pred[1] * av;
+    if (has_prev && P.use_pred2) {
+        x += P.pred2[0] * ddu + P.pred2[1] * ddu_prev;
+        ax += P.pred2[0] * aa + P.pred2[1] * aa_prev;
+    } else {
+        x += P.pred[2] * ddu;
+        ax += P.pred[2] * aa;
+    }
+    P.X0[i] = x;
+    P.AX[i] = ax;
+}
+
+// after a forward solve (Newmark corrector, LinearElasticity.cc:1363-1375):
+// the new state into history slot j; the tracked products of the new state,
+// A u = b - r (the solve's final, FP64-accurate residual; 0 when the solve
+// zeroed x), A du and A ddu by the same linear corrector; then the next
+// step's KS, X0 (into x), BT (into b) and AX (into r)
+static __global__ void k_newmark_track(long long ndof, double *x, const StepCtx *st, const double *cp, double *Uh,
+                                       double *DUh, double *DDUh, Newmark nm, double *b, double *r,
+                                       const SolveScalars *S, double *AU, double *AV, double *AA, FwdPrep P) {
+    const int j = st->j;
+    const double *u, *du, *ddu;
+    if (j == 0) {
+        const double *base = cp + (long long)st->block * 3 * ndof;
+        u = base;
+        du = base + ndof;
+        ddu = base + 2 * ndof;
+    } else {
+        u = Uh + (long long)(j - 1) * ndof;
+        du = DUh + (long long)(j - 1) * ndof;
+        ddu = DDUh + (long long)(j - 1) * ndof;
+    }
+    double *uo = Uh + (long long)j * ndof, *duo = DUh + (long long)j * ndof, *dduo = DDUh + (long long)j * ndof;
     const bool zx = S->zero_x != 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        const double un = x[i], dU = un - u[i], dup = du[i], ddup = ddu[i];
+        const double dun = nm.a[0] * dup + nm.a[1] * ddup + nm.a[2] * dU;
+        const double ddun = -nm.a[3] * dup - nm.a[4] * ddup + nm.a[5] * dU;
+        uo[i] = un;
+        duo[i] = dun;
+        dduo[i] = ddun;
         const double aun = zx ? 0.0 : b[i] - r[i], d = aun - AU[i];
         const double av = AV[i], aa = AA[i];
-        AAp[i] = aa;
+        const double avn = nm.a[0] * av + nm.a[1] * aa + nm.a[2] * d;
+        const double aan = -nm.a[3] * av - nm.a[4] * aa + nm.a[5] * d;
         AU[i] = aun;
-        AV[i] = nm.a[0] * av + nm.a[1] * aa + nm.a[2] * d;
-        AA[i] = -nm.a[3] * av - nm.a[4] * aa + nm.a[5] * d;
+        AV[i] = avn;
+        AA[i] = aan;
+        fwd_prep(i, un, dun, ddun, ddup, true, aun, avn, aan, aa, P);
     }
+}
+
+// next-step preparation from given states and tracked products (block start:
+// no older acceleration; re-anchoring: ddu_prev and A ddu_prev given)
+static __global__ void k_fwd_prep(long long ndof, const double *__restrict__ u, const double *__restrict__ du,
+                                  const double *__restrict__ ddu, const double *__restrict__ ddu_prev,
+                                  const double *__restrict__ AU, const double *__restrict__ AV,
+                                  const double *__restrict__ AA, const double *__restrict__ AAprev, FwdPrep P) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)
+        fwd_prep(i, u[i], du[i], ddu[i], ddu_prev ? ddu_prev[i] : 0.0, ddu_prev != nullptr, AU[i], AV[i], AA[i],
+                 AAprev ? AAprev[i] : 0.0, P);
 }
 
 static __global__ void k_step_set(StepCtx *st, int block, int j) {

@@ -326,10 +326,11 @@ struct TopoLE {
     // solve takes (N A N + I - N) x0 from ax0 (= sq)
     double *KLh1 = nullptr, *MLh1 = nullptr, *KLh2 = nullptr, *MLh2 = nullptr;
     bool ax0_pending = false;
-    // forward sweep: tracked products A u-, A du-, A ddu-, A ddu-- of the
-    // previous state; fwd_init_pending: the next solve's initial residual
-    // comes from the fused right-hand-side pass (PolRhsInit)
-    double *AUt = nullptr, *AVt = nullptr, *AAt = nullptr, *AApt = nullptr;
+    // mixed forward sweep: tracked products A u-, A du-, A ddu- of the
+    // previous state, AApt scratch for A ddu-- when re-anchoring, KSt the
+    // next step's K-pass input; fwd_init_pending: the next solve's initial
+    // residual comes from the fused right-hand-side pass (PolRhsInit)
+    double *AUt = nullptr, *AVt = nullptr, *AAt = nullptr, *AApt = nullptr, *KSt = nullptr;
     bool fwd_init_pending = false;
     int kb = 0;
     bool fp64_solves = false;  // the SOMMG basis solves run the FP64 FCG in either mode
@@ -497,6 +498,7 @@ int le_alloc(TopoLE *le) {
         AG(le->AVt, nd);
         AG(le->AAt, nd);
         AG(le->AApt, nd);
+        AG(le->KSt, nd);
     }
     if (!p.reduction) {
         AG(le->KLh1, nd);
@@ -1294,67 +1296,70 @@ static void fwd_rhs(TopoLE *le) {
         fwd_rhs_t<double>(le);
 }
 
-template <class A>
-static void fwd_rhs_init_t(TopoLE *le, cudaGraphConditionalHandle cond, int has_cond) {
+// coefficients of the next-step preparation (k_newmark_track, k_fwd_prep)
+static FwdPrep fwd_prep_args(TopoLE *le) {
     const LEParams &p = le->p;
-    Level &l0 = le->L[0];
     const double *a = le->a;
     const Operator &op = le->ops[0];
-    PolRhsInit<A> pr;
-    memset(&pr, 0, sizeof(pr));
-    pr.fixed = l0.fixed;
-    pr.w = fine_weights<A>(le, true, false, nullptr, 1.0, 0.0);
-    pr.cp = le->cp;
-    pr.Uh = le->Uh;
-    pr.DUh = le->DUh;
-    pr.DDUh = le->DDUh;
-    pr.ndof = le->ndof;
-    pr.rhs0 = le->rhs0;
-    pr.load_scale = 1.0 / (p.ny - 1);
-    pr.loadsignal = p.loadsignal;
-    pr.load2_dof = p.load2_node >= 0 ? 3LL * p.load2_node + 2 : -1;
-    pr.load2_phase = p.load2_phase;
+    FwdPrep P;
+    memset(&P, 0, sizeof(P));
     // B_i = cM_i M + cK_i K of (u-, du-, ddu-) (LinearElasticity.cc:1028-1044)
     const double cM[3] = {a[5] + a[2] * p.dalpha, a[3] - a[0] * p.dalpha, a[4] - a[1] * p.dalpha};
     const double cK[3] = {a[2] * p.dbeta, -a[0] * p.dbeta, -a[1] * p.dbeta};
     for (int i = 0; i < 3; i++) {
-        pr.cA[i] = cM[i] / op.sM;
-        pr.ck[i] = cK[i] - cM[i] * op.sK / op.sM;
+        P.cA[i] = cM[i] / op.sM;
+        P.ck[i] = cK[i] - cM[i] * op.sK / op.sM;
     }
     // initial guess: the Newmark predictor u- + dt du- + (1/2 - 1/4) dt^2 ddu-,
     // or (extrapolate >= 1) with ddu+ = ddu- held over the step,
     // u- + dt du- + dt^2/2 ddu-; third order (extrapolate = 2): ddu+
     // extrapolated linearly, u- + dt du- + dt^2/4 (3 ddu- - ddu--)
     const double dt = le->dt;
-    pr.pred[0] = 1.0;
-    pr.pred[1] = (p.ti == 0) ? 0.0 : dt;
-    pr.pred[2] = (p.ti == 0) ? 0.0 : (p.extrapolate ? 0.5 : 0.25) * dt * dt;
-    pr.use_pred2 = (p.ti != 0 && p.extrapolate >= 2) ? 1 : 0;
-    pr.pred2[0] = 0.75 * dt * dt;
-    pr.pred2[1] = -0.25 * dt * dt;
-    pr.AU = le->AUt;
-    pr.AV = le->AVt;
-    pr.AA = le->AAt;
-    pr.AAp = le->AApt;
+    P.pred[0] = 1.0;
+    P.pred[1] = (p.ti == 0) ? 0.0 : dt;
+    P.pred[2] = (p.ti == 0) ? 0.0 : (p.extrapolate ? 0.5 : 0.25) * dt * dt;
+    P.use_pred2 = (p.ti != 0 && p.extrapolate >= 2) ? 1 : 0;
+    P.pred2[0] = 0.75 * dt * dt;
+    P.pred2[1] = -0.25 * dt * dt;
+    P.KS = le->KSt;
+    P.X0 = le->sx;
+    P.BT = le->sb;
+    P.AX = le->sr;
+    return P;
+}
+
+// mixed path only (tracked products exist only there); the K-only pass stays
+// FP64-accurate: K applied to the near-rigid local motion of the state cancels
+// strongly, and FP32 rounding of that product puts noise into b above the
+// solve tolerance (measured: 4.3 instead of 2.8 Krylov iterations per solve on
+// the 96x48x48 cantilever)
+static void fwd_rhs_init(TopoLE *le, cudaGraphConditionalHandle cond, int has_cond) {
+    const LEParams &p = le->p;
+    Level &l0 = le->L[0];
+    PolRhsInit<df> pr;
+    memset(&pr, 0, sizeof(pr));
+    pr.fixed = l0.fixed;
+    pr.w = fine_weights<df>(le, true, false, nullptr, 1.0, 0.0);
+    pr.KS = le->KSt;
+    pr.rhs0 = le->rhs0;
+    pr.load_scale = 1.0 / (p.ny - 1);
+    pr.loadsignal = p.loadsignal;
+    pr.load2_dof = p.load2_node >= 0 ? 3LL * p.load2_node + 2 : -1;
+    pr.load2_phase = p.load2_phase;
     pr.st = le->st;
     pr.b = le->sb;
-    pr.x0 = le->sx;
     pr.r = le->sr;
     pr.S = le->S;
     pr.cond = cond;
     pr.has_cond = has_cond;
     pr.part = P2(le);
-    launch_tile<A>(l0.g, fine_const<A>(le), pr, le->stream);
-}
-// mixed path only (tracked products exist only there): every solve ends on an
-// FP64-accurate true residual, so A u+ = b - r holds to double-float rounding
-static void fwd_rhs_init(TopoLE *le, cudaGraphConditionalHandle cond, int has_cond) {
-    fwd_rhs_init_t<df>(le, cond, has_cond);
+    launch_tile<df>(l0.g, fine_const<df>(le), pr, le->stream);
 }
 
 template <bool HK, bool HM>
 static void product(TopoLE *le, const double *x, double *y, const double *P, double sK, double sM);
-// tracked products A u, A du, A ddu of a block's start state (checkpoint c)
+// tracked products A u, A du, A ddu of a block's start state (checkpoint c),
+// then the first step's preparation
 static void track_block_start(TopoLE *le, int c) {
     const long long nd = le->ndof;
     const double *base = le->cp + (size_t)c * 3 * nd;
@@ -1362,28 +1367,38 @@ static void track_block_start(TopoLE *le, int c) {
     product<true, true>(le, base, le->AUt, nullptr, op.sK, op.sM);
     product<true, true>(le, base + nd, le->AVt, nullptr, op.sK, op.sM);
     product<true, true>(le, base + 2 * nd, le->AAt, nullptr, op.sK, op.sM);
+    count_launch();
+    k_fwd_prep<<<ew_blocks(nd), EW, 0, le->stream>>>(nd, base, base + nd, base + 2 * nd, nullptr, le->AUt, le->AVt,
+                                                      le->AAt, nullptr, fwd_prep_args(le));
 }
 
-// Re-anchoring of the tracked A du, A ddu, A ddu-- before step j of block c.
-// Given the states u, the corrector du+ = -du + (2/dt) (u+ - u),
-// ddu+ = (4/dt^2) (u+ - u) - (4/dt) du - ddu has a double eigenvalue -1, so
-// rounding in the tracked A u (about 1e-14 relative) grows like n^1.5 in
-// A ddu; over 200 steps it reaches the 1e-10 solve tolerance and costs extra
-// Krylov iterations.  Exact products every TRACK_ANCHOR steps bound n.
+// Re-anchoring of the tracked A du, A ddu before step j of block c (and the
+// step's preparation).  Given the states u, the corrector
+// du+ = -du + (2/dt) (u+ - u), ddu+ = (4/dt^2) (u+ - u) - (4/dt) du - ddu has
+// a double eigenvalue -1, so rounding in the tracked A u (about 1e-14
+// relative) grows like n^1.5 in A ddu; over 200 steps it reaches the 1e-10
+// solve tolerance and costs extra Krylov iterations.  Exact products every
+// TRACK_ANCHOR steps bound n.
 constexpr int TRACK_ANCHOR = 32;
 static void track_anchor(TopoLE *le, int c, int j) {
     const long long nd = le->ndof;
     const Operator &op = le->ops[0];
+    const double *u = le->Uh + (size_t)(j - 1) * nd, *du = le->DUh + (size_t)(j - 1) * nd,
+                 *ddu = le->DDUh + (size_t)(j - 1) * nd;
     const double *ddu2 = (j >= 2) ? le->DDUh + (size_t)(j - 2) * nd : le->cp + (size_t)c * 3 * nd + 2 * nd;
-    product<true, true>(le, le->DUh + (size_t)(j - 1) * nd, le->AVt, nullptr, op.sK, op.sM);
-    product<true, true>(le, le->DDUh + (size_t)(j - 1) * nd, le->AAt, nullptr, op.sK, op.sM);
+    product<true, true>(le, du, le->AVt, nullptr, op.sK, op.sM);
+    product<true, true>(le, ddu, le->AAt, nullptr, op.sK, op.sM);
     product<true, true>(le, ddu2, le->AApt, nullptr, op.sK, op.sM);
+    count_launch();
+    k_fwd_prep<<<ew_blocks(nd), EW, 0, le->stream>>>(nd, u, du, ddu, ddu2, le->AUt, le->AVt, le->AAt, le->AApt,
+                                                      fwd_prep_args(le));
 }
 
-// Mixed path: right-hand side, initial guess and initial residual in one
-// K-only pass from the tracked products (PolRhsInit), the products of the new
-// state tracked after the corrector.  Plain FP64 path: right-hand side from
-// the stored states, then the initial residual b - A x0.
+// Mixed path: right-hand side and initial residual in one K-only pass
+// (PolRhsInit) from what the previous corrector prepared; the corrector
+// tracks the products of the new state and prepares the next step
+// (k_newmark_track).  Plain FP64 path: right-hand side from the stored
+// states, the initial residual b - A x0, the corrector.
 static int fwd_step(TopoLE *le, bool capturing) {
     cudaStream_t s = le->stream;
     const bool track = le->AUt != nullptr;
@@ -1397,12 +1412,13 @@ static int fwd_step(TopoLE *le, bool capturing) {
     Newmark nm;
     memcpy(nm.a, le->a, sizeof(nm.a));
     count_launch();
-    k_newmark<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh, le->DUh, le->DDUh, nm);
-    if (track) {
-        count_launch();
-        k_track_products<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sb, le->sr, le->S, le->AUt, le->AVt,
-                                                            le->AAt, le->AApt, nm);
-    }
+    if (track)
+        k_newmark_track<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh, le->DUh,
+                                                           le->DDUh, nm, le->sb, le->sr, le->S, le->AUt, le->AVt,
+                                                           le->AAt, fwd_prep_args(le));
+    else
+        k_newmark<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh, le->DUh, le->DDUh,
+                                                     nm);
     count_launch();
     k_step_add<<<1, 1, 0, s>>>(le->st, +1);
     return TOPO_OK;

@@ -562,19 +562,18 @@ struct PolRhsFwd {
 };
 
 // ---------------------------------------------------------------------------
-// Forward step right-hand side and initial residual in one K-only pass.
-// With A = sK K + sM M the step operator and the tracked products
-// AS_i = A s_i of the previous state s = (u-, du-, ddu-) (exact: A u = b - r
-// of the previous solve, and A du, A ddu follow the Newmark corrector, which
-// is linear), M s_i = (AS_i - sK K s_i) / sM and
+// Forward step right-hand side and initial residual in one K-only pass
+// (mixed path).  With A = sK K + sM M the step operator and the tracked
+// products AS_i = A s_i of the previous state s = (u-, du-, ddu-),
+// M s_i = (AS_i - sK K s_i) / sM, so
 //   b = f + sum_i B_i s_i = f + sum_i (cM_i / sM) AS_i + K (sum_i c'_i s_i),
 //   c'_i = cK_i - cM_i sK / sM
-// (SolveStateBlock, LinearElasticity.cc:1317-1361); the initial guess x0 is the
-// predictor and A x0 the same combination of the tracked products, so
-// r0 = b - A x0 needs no operator pass.  The pass also forms b.b and r.r and
-// sets up the FCG state.  Initial guess: the Newmark predictor
-// u- + dt du- + (1/2 - beta) dt^2 ddu- (pred), or with the acceleration
-// extrapolated linearly from ddu- and ddu-- (use_pred2, pred2).
+// (SolveStateBlock, LinearElasticity.cc:1317-1361).  The corrector of the
+// previous step (k_newmark_track, or k_fwd_prep at a block start) has left
+// KS = sum c'_i s_i, BT = sum (cM_i/sM) AS_i in b, the initial guess x0 (the
+// predictor) in x and A x0 (the predictor applied to the tracked products) in
+// r, so this pass forms b = f + BT + K KS and r0 = b - A x0 with b.b and r.r,
+// and sets up the FCG state.
 // ---------------------------------------------------------------------------
 template <class T>
 struct PolRhsInit {
@@ -582,55 +581,26 @@ struct PolRhsInit {
     static constexpr bool HAS_K = true, HAS_M = false;
     const uint8_t *fixed;
     Weights<T> w;                       // kf, sK = 1
-    const double *cp, *Uh, *DUh, *DDUh;
-    long long ndof;
+    const double *KS;
     const double *rhs0;
     double load_scale;
     int loadsignal;
     long long load2_dof;
     double load2_phase;
-    double ck[3];                       // c'_i
-    double cA[3];                       // cM_i / sM
-    double pred[3], pred2[2];
-    int use_pred2;
-    const double *AU, *AV, *AA, *AAp;   // A u-, A du-, A ddu-, A ddu-- (free rows)
     const StepCtx *st;
-    double *b, *x0, *r;
+    double *b, *r;                      // in: BT and A x0; out: b and r0
     SolveScalars *S;
     cudaGraphConditionalHandle cond;
     int has_cond;
     Partials<2> part;
-    __device__ __forceinline__ void prev(const double *&u, const double *&du, const double *&ddu) const {
-        int j = st->j;
-        if (j == 0) {
-            const double *base = cp + (long long)st->block * 3 * ndof;
-            u = base;
-            du = base + ndof;
-            ddu = base + 2 * ndof;
-        } else {
-            u = Uh + (long long)(j - 1) * ndof;
-            du = DUh + (long long)(j - 1) * ndof;
-            ddu = DDUh + (long long)(j - 1) * ndof;
-        }
-    }
     __device__ void load(long long n, T v[1][3]) const {
-        const double *u, *du, *ddu;
-        prev(u, du, ddu);
-        for (int c = 0; c < 3; c++) {
-            const long long i = 3 * n + c;
-            v[0][c] = T(ck[0] * u[i] + ck[1] * du[i] + ck[2] * ddu[i]);
-        }
+        v[0][0] = T(KS[3 * n]);
+        v[0][1] = T(KS[3 * n + 1]);
+        v[0][2] = T(KS[3 * n + 2]);
         mask3(fixed[n], v[0]);
     }
     __device__ void coef(long long e, T &kc, T &mc) const { w.get(e, kc, mc); }
     __device__ void epilogue(long long n, int, int, int, const T y[3], double red[2]) const {
-        const double *u, *du, *ddu;
-        prev(u, du, ddu);
-        const double *ddu2 = nullptr;
-        if (use_pred2 && st->j >= 2)
-            ddu2 = DDUh + (long long)(st->j - 2) * ndof;
-        else if (use_pred2 && st->j == 1)
-            ddu2 = cp + (long long)st->block * 3 * ndof + 2 * ndof;
         const int t = st->tsc * st->block + st->j + 1;
         const double s = load_signal(loadsignal, t * st->dt) * load_scale;
         const uint8_t f = fixed[n];
@@ -638,23 +608,13 @@ struct PolRhsInit {
             const long long i = 3 * n + c;
             if ((f >> c) & 1) {
                 b[i] = 0.0;
-                x0[i] = 0.0;
                 r[i] = 0.0;
                 continue;
             }
             const double f2 = (i == load2_dof) ? load2_signal(load2_phase, t * st->dt) * load_scale : 0.0;
-            const double bv = rhs0[i] * s + f2 + cA[0] * AU[i] + cA[1] * AV[i] + cA[2] * AA[i] + todbl(y[c]);
-            double xv = pred[0] * u[i] + pred[1] * du[i], ax = pred[0] * AU[i] + pred[1] * AV[i];
-            if (ddu2) {
-                xv += pred2[0] * ddu[i] + pred2[1] * ddu2[i];
-                ax += pred2[0] * AA[i] + pred2[1] * AAp[i];
-            } else {
-                xv += pred[2] * ddu[i];
-                ax += pred[2] * AA[i];
-            }
-            const double rv = bv - ax;
+            const double bv = rhs0[i] * s + f2 + b[i] + todbl(y[c]);
+            const double rv = bv - r[i];
             b[i] = bv;
-            x0[i] = xv;
             r[i] = rv;
             red[0] += bv * bv;
             red[1] += rv * rv;
