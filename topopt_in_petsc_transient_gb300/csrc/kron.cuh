@@ -23,9 +23,12 @@
 
 namespace topo {
 
-// node scaling s_n = 1 / sqrt(sM * mean_{e at n} mf_e)
+// masked node scaling per DOF: ms[3n + c] = 1 / sqrt(sM * mean_{e at n} mf_e)
+// on free DOFs and -1 on clamped ones (the mask N and the scaling S of P^-1
+// in one array laid out like the residual)
 template <class T>
-static __global__ void k_kron_scale(GridDesc g, const double *__restrict__ mf, double sM, T *scale) {
+static __global__ void k_kron_scale(GridDesc g, const uint8_t *__restrict__ fixed, const double *__restrict__ mf,
+                                    double sM, T *ms) {
     long long nn = g.nn();
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
         int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
@@ -38,7 +41,9 @@ static __global__ void k_kron_scale(GridDesc g, const double *__restrict__ mf, d
             cnt++;
         }
         double w = sM * s / (double)(cnt > 0 ? cnt : 1);
-        scale[n] = (T)(w > 0.0 ? 1.0 / sqrt(w) : 0.0);
+        const T sc = (T)(w > 0.0 ? 1.0 / sqrt(w) : 0.0);
+        const uint8_t f = fixed[n];
+        for (int c = 0; c < 3; c++) ms[3 * n + c] = ((f >> c) & 1) ? T(-1) : sc;
     }
 }
 
@@ -71,13 +76,15 @@ struct KronBand {
 };
 
 // The three axis passes stage whole grid lines in shared memory: each input
-// value is read from global memory once per pass.  A thread computes KRON_MP
+// value is read from global memory once per pass, with every load of a
+// thread issued before the CTA's barrier.  A thread computes KRON_MP
 // consecutive outputs of one line from a register window of KRON_MP + 2 KRON_B
 // staged values (3 shared-memory reads per output instead of 17).  Positions
 // at least KRON_B from both line ends use the interior taps, staged once per
 // CTA (the interior rows of the exact inverse agree with them to
-// 0.268^(2 KRON_B) relative); the others use their exact rows, which are zero
-// past the line end, so the window clamps indices there.
+// 0.268^(2 KRON_B) relative) and held in registers for a group of interior
+// outputs; the others use their exact rows, which are zero past the line end,
+// so the window clamps indices there.
 struct KronDot {
     const float *q32;
     SolveScalars *S;
@@ -85,6 +92,7 @@ struct KronDot {
 };
 
 constexpr int KRON_THREADS = 256;
+constexpr size_t KRON_SMEM_MAX = 200 * 1024;    // per-CTA staging limit (the selection checks it)
 constexpr int KRON_MP = 8;                      // outputs per thread along a line
 constexpr int KRON_WIN = KRON_MP + 2 * KRON_B;  // register window
 
@@ -110,6 +118,19 @@ __device__ __forceinline__ void kron_line(const T *src, int sstride, int len, in
         p = p < 0 ? 0 : (p > len - 1 ? len - 1 : p);
         win[k] = src[p * sstride];
     }
+    if (p0 >= KRON_B && p0 + KRON_MP <= len - KRON_B) {  // interior group: taps in registers
+        T tap[KRON_W];
+#pragma unroll
+        for (int d = 0; d < KRON_W; d++) tap[d] = tint[c * KRON_W + d];
+#pragma unroll
+        for (int k = 0; k < KRON_MP; k++) {
+            T acc = T(0);
+#pragma unroll
+            for (int d = 0; d < KRON_W; d++) acc += tap[d] * win[k + d];
+            out[k] = acc;
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < KRON_MP; k++) {
         const int pos = p0 + k;
@@ -122,34 +143,44 @@ __device__ __forceinline__ void kron_line(const T *src, int sstride, int len, in
     }
 }
 
-// x pass: KX_LINES x-lines (3 nx consecutive values each) per CTA.  The
-// staged input is the masked, node-scaled residual t = S N r; in the mixed
-// FCG the staging also re-forms r32 = sigma r after a residual replacement
-// (S->rescale).
-constexpr int KX_LINES = 8;
-
+// x pass: kx lines (3 nx consecutive values each) per CTA.  The staged input
+// is the masked, node-scaled residual t = S N r; in the mixed FCG the staging
+// also re-forms r32 = sigma r after a residual replacement (S->rescale).
+// Shared layout [line][component][position] with an odd pitch (conflict-free
+// windows); the outputs go through shared memory so that the global stores
+// are coalesced.
+__host__ __device__ inline int kx_pitch(int nx) { return nx | 1; }
+__host__ inline int kx_lines(const GridDesc &g, size_t elem) {
+    const size_t per_line = elem * 2 * 3 * (size_t)kx_pitch(g.nx);
+    int L = (int)((size_t)(48 * 1024) / per_line);
+    return L < 1 ? 1 : (L > 8 ? 8 : L);
+}
 __host__ inline size_t kron_x_smem(const GridDesc &g, size_t elem) {
-    return elem * ((size_t)KX_LINES * 3 * g.nx + 3 * KRON_W);
+    return elem * ((size_t)kx_lines(g, elem) * 2 * 3 * kx_pitch(g.nx) + 3 * KRON_W);
 }
 
 template <class T, class R>
 static __global__ void __launch_bounds__(KRON_THREADS)
-    k_kron_x(GridDesc g, const uint8_t *__restrict__ fixed, R *r, const double *__restrict__ r64,
-             const SolveScalars *S, const T *__restrict__ scale, KronBand<T> B, T *out) {
+    k_kron_x(GridDesc g, int kx, R *r, const double *__restrict__ r64, const SolveScalars *S, const T *__restrict__ ms,
+             KronBand<T> B, T *out) {
     extern __shared__ __align__(16) unsigned char kron_smem[];
-    T *tile = reinterpret_cast<T *>(kron_smem);  // [KX_LINES][3 nx]
-    T *tint = tile + KX_LINES * 3 * g.nx;        // [3][KRON_W]
+    const int LP = kx_pitch(g.nx);
+    T *tile = reinterpret_cast<T *>(kron_smem);  // [kx][3][LP]
+    T *otile = tile + kx * 3 * LP;               // [kx][3][LP]
+    T *tint = otile + kx * 3 * LP;               // [3][KRON_W]
     const int row = 3 * g.nx;
     const long long nlines = (long long)g.ny * g.nz;
-    const long long line0 = (long long)blockIdx.x * KX_LINES;
-    const int nl = (int)(nlines - line0 < KX_LINES ? nlines - line0 : KX_LINES);
+    const long long line0 = (long long)blockIdx.x * kx;
+    const int nl = (int)(nlines - line0 < kx ? nlines - line0 : kx);
     const bool rs = S != nullptr && S->rescale != 0;
     const double sg = rs ? S->sigma : 1.0;
     kron_stage_interior(B, 0, g.nx, tint);
-    for (int t = threadIdx.x; t < nl * row; t += blockDim.x) {
+    const long long q0 = line0 * row;
+    const int nv = nl * row;
+#pragma unroll 4
+    for (int t = threadIdx.x; t < nv; t += KRON_THREADS) {
         const int l = t / row, w = t - l * row, i = w / 3, c = w - 3 * i;
-        const long long q = (line0 + l) * row + w;
-        const long long n = (line0 + l) * g.nx + i;
+        const long long q = q0 + t;
         R rv;
         if (rs) {
             rv = (R)(sg * r64[q]);
@@ -157,44 +188,57 @@ static __global__ void __launch_bounds__(KRON_THREADS)
         } else {
             rv = r[q];
         }
-        tile[t] = ((fixed[n] >> c) & 1) ? T(0) : (T)rv * scale[n];
+        const T m = ms[q];
+        tile[(l * 3 + c) * LP + i] = m < T(0) ? T(0) : (T)rv * m;
     }
     __syncthreads();
     const int ngrp = (g.nx + KRON_MP - 1) / KRON_MP;
-    for (int t = threadIdx.x; t < nl * 3 * ngrp; t += blockDim.x) {
-        const int l = t / (3 * ngrp), rem = t - l * 3 * ngrp, c = rem / ngrp, grp = rem - c * ngrp;
+    const int nrows = nl * 3;
+    for (int t = threadIdx.x; t < nrows * ngrp; t += KRON_THREADS) {
+        const int rw = t % nrows, grp = t / nrows, c = rw % 3;
         const int p0 = grp * KRON_MP;
         T o[KRON_MP];
-        kron_line(tile + l * row + c, 3, g.nx, p0, tint, B, 0, c, o);
-        T *dst = out + (line0 + l) * row + c;
+        kron_line(tile + rw * LP, 1, g.nx, p0, tint, B, 0, c, o);
 #pragma unroll
         for (int k = 0; k < KRON_MP; k++)
-            if (p0 + k < g.nx) dst[3 * (p0 + k)] = o[k];
+            if (p0 + k < g.nx) otile[rw * LP + p0 + k] = o[k];
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int t = threadIdx.x; t < nv; t += KRON_THREADS) {
+        const int l = t / row, w = t - l * row, i = w / 3, c = w - 3 * i;
+        out[q0 + t] = otile[(l * 3 + c) * LP + i];
     }
 }
 
 // y pass (AXIS 1) and z pass (AXIS 2): a CTA stages a chunk of KW values of
 // one x-row (consecutive in memory) at every position along the line.  The
 // z pass finishes P^-1: out = S x on free DOFs, r on clamped ones; with DOT it
-// also forms the FCG dot products z.r and z.q of its output.
+// also forms the FCG dot products z.r and z.q of its output.  The z pass
+// stages its epilogue operands (r, the masked scale, q) with the input, so
+// that no global load waits inside the output loop.
 constexpr int KW = 32;
 
 __host__ inline unsigned kron_yz_blocks(const GridDesc &g, int axis) {
     const int nchunk = (3 * g.nx + KW - 1) / KW;
     return (unsigned)nchunk * (unsigned)(axis == 1 ? g.nz : g.ny);
 }
-__host__ inline size_t kron_yz_smem(const GridDesc &g, int axis, size_t elem) {
-    return elem * ((size_t)KW * (axis == 1 ? g.ny : g.nz) + 3 * KRON_W);
+__host__ inline size_t kron_yz_smem(const GridDesc &g, int axis, size_t elem, bool dot = false) {
+    const size_t len = (size_t)(axis == 1 ? g.ny : g.nz);
+    return elem * (KW * len * (axis == 2 ? 3 : 1) + 3 * KRON_W) + (dot ? sizeof(float) * KW * len : 0);
 }
 
 template <class T, class R, int AXIS, bool DOT>
 static __global__ void __launch_bounds__(KRON_THREADS)
-    k_kron_yz(GridDesc g, const uint8_t *__restrict__ fixed, const R *__restrict__ r, const T *__restrict__ scale,
-              KronBand<T> B, const T *__restrict__ in, T *out, KronDot kd) {
+    k_kron_yz(GridDesc g, const R *__restrict__ r, const T *__restrict__ ms, KronBand<T> B, const T *__restrict__ in,
+              T *out, KronDot kd) {
     extern __shared__ __align__(16) unsigned char kron_smem[];
     const int len = AXIS == 1 ? g.ny : g.nz;
     T *tile = reinterpret_cast<T *>(kron_smem);  // [len][KW]
     T *tint = tile + (size_t)len * KW;           // [3][KRON_W]
+    T *rt = tint + 3 * KRON_W;                   // AXIS 2: r [len][KW]
+    T *mt = rt + (size_t)len * KW;               // AXIS 2: masked scale [len][KW]
+    float *qt = reinterpret_cast<float *>(mt + (size_t)len * KW);  // DOT: q [len][KW]
     const int row = 3 * g.nx;
     const int nchunk = (row + KW - 1) / KW;
     const int chunk = blockIdx.x % nchunk, other = blockIdx.x / nchunk;
@@ -202,17 +246,26 @@ static __global__ void __launch_bounds__(KRON_THREADS)
     const long long S = AXIS == 1 ? (long long)row : (long long)row * g.ny;
     const long long base = AXIS == 1 ? (long long)other * row * g.ny + w0 : (long long)other * row + w0;
     kron_stage_interior(B, AXIS, len, tint);
-    for (int t = threadIdx.x; t < len * KW; t += blockDim.x) {
+#pragma unroll 4
+    for (int t = threadIdx.x; t < len * KW; t += KRON_THREADS) {
         const int p = t / KW, w = t - p * KW;
-        if (w < wn) tile[t] = in[base + p * S + w];
+        if (w < wn) {
+            const long long q = base + p * S + w;
+            tile[t] = in[q];
+            if (AXIS == 2) {
+                rt[t] = (T)r[q];
+                mt[t] = ms[q];
+                if (DOT) qt[t] = kd.q32[q];
+            }
+        }
     }
     __syncthreads();
     double red[2] = {0.0, 0.0};
     const int ngrp = (len + KRON_MP - 1) / KRON_MP;
-    for (int t = threadIdx.x; t < ngrp * KW; t += blockDim.x) {
+    for (int t = threadIdx.x; t < ngrp * KW; t += KRON_THREADS) {
         const int grp = t / KW, w = t - grp * KW;
         if (w >= wn) continue;
-        const int i3 = w0 + w, i = i3 / 3, c = i3 - 3 * i;
+        const int c = (w0 + w) % 3;
         const int p0 = grp * KRON_MP;
         T o[KRON_MP];
         kron_line(tile + w, KW, len, p0, tint, B, AXIS, c, o);
@@ -222,12 +275,13 @@ static __global__ void __launch_bounds__(KRON_THREADS)
             if (p >= len) break;
             const long long q = base + p * S + w;
             if (AXIS == 2) {
-                const long long n = i + (long long)g.nx * (other + (long long)g.ny * p);
-                const T z = ((fixed[n] >> c) & 1) ? (T)r[q] : scale[n] * o[k];
+                const int sidx = p * KW + w;
+                const T m = mt[sidx], rv = rt[sidx];
+                const T z = m < T(0) ? rv : m * o[k];
                 out[q] = z;
                 if (DOT) {
-                    red[0] += (double)((float)z * (float)r[q]);
-                    red[1] += (double)((float)z * kd.q32[q]);
+                    red[0] += (double)((float)z * (float)rv);
+                    red[1] += (double)((float)z * qt[sidx]);
                 }
             } else {
                 out[q] = o[k];

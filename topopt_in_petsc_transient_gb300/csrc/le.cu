@@ -626,8 +626,8 @@ int le_alloc(TopoLE *le) {
         le->mu_KM = mass_scaled_lmax(KE, ME);
         le->nops = p.reduction ? 3 : 2;
         for (int o = 0; o < le->nops; o++) {
-            AG(le->ops[o].kscale_d, nn);
-            AG(le->ops[o].kscale_f, nn);
+            AG(le->ops[o].kscale_d, 3 * nn);  // masked scale, one value per DOF
+            AG(le->ops[o].kscale_f, 3 * nn);
         }
     }
 
@@ -780,9 +780,9 @@ static int setup_operator(TopoLE *le, int o) {
     {
         Level &l0 = le->L[0];
         count_launch();
-        k_kron_scale<double><<<ew_blocks(l0.g.nn()), EW, 0, s>>>(l0.g, l0.mfd, op.sM, op.kscale_d);
+        k_kron_scale<double><<<ew_blocks(l0.g.nn()), EW, 0, s>>>(l0.g, l0.fixed, l0.mfd, op.sM, op.kscale_d);
         count_launch();
-        k_kron_scale<float><<<ew_blocks(l0.g.nn()), EW, 0, s>>>(l0.g, l0.mfd, op.sM, op.kscale_f);
+        k_kron_scale<float><<<ew_blocks(l0.g.nn()), EW, 0, s>>>(l0.g, l0.fixed, l0.mfd, op.sM, op.kscale_f);
         op.share = 0.0;
         if (op.sK != 0.0) {
             unsigned long long hb = 0ull;
@@ -796,8 +796,9 @@ static int setup_operator(TopoLE *le, int o) {
             op.share = op.sK / op.sM * ratio * le->mu_KM;
         }
         // the line-staging passes hold whole grid lines in shared memory (FP64: 8 bytes a value)
-        const size_t stage = std::max(kron_x_smem(l0.g, 8), std::max(kron_yz_smem(l0.g, 1, 8), kron_yz_smem(l0.g, 2, 8)));
-        op.kron = stage <= 100 * 1024 && op.sM > 0.0 && op.sK >= 0.0 &&
+        const size_t stage = std::max(std::max(kron_x_smem(l0.g, 8), kron_yz_smem(l0.g, 1, 8)),
+                                      std::max(kron_yz_smem(l0.g, 2, 8), kron_yz_smem(l0.g, 2, 4, true)));
+        op.kron = stage <= KRON_SMEM_MAX && op.sM > 0.0 && op.sK >= 0.0 &&
                   (le->p.mass_precond == 1 || (le->p.mass_precond == 2 && op.share <= le->p.mass_precond_share));
     }
     // adaptive depth: stop at the first level whose Jacobi-scaled operator is
@@ -986,35 +987,35 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     const T *sc = kron_scale<T>(le->ops[o]);
     const bool mixed = fz && std::is_same<T, float>::value;
     const long long nlines = (long long)g.ny * g.nz;
-    const size_t smx = kron_x_smem(g, sizeof(T)), smy = kron_yz_smem(g, 1, sizeof(T)), smz = kron_yz_smem(g, 2, sizeof(T));
+    const int kx = kx_lines(g, sizeof(T));
+    const size_t smx = kron_x_smem(g, sizeof(T)), smy = kron_yz_smem(g, 1, sizeof(T));
     static bool attr = false;
-    if (!attr) {  // lines of up to 1024 nodes
-        cudaFuncSetAttribute(k_kron_x<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        cudaFuncSetAttribute(k_kron_yz<T, T, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        cudaFuncSetAttribute(k_kron_yz<T, T, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        cudaFuncSetAttribute(k_kron_yz<T, T, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    if (!attr) {  // staged lines: the selection keeps every pass within KRON_SMEM_MAX
+        cudaFuncSetAttribute(k_kron_x<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
+        cudaFuncSetAttribute(k_kron_yz<T, T, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
+        cudaFuncSetAttribute(k_kron_yz<T, T, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
+        cudaFuncSetAttribute(k_kron_yz<T, T, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
         attr = true;
     }
     bool t;
     count_launch();
     t = timer_begin(TOPO_KT_KRON, g.nn(), s);
-    k_kron_x<T, T><<<(unsigned)((nlines + KX_LINES - 1) / KX_LINES), KRON_THREADS, smx, s>>>(
-        g, l0.fixed, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
+    k_kron_x<T, T><<<(unsigned)((nlines + kx - 1) / kx), KRON_THREADS, smx, s>>>(
+        g, kx, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
     timer_end(t, s);
     count_launch();
     t = timer_begin(TOPO_KT_KRON, g.nn(), s);
-    k_kron_yz<T, T, 1, false><<<kron_yz_blocks(g, 1), KRON_THREADS, smy, s>>>(g, l0.fixed, r, sc, B, w.xa, w.xb,
-                                                                             KronDot{});
+    k_kron_yz<T, T, 1, false><<<kron_yz_blocks(g, 1), KRON_THREADS, smy, s>>>(g, r, sc, B, w.xa, w.xb, KronDot{});
     timer_end(t, s);
     count_launch();
     t = timer_begin(TOPO_KT_KRON, g.nn(), s);
     if (mixed && le->p.mass_precond_smooth <= 0) {
-        k_kron_yz<T, T, 2, true><<<kron_yz_blocks(g, 2), KRON_THREADS, smz, s>>>(g, l0.fixed, r, sc, B, w.xb, w.xa,
-                                                                                KronDot{fz->q32, fz->S, fz->part});
+        k_kron_yz<T, T, 2, true><<<kron_yz_blocks(g, 2), KRON_THREADS, kron_yz_smem(g, 2, sizeof(T), true), s>>>(
+            g, r, sc, B, w.xb, w.xa, KronDot{fz->q32, fz->S, fz->part});
         fz->dotted = true;
     } else {
-        k_kron_yz<T, T, 2, false><<<kron_yz_blocks(g, 2), KRON_THREADS, smz, s>>>(g, l0.fixed, r, sc, B, w.xb, w.xa,
-                                                                                 KronDot{});
+        k_kron_yz<T, T, 2, false><<<kron_yz_blocks(g, 2), KRON_THREADS, kron_yz_smem(g, 2, sizeof(T)), s>>>(
+            g, r, sc, B, w.xb, w.xa, KronDot{});
     }
     timer_end(t, s);
     if (mixed) fz->scaled = true;

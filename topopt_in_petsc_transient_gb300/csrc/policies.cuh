@@ -177,7 +177,7 @@ struct PolPQ32 {
     Partials<1> part;
     __device__ __forceinline__ void pnew(long long n, float v[3]) const {
         const float beta = (float)S->beta;
-        const float *pp = pb[S->it & 1];
+        const float *pp = (S->it & 1) ? pb[1] : pb[0];  // a select: no local copy of pb
         for (int c = 0; c < 3; c++) v[c] = (beta == 0.0f) ? z[3 * n + c] : z[3 * n + c] + beta * pp[3 * n + c];
     }
     __device__ void load(long long n, float v[1][3]) const {
@@ -196,7 +196,7 @@ struct PolPQ32 {
         return r;
     }
     __device__ void epilogue(long long n, int, int, int, const float y[3], double red[1], const Pre &r) const {
-        float *pout = pb[(S->it + 1) & 1];
+        float *pout = (S->it & 1) ? pb[0] : pb[1];
         float s = 0.0f;
         for (int c = 0; c < 3; c++) {
             float pv = r.p[c];
