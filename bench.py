@@ -247,13 +247,15 @@ def run_gb300(args):
     # algorithmic bytes per launch (FP32 vectors of 3 nn values, 1-byte
     # clamp mask per node, FP32 element factors kf, mf):
     #   PQ32: stage z and p_prev, write p and q (4 x 12 B/node), mask, kf/mf
-    #   Kronecker pass: read and write one vector (24 B/node); the last of the
-    #     three passes also reads r, q, mask and node scaling (+29 B/node)
+    #   Kronecker pass: x pass reads r and the per-DOF masked scale and writes
+    #     its output (36 B/node); y pass reads and writes one vector (24 B/node);
+    #     z pass reads its input, r, the masked scale and q and writes z
+    #     (60 B/node)
     #   smoothing step: x, b, 1/diag, d read, d and x written (72 B/node), mask, kf/mf
     classes = [(1, "k_tile<float,PolPQ32> (FCG operator product q = A p with p = z + beta p_prev, FP32)",
                 49.0 * nn + 8.0 * nel),
                (2, "k_kron_pass<float> (one axis pass of the Kronecker mass inverse, 17-tap stencil, FP32)",
-                (24.0 + 24.0 + 53.0) / 3.0 * nn),
+                (36.0 + 24.0 + 60.0) / 3.0 * nn),
                (0, "k_tile<float,PolCheb> (FP32 Chebyshev-Jacobi smoothing step)", 73.0 * nn + 8.0 * nel)]
     kern = []
     for cls, name, nbytes in classes:
@@ -290,7 +292,7 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic (seedless uniform density 0.12, analytic load pulse)",
-        "config": {"workload": workload_name(args), "mode": "mixed: FP32 multigrid inside FP64 flexible CG",
+        "config": {"workload": workload_name(args), "mode": "mixed: FP32 flexible-CG recurrence, Kronecker mass preconditioner (multigrid when the stiffness share is large), FP64-accurate residual replacements",
                    "dofs": 3 * nn, "elements": nel, "steps_per_design_iter": args.nsteps, "ncp": args.ncp,
                    "rtol": args.rtol, "smooth": args.smooth, "nlvls": args.nlvls,
                    "l2": "state history %.1f GB > 129 MB L2; 256 MB L2 flush between timed iterations"

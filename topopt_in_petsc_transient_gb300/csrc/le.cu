@@ -248,17 +248,27 @@ constexpr int tile_class() {
                                                                                                : -1;
 }
 
+// FP32 tile kernels are persistent: as many CTAs as are resident on the device
+// at once (occupancy of this instantiation x SM count), capped by the brick
+// count; the others launch one CTA per brick
 template <class T, class Pol>
 static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, cudaStream_t s) {
-    static bool attr = false;
+    static int resident = 0;
     const size_t sm = tile_smem_bytes<T, Pol>();
-    if (!attr) {
+    if (!resident) {
         cudaFuncSetAttribute(k_tile<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        attr = true;
+        int dev = 0, nsm = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<T, Pol>, TILE_THREADS, sm);
+        resident = std::max(1, per_sm) * std::max(1, nsm);
     }
+    int ntx, nty;
+    const int ntiles = tile_count(g, ntx, nty);
     const bool timed = tile_class<T, Pol>() >= 0 && timer_begin(tile_class<T, Pol>(), g.nn(), s);
     count_launch();
-    k_tile<T, Pol><<<tile_grid(g), TILE_THREADS, sm, s>>>(g, C, pol);
+    const int grid = tile_persistent<T>() ? std::min(ntiles, resident) : ntiles;
+    k_tile<T, Pol><<<(unsigned)grid, TILE_THREADS, sm, s>>>(g, C, pol);
     timer_end(timed, s);
 }
 

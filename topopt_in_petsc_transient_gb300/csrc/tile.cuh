@@ -31,8 +31,10 @@ constexpr size_t tile_smem_bytes() {
     return sizeof(T) * ((size_t)Pol::NIN * TILE_STAGED * 3 + (size_t)TILE_THREADS * EL_STRIDE);
 }
 
-__host__ inline dim3 tile_grid(const GridDesc &g) {
-    return dim3((g.nx + TILE - 1) / TILE, (g.ny + TILE - 1) / TILE, (g.nz + TILE - 1) / TILE);
+__host__ __device__ inline int tile_count(const GridDesc &g, int &ntx, int &nty) {
+    ntx = (g.nx + TILE - 1) / TILE;
+    nty = (g.ny + TILE - 1) / TILE;
+    return ntx * nty * ((g.nz + TILE - 1) / TILE);
 }
 
 // Policy interface:
@@ -79,42 +81,56 @@ __device__ __forceinline__ void pol_epi(const P &p, long long n, int i, int j, i
     p.epilogue(n, i, j, k, y, red);
 }
 
+// staged input nodes of brick `tile` held by this thread (at most two)
 template <class T, class Pol>
-__global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(const GridDesc g, const ElemConst<T> C, const Pol pol) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *sIn = reinterpret_cast<T *>(smem_raw);
-    T *sEl = sIn + Pol::NIN * TILE_STAGED * 3;
-    const int tid = threadIdx.x;
-    const int i0 = blockIdx.x * TILE, j0 = blockIdx.y * TILE, k0 = blockIdx.z * TILE;
-    if (pol_skip(pol, 0)) return;
-
-    // ---- stage inputs (brick + halo), zero outside the domain: every
-    // thread issues its (at most two) node loads before any shared store ----
-    static_assert(TILE_STAGED <= 2 * TILE_THREADS, "staging assumes two passes");
-    {
-        T v[2][Pol::NIN][3];
+__device__ __forceinline__ void tile_fetch(const Pol &pol, const GridDesc &g, int tile, int ntx, int nty,
+                                           T v[2][Pol::NIN][3]) {
+    const int i0 = (tile % ntx) * TILE, j0 = ((tile / ntx) % nty) * TILE, k0 = (tile / (ntx * nty)) * TILE;
 #pragma unroll
-        for (int it = 0; it < 2; it++) {
-            const int s = tid + it * TILE_THREADS;
-            const int lx = s % TILE_N, ly = (s / TILE_N) % TILE_N, lz = s / (TILE_N * TILE_N);
-            const int gi = i0 - 1 + lx, gj = j0 - 1 + ly, gk = k0 - 1 + lz;
-            if (s < TILE_STAGED && gi >= 0 && gi < g.nx && gj >= 0 && gj < g.ny && gk >= 0 && gk < g.nz) {
-                long long n = gi + (long long)g.nx * (gj + (long long)g.ny * gk);
-                pol.load(n, v[it]);
-            } else {
+    for (int it = 0; it < 2; it++) {
+        const int s = threadIdx.x + it * TILE_THREADS;
+        const int lx = s % TILE_N, ly = (s / TILE_N) % TILE_N, lz = s / (TILE_N * TILE_N);
+        const int gi = i0 - 1 + lx, gj = j0 - 1 + ly, gk = k0 - 1 + lz;
+        if (s < TILE_STAGED && gi >= 0 && gi < g.nx && gj >= 0 && gj < g.ny && gk >= 0 && gk < g.nz) {
+            long long n = gi + (long long)g.nx * (gj + (long long)g.ny * gk);
+            pol.load(n, v[it]);
+        } else {
 #pragma unroll
-                for (int f = 0; f < Pol::NIN; f++) v[it][f][0] = v[it][f][1] = v[it][f][2] = T(0);
-            }
+            for (int f = 0; f < Pol::NIN; f++) v[it][f][0] = v[it][f][1] = v[it][f][2] = T(0);
         }
+    }
+}
+
+// FP32 kernels are persistent: the grid holds as many CTAs as fit on the
+// device, each CTA walks the bricks tile = blockIdx.x, + gridDim.x, ... and
+// loads the next brick's staged nodes into registers while it computes the
+// current one, so the global-load latency of the staging overlaps the element
+// arithmetic.  Reductions accumulate over a CTA's bricks in a fixed order and
+// are reduced once over the grid.  FP64 and double-float kernels (one CTA of
+// 128 registers a thread per SM) launch one CTA per brick: holding the next
+// brick's values would spill.
+template <class T>
+constexpr bool tile_persistent() {
+    return sizeof(T) == 4;
+}
+// one brick: stage (v holds its staged nodes), element phase, gather and
+// epilogue; with `next` >= 0 the staged nodes of brick `next` are loaded into
+// v while this brick is computed
+template <class T, class Pol>
+__device__ __forceinline__ void tile_brick(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, T *sIn, T *sEl,
+                                           int tile, int next, int ntx, int nty, T v[2][Pol::NIN][3],
+                                           double *red) {
+    const int tid = threadIdx.x;
+    const int i0 = (tile % ntx) * TILE, j0 = ((tile / ntx) % nty) * TILE, k0 = (tile / (ntx * nty)) * TILE;
+    // ---- staged inputs (brick + halo, zero outside the domain) to shared memory ----
 #pragma unroll
-        for (int it = 0; it < 2; it++) {
-            const int s = tid + it * TILE_THREADS;
-            if (s < TILE_STAGED) {
+    for (int it = 0; it < 2; it++) {
+        const int s = tid + it * TILE_THREADS;
+        if (s < TILE_STAGED) {
 #pragma unroll
-                for (int f = 0; f < Pol::NIN; f++)
+            for (int f = 0; f < Pol::NIN; f++)
 #pragma unroll
-                    for (int c = 0; c < 3; c++) sIn[(f * TILE_STAGED + s) * 3 + c] = v[it][f][c];
-            }
+                for (int c = 0; c < 3; c++) sIn[(f * TILE_STAGED + s) * 3 + c] = v[it][f][c];
         }
     }
     // output node of this thread and its prefetched epilogue operands
@@ -124,6 +140,7 @@ __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(c
     const long long on = has_out ? oi + (long long)g.nx * (oj + (long long)g.ny * ok) : 0;
     const auto pre = pol_pre(pol, on, 0);
     __syncthreads();
+    if (next >= 0) tile_fetch<T>(pol, g, next, ntx, nty, v);
 
     // ---- one element per thread ----
     {
@@ -193,9 +210,6 @@ __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(c
     __syncthreads();
 
     // ---- gather + policy epilogue ----
-    double red[Pol::NRED > 0 ? Pol::NRED : 1];
-#pragma unroll
-    for (int r = 0; r < (Pol::NRED > 0 ? Pol::NRED : 1); r++) red[r] = 0.0;
     if (has_out) {
         T y[3] = {T(0), T(0), T(0)};
 #pragma unroll
@@ -206,6 +220,32 @@ __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(c
             for (int c = 0; c < 3; c++) y[c] += sEl[le * EL_STRIDE + L * 3 + c];
         }
         pol_epi(pol, on, oi, oj, ok, y, red, pre, 0);
+    }
+}
+
+template <class T, class Pol>
+__global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(const GridDesc g, const ElemConst<T> C, const Pol pol) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sIn = reinterpret_cast<T *>(smem_raw);
+    T *sEl = sIn + Pol::NIN * TILE_STAGED * 3;
+    if (pol_skip(pol, 0)) return;
+    static_assert(TILE_STAGED <= 2 * TILE_THREADS, "staging assumes two passes");
+    int ntx, nty;
+    const int ntiles = tile_count(g, ntx, nty);
+    double red[Pol::NRED > 0 ? Pol::NRED : 1];
+#pragma unroll
+    for (int r = 0; r < (Pol::NRED > 0 ? Pol::NRED : 1); r++) red[r] = 0.0;
+    T v[2][Pol::NIN][3];
+    if constexpr (tile_persistent<T>()) {
+        if ((int)blockIdx.x < ntiles) tile_fetch<T>(pol, g, blockIdx.x, ntx, nty, v);
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            const int next = tile + (int)gridDim.x < ntiles ? tile + (int)gridDim.x : -1;
+            tile_brick<T>(g, C, pol, sIn, sEl, tile, next, ntx, nty, v, red);
+            __syncthreads();  // shared memory is restaged for the next brick
+        }
+    } else {
+        tile_fetch<T>(pol, g, blockIdx.x, ntx, nty, v);
+        tile_brick<T>(g, C, pol, sIn, sEl, blockIdx.x, -1, ntx, nty, v, red);
     }
     if constexpr (Pol::NRED > 0) {
         double tot[Pol::NRED];
