@@ -346,6 +346,8 @@ def run_e2e(args, wl, flush_l2):
         flush_l2()
         t0 = time.perf_counter()
         ph.CompleteInitialState(xP, o.Emin, o.Emax, o.Rmin, o.Rmax, o.penalK, o.penalM)
+        if o.ncp > 1:  # main.cc:84-86
+            ph.GenerateCheckPoints()
         fx = ph.ComputeObjectiveSensitivities(df)
         gx = ph.VolumeConstraint(dg, xP, o.volfrac)
         filt.Gradients(x, xT, df, 1, dg, False, o.beta, o.eta)

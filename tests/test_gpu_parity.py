@@ -297,6 +297,15 @@ def test_solver_failures_are_reported(gpu):
     with pytest.raises(TopoError) as e:
         le.GenerateCheckPoints()  # before CompleteInitialState
     assert e.value.status == 7
+    # with ncp > 1 the reverse sweep restarts from checkpoints of this design:
+    # sensitivities without GenerateCheckPoints are refused, not computed from
+    # stale checkpoints (main.cc:84-90 calls it between the two)
+    le.CompleteInitialState(np.full(128, 0.3), *M6)
+    with pytest.raises(TopoError) as e:
+        le.ComputeObjectiveSensitivities(np.zeros(128))
+    assert e.value.status == 7
+    le.GenerateCheckPoints()
+    le.ComputeObjectiveSensitivities(np.zeros(128))
     # an iteration cap of 1 must surface as "not converged", not as a wrong answer
     le = _le((8, 4, 4), nlvls=2, ncp=2, tsc=2, t1=0.2, loadsignal=1, maxit=1, rtol=1e-14)
     x = np.full(128, 0.3)

@@ -394,6 +394,9 @@ struct TopoLE {
     LEStats stats;
     int last_block_resident = -1;
     int design_ready = 0;
+    // checkpoints 1..ncp-1 belong to the current design (GenerateCheckPoints
+    // ran after the last CompleteInitialState; always true for ncp = 1)
+    int checkpoints_ready = 0;
 };
 
 static Partials<1> P1(TopoLE *le) { return Partials<1>{le->part, le->counter}; }
@@ -2047,6 +2050,7 @@ int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, 
     rc = check_err(le);
     if (rc) return rc;
     le->design_ready = 1;
+    le->checkpoints_ready = le->p.ncp <= 1;
     le->last_block_resident = -1;
     return TOPO_OK;
 }
@@ -2070,6 +2074,7 @@ int le_generate_checkpoints(TopoLE *le) {
                            cudaMemcpyDeviceToDevice, le->stream));
     }
     le->last_block_resident = le->p.ncp - 1;
+    le->checkpoints_ready = 1;
     return check_err(le);
 }
 
@@ -2079,6 +2084,10 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
         return TOPO_ERR_STATE;
     }
     if (le->kb) return sommg_objective_sensitivities(le, fx, dfdx_dev);
+    if (!le->checkpoints_ready) {  // the reverse sweep restarts blocks from checkpoints 1..ncp-1
+        set_error("ComputeObjectiveSensitivities with ncp > 1 needs GenerateCheckPoints after CompleteInitialState");
+        return TOPO_ERR_STATE;
+    }
     cudaStream_t s = le->stream;
     long long nd = le->ndof;
     CK(cudaMemsetAsync(le->df, 0, sizeof(double) * le->nel, s));
