@@ -31,7 +31,15 @@ METRIC = "forward+adjoint design iters/s on 1 GB300: mixed vs plain FP64 at equa
 
 # DRAM bytes (read + write) per launch from ncu captures summarised under
 # profiles/, keyed by (mesh, kernel name); absent pairs report null
-TRAFFIC = {}
+# DRAM bytes (read + write) per launch of the roofline kernel classes, from
+# one `ncu --set full` capture of each pass on the named mesh (mean over the
+# three Kronecker passes); below the algorithmic bytes where vectors stay in L2
+TRAFFIC = {
+    ("96x48x48", "k_kron_pass<float>"): (5.624e6 + 2.819e6 + 11.22e6) / 3.0,
+    ("96x48x48", "k_tile<float,PolPQ32>"): 7.627e6,
+    ("192x96x96", "k_kron_pass<float>"): (43.62e6 + 0.437e6 + 21.82e6 + 87.26e6 + 5.977e6) / 3.0,
+    ("192x96x96", "k_tile<float,PolPQ32>"): 59.60e6 + 6.723e6,
+}
 UNIT = "design_iter/s"
 
 
@@ -270,14 +278,14 @@ def run_gb300(args):
         ach = nbytes / (ms_launch * 1e-3) / 1e9
         kern.append({"kernel": name, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": ach / peaks["hbm_gbs"], "ms_per_launch": ms_launch, "launches_timed": nlaunch.value,
-                     "ms_per_design_iter": tot_ms.value, "algorithmic_bytes": nbytes})
+                     "ms_per_design_iter": tot_ms.value, "algorithmic_bytes": nbytes,
+                     "traffic": TRAFFIC.get((args.mesh, name.split(" ")[0]))})
     ms_fp64 = C.c_double()
     _lib.check(L.topo_le_time_apply(probe.physics._h, 0, 5, 50, C.byref(ms_fp64)), "time_apply")
     del probe
     kern.sort(key=lambda k: -k["ms_per_design_iter"])
     roof = dict(kern[0]) if kern else {"kernel": None}
-    roof.update({"traffic": TRAFFIC.get((args.mesh, (roof.get("kernel") or "").split(" ")[0])),
-                 "peak_source": peaks["source"],
+    roof.update({"peak_source": peaks["source"],
                  "timing": "CUDA events around every launch of the class in one design iteration, library stream",
                  "other_kernels": kern[1:],
                  "fp64_apply": {"kernel": "k_tile<double,PolResid>", "ms_per_launch": ms_fp64.value,
