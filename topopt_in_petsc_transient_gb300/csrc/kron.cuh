@@ -155,8 +155,16 @@ __host__ inline int kx_lines(const GridDesc &g, size_t elem) {
     int L = (int)((size_t)(48 * 1024) / per_line);
     return L < 1 ? 1 : (L > 8 ? 8 : L);
 }
-__host__ inline size_t kron_x_smem(const GridDesc &g, size_t elem) {
-    return elem * ((size_t)kx_lines(g, elem) * 2 * 3 * kx_pitch(g.nx) + 3 * KRON_W);
+__host__ inline size_t kron_x_smem(const GridDesc &g, size_t elem, int kx = 0) {
+    return elem * ((size_t)(kx > 0 ? kx : kx_lines(g, elem)) * 2 * 3 * kx_pitch(g.nx) + 3 * KRON_W);
+}
+// lines per CTA for a launch: the shared-memory cap, lowered so that the grid
+// still fills one wave of `slots` resident CTAs
+__host__ inline int kx_lines_launch(const GridDesc &g, size_t elem, long long slots) {
+    const long long nlines = (long long)g.ny * g.nz;
+    const long long want = (nlines + slots - 1) / slots;
+    const int cap = kx_lines(g, elem);
+    return (int)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
 template <class T, class R>
@@ -229,7 +237,7 @@ __host__ inline size_t kron_yz_smem(const GridDesc &g, int axis, size_t elem, bo
 }
 
 template <class T, class R, int AXIS, bool DOT>
-static __global__ void __launch_bounds__(KRON_THREADS)
+static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
     k_kron_yz(GridDesc g, const R *__restrict__ r, const T *__restrict__ ms, KronBand<T> B, const T *__restrict__ in,
               T *out, KronDot kd) {
     extern __shared__ __align__(16) unsigned char kron_smem[];

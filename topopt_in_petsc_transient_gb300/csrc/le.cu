@@ -1000,8 +1000,15 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     const T *sc = kron_scale<T>(le->ops[o]);
     const bool mixed = fz && std::is_same<T, float>::value;
     const long long nlines = (long long)g.ny * g.nz;
-    const int kx = kx_lines(g, sizeof(T));
-    const size_t smx = kron_x_smem(g, sizeof(T)), smy = kron_yz_smem(g, 1, sizeof(T));
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        nsm = std::max(nsm, 1);
+    }
+    const int kx = kx_lines_launch(g, sizeof(T), 4LL * nsm);  // 4 resident CTAs of the x pass per SM
+    const size_t smx = kron_x_smem(g, sizeof(T), kx), smy = kron_yz_smem(g, 1, sizeof(T));
     static bool attr = false;
     if (!attr) {  // staged lines: the selection keeps every pass within KRON_SMEM_MAX
         cudaFuncSetAttribute(k_kron_x<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
