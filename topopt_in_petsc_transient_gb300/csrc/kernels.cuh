@@ -440,14 +440,36 @@ static __global__ void k_mfcg_dot(long long ndof, const float *__restrict__ z, c
 
 // p is double-buffered (PolPQ32 reads the previous p from pb[it & 1] and
 // writes the new one to pb[(it + 1) & 1])
-static __global__ void k_mfcg_update(long long ndof, double *x, float *r32, const float *pb0, const float *pb1,
-                                     const float *__restrict__ q, SolveScalars *S, Partials<1> part) {
+static __global__ void k_mfcg_update(long long ndof, double *__restrict__ x, float *__restrict__ r32,
+                                     const float *pb0, const float *pb1, const float *__restrict__ q, SolveScalars *S,
+                                     Partials<1> part) {
     const float *__restrict__ p = ((S->it + 1) & 1) ? pb1 : pb0;
     double alpha = S->alpha;
     float af = (float)alpha;
     double ax = alpha / S->sigma;  // correction in unscaled units
     float s = 0.0f;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+    // four grid strides per trip: all loads of a trip are issued before its stores
+    const long long st = (long long)gridDim.x * blockDim.x;
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i + 3 * st < ndof; i += 4 * st) {
+        double xv[4];
+        float pv[4], rv[4], qv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            xv[u] = x[i + u * st];
+            pv[u] = p[i + u * st];
+            rv[u] = r32[i + u * st];
+            qv[u] = q[i + u * st];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            x[i + u * st] = xv[u] + ax * (double)pv[u];
+            const float r = rv[u] - af * qv[u];
+            r32[i + u * st] = r;
+            s += r * r;
+        }
+    }
+    for (; i < ndof; i += st) {
         x[i] += ax * (double)p[i];
         float rv = r32[i] - af * q[i];
         r32[i] = rv;
