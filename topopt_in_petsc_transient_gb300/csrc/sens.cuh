@@ -121,14 +121,14 @@ static __global__ void k_adj_combine(AdjCombine A) {
                 if (w3 != 0.0) g += w3 * A.Lp3[i];
                 A.x0[i] = fx ? 0.0 : g;
                 if (A.ax0) {
-                    double kx = w1 * A.KL[i], mx = w1 * A.ML[i];
-                    if (w2 != 0.0) {
-                        kx += w2 * A.KLh1[i];
-                        mx += w2 * A.MLh1[i];
-                    }
-                    if (w3 != 0.0) {
-                        kx += w3 * A.KLh2[i];
-                        mx += w3 * A.MLh2[i];
+                    double mx = w1 * A.ML[i];
+                    if (w2 != 0.0) mx += w2 * A.MLh1[i];
+                    if (w3 != 0.0) mx += w3 * A.MLh2[i];
+                    double kx = 0.0;
+                    if (A.sK != 0.0) {  // mixed path: the ML slots hold A L and sK = 0
+                        kx = w1 * A.KL[i];
+                        if (w2 != 0.0) kx += w2 * A.KLh1[i];
+                        if (w3 != 0.0) kx += w3 * A.KLh2[i];
                     }
                     A.ax0[i] = fx ? 0.0 : A.sK * kx + A.sM * mx;
                 }
