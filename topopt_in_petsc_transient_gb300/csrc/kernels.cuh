@@ -125,6 +125,17 @@ static __global__ void k_dinv(GridDesc g, const uint8_t *__restrict__ fixed, con
 // lambda_min(Dinv A) >= min_{e,i} cm lamMlo dM / (ck dK_i + cm dM)  (lamK_min = 0).
 // Non-negative doubles order like their bit patterns, so atomicMax/Min on the
 // bits is exact and order independent.
+// order-preserving map of doubles to unsigned integers (negative values
+// included), so that atomicMin / atomicMax on the image order like the values
+__device__ __forceinline__ unsigned long long ord_bits(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord_value(unsigned long long u) {
+    const unsigned long long b = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+    return __longlong_as_double((long long)b);
+}
+
 static __global__ void k_bounds(long long nel, const double *__restrict__ kf, const double *__restrict__ mf, double sK,
                          double sM, double dK0, double dK1, double dK2, double dM, double lamK, double lamMlo,
                          double lamMhi, unsigned long long *bits /* [0]=max hi, [1]=min lo */) {
@@ -146,30 +157,35 @@ static __global__ void k_bounds(long long nel, const double *__restrict__ kf, co
         hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
         lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
     }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMax(&bits[0], (unsigned long long)__double_as_longlong(hi));
-        atomicMin(&bits[1], (unsigned long long)__double_as_longlong(lo));
+    if ((threadIdx.x & 31) == 0) {  // lo is negative for the shifted operator K - om^2 M
+        atomicMax(&bits[0], ord_bits(hi));
+        atomicMin(&bits[1], ord_bits(lo));
     }
 }
 
 static __global__ void k_bounds_init(unsigned long long *bits) {
-    bits[0] = 0ull;
-    bits[1] = (unsigned long long)__double_as_longlong(1e300);
+    bits[0] = ord_bits(0.0);
+    bits[1] = ord_bits(1e300);
 }
 
 // Chebyshev interval: [max(lo_bound, hi/ratio), hi]; the Dirichlet identity
 // rows contribute eigenvalue 1 and are kept inside the interval.
 // lohi[0..1]: smoothing interval, lohi[2..3]: full-spectrum bounds
+// lohi[4]: the element-wise lower bound itself.  A bound <= 0 (it cannot show
+// the shifted operator K - om^2 M positive) keeps the level out of the
+// well-conditioned test, and the full-spectrum table then uses the smoothing
+// interval.
 static __global__ void k_bounds_final(const unsigned long long *bits, double ratio, double *lohi) {
-    double hi = __longlong_as_double((long long)bits[0]);
-    double lo = __longlong_as_double((long long)bits[1]);
+    double hi = ord_value(bits[0]);
+    double lo = ord_value(bits[1]);
     hi = fmax(hi, 1.0);
     double l = fmax(lo, hi / ratio);
     l = fmin(l, 1.0);
     lohi[0] = l;
     lohi[1] = hi;
-    lohi[2] = fmin(lo, 1.0);
+    lohi[2] = lo > 0.0 ? fmin(lo, 1.0) : l;
     lohi[3] = hi;
+    lohi[4] = lo;
 }
 
 // first Chebyshev step from a zero initial guess: d = Dinv b / theta, x = d

@@ -298,10 +298,10 @@ struct Level {
 struct OpLevel {
     double *dinvd = nullptr;
     float *dinvf = nullptr;
-    double *lohi = nullptr;  // device [2]
+    double *lohi = nullptr;  // device [5]: smoothing interval, full-spectrum interval, raw lower bound
     double *cheb = nullptr;   // device [kmax][2] Chebyshev step coefficients (smoothing)
     double *chebf = nullptr;  // same over the full spectrum (smoother-as-solver level)
-    double hlohi[4] = {0, 0, 0, 0};
+    double hlohi[5] = {0, 0, 0, 0, 0};
 };
 
 struct Operator {
@@ -735,7 +735,7 @@ int le_alloc(TopoLE *le) {
             long long lnd = 3 * le->L[l].g.nn();
             AG(op.lv[l].dinvd, lnd);
             AG(op.lv[l].dinvf, lnd);
-            AG(op.lv[l].lohi, 4);
+            AG(op.lv[l].lohi, 5);
             AG(op.lv[l].cheb, 2 * 64);
             AG(op.lv[l].chebf, 2 * 64);
         }
@@ -820,12 +820,12 @@ static int setup_operator(TopoLE *le, int o) {
     op.depth = le->nlev;
     if (le->p.adaptive_kappa > 0.0) {
         for (int l = 0; l < le->nlev; l++) {
-            CK(cudaMemcpyAsync(op.lv[l].hlohi, op.lv[l].lohi, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(op.lv[l].hlohi, op.lv[l].lohi, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
         }
         CK(cudaStreamSynchronize(s));
         for (int l = 0; l < le->nlev - 1; l++) {
             const double *hb = op.lv[l].hlohi;
-            if (hb[2] > 0.0 && hb[3] / hb[2] <= le->p.adaptive_kappa) {
+            if (hb[4] > 0.0 && hb[3] / hb[2] <= le->p.adaptive_kappa) {
                 op.depth = l + 1;
                 break;
             }
