@@ -288,6 +288,21 @@ def test_mma_matches_oracle(gpu):
         assert _rel(xg.cpu().numpy(), xo) < 1e-10, it
 
 
+def test_sommg_basis_solves_descend_the_multigrid_hierarchy(gpu):
+    # the shifted operator K - om^2 M has negative element-wise lower bounds;
+    # they must not make the V-cycle stop at the fine level (a one-level
+    # Chebyshev solve took 86 FCG iterations per basis solve on this mesh,
+    # the full V-cycle about 12)
+    n = (48, 24, 24)
+    le = _le(n, nlvls=4, ncp=1, tsc=10, t1=0.05, objective=3, loadsignal=1, dalpha=0.0, dbeta=1e-3, mixed=False,
+             rtol=1e-10, reduction=1, basis=4, omega0=1e-4)
+    s0 = le.stats()
+    le.CompleteInitialState(np.full(np.prod(n), 0.12), *M6)
+    s1 = le.stats()
+    its = (s1["cg_iterations"] - s0["cg_iterations"]) / (s1["solves"] - s0["solves"])
+    assert its < 25
+
+
 def test_solver_failures_are_reported(gpu):
     from topopt_in_petsc_transient_gb300 import TopoError
     with pytest.raises(TopoError) as e:

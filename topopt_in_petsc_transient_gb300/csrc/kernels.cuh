@@ -123,8 +123,9 @@ static __global__ void k_dinv(GridDesc g, const uint8_t *__restrict__ fixed, con
 // x'Ax = sum_e x_e'(ck KE + cm ME)x_e <= sum_e sum_i x_ei^2 (ck lamK dK_i + cm lamM dM)
 // so lambda_max(Dinv A) <= max_{e,i} (ck lamK dK_i + cm lamMhi dM)/(ck dK_i + cm dM),
 // lambda_min(Dinv A) >= min_{e,i} cm lamMlo dM / (ck dK_i + cm dM)  (lamK_min = 0).
-// Non-negative doubles order like their bit patterns, so atomicMax/Min on the
-// bits is exact and order independent.
+// The lower bound is negative for a negative mass coefficient (the shifted
+// operator K - om^2 M), so the atomics act on an order-preserving image of the
+// doubles (exact and order independent).
 // order-preserving map of doubles to unsigned integers (negative values
 // included), so that atomicMin / atomicMax on the image order like the values
 __device__ __forceinline__ unsigned long long ord_bits(double v) {
