@@ -632,6 +632,47 @@ static __global__ void k_fwd_prep(long long ndof, const double *__restrict__ u, 
                  AAprev ? AAprev[i] : 0.0, P);
 }
 
+// Mixed forward step, after the K-only double-float product y = K KS:
+// b = f(t) + BT + y and r0 = b - A x0 on free DOFs (0 on clamped ones), b.b,
+// r.r and the FCG set-up; BT arrives in b and A x0 in r (k_newmark_track /
+// k_fwd_prep).  x0 is never accepted without a true residual: A u+ = b - r
+// must hold for the stored u+ and r0 rests on tracked products.  A streaming
+// kernel at full occupancy: the tile kernel's epilogue runs one CTA per SM in
+// double-float (SolveStateBlock, LinearElasticity.cc:1317-1361).
+struct RhsLoad {
+    const double *rhs0;
+    double load_scale;
+    int loadsignal;
+    long long load2_dof;
+    double load2_phase;
+};
+static __global__ void k_rhs_finish(long long ndof, const uint8_t *__restrict__ fixed, const double *__restrict__ y,
+                                    RhsLoad L, const StepCtx *st, double *__restrict__ b, double *__restrict__ r,
+                                    SolveScalars *S, cudaGraphConditionalHandle cond, int has_cond, Partials<2> part) {
+    const int t = st->tsc * st->block + st->j + 1;
+    const double time = t * st->dt;
+    const double s = load_signal(L.loadsignal, time) * L.load_scale;
+    double red[2] = {0.0, 0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        const long long n = i / 3;
+        const int c = (int)(i - 3 * n);
+        if ((fixed[n] >> c) & 1) {
+            b[i] = 0.0;
+            r[i] = 0.0;
+            continue;
+        }
+        const double f2 = (i == L.load2_dof) ? load2_signal(L.load2_phase, time) * L.load_scale : 0.0;
+        const double bv = L.rhs0[i] * s + f2 + b[i] + y[i];
+        const double rv = bv - r[i];
+        b[i] = bv;
+        r[i] = rv;
+        red[0] += bv * bv;
+        red[1] += rv * rv;
+    }
+    double tot[2];
+    if (grid_reduce<EW, 2>(red, part, tot)) init_finish(S, tot, true, cond, has_cond, false);
+}
+
 static __global__ void k_step_set(StepCtx *st, int block, int j) {
     st->block = block;
     st->j = j;

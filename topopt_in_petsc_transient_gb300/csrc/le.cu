@@ -339,7 +339,7 @@ struct TopoLE {
     // mixed forward sweep: tracked products A u-, A du-, A ddu- of the
     // previous state, AApt scratch for A ddu-- when re-anchoring, KSt the
     // next step's K-pass input; fwd_init_pending: the next solve's initial
-    // residual comes from the fused right-hand-side pass (PolRhsInit)
+    // residual comes from the K-only right-hand-side pass (fwd_rhs_init)
     double *AUt = nullptr, *AVt = nullptr, *AAt = nullptr, *AApt = nullptr, *KSt = nullptr;
     bool fwd_init_pending = false;
     int kb = 0;
@@ -1349,36 +1349,27 @@ static FwdPrep fwd_prep_args(TopoLE *le) {
     return P;
 }
 
-// mixed path only (tracked products exist only there); the K-only pass stays
-// FP64-accurate: K applied to the near-rigid local motion of the state cancels
-// strongly, and FP32 rounding of that product puts noise into b above the
-// solve tolerance (measured: 4.3 instead of 2.8 Krylov iterations per solve on
-// the 96x48x48 cantilever)
-static void fwd_rhs_init(TopoLE *le, cudaGraphConditionalHandle cond, int has_cond) {
-    const LEParams &p = le->p;
-    Level &l0 = le->L[0];
-    PolRhsInit<df> pr;
-    memset(&pr, 0, sizeof(pr));
-    pr.fixed = l0.fixed;
-    pr.w = fine_weights<df>(le, true, false, nullptr, 1.0, 0.0);
-    pr.KS = le->KSt;
-    pr.rhs0 = le->rhs0;
-    pr.load_scale = 1.0 / (p.ny - 1);
-    pr.loadsignal = p.loadsignal;
-    pr.load2_dof = p.load2_node >= 0 ? 3LL * p.load2_node + 2 : -1;
-    pr.load2_phase = p.load2_phase;
-    pr.st = le->st;
-    pr.b = le->sb;
-    pr.r = le->sr;
-    pr.S = le->S;
-    pr.cond = cond;
-    pr.has_cond = has_cond;
-    pr.part = P2(le);
-    launch_tile<df>(l0.g, fine_const<df>(le), pr, le->stream);
-}
-
 template <bool HK, bool HM>
 static void product(TopoLE *le, const double *x, double *y, const double *P, double sK, double sM);
+template <class A, bool HK, bool HM>
+static void product_t(TopoLE *le, const double *x, double *y, const double *P, double sK, double sM);
+
+// Mixed path only (tracked products exist only there): y = K KS in one K-only
+// double-float pass (FP32 rounding of K applied to the near-rigid local motion
+// of the state would put noise into b above the solve tolerance: measured 4.3
+// instead of 2.8 Krylov iterations per solve on the 96x48x48 cantilever), then
+// b, r0 and the FCG set-up in a streaming kernel
+static void fwd_rhs_init(TopoLE *le, cudaGraphConditionalHandle cond, int has_cond) {
+    const LEParams &p = le->p;
+    product_t<df, true, false>(le, le->KSt, le->sq, nullptr, 1.0, 0.0);
+    RhsLoad L{le->rhs0, 1.0 / (p.ny - 1), p.loadsignal, p.load2_node >= 0 ? 3LL * p.load2_node + 2 : -1,
+              p.load2_phase};
+    count_launch();
+    k_rhs_finish<<<red_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, le->L[0].fixed, le->sq, L, le->st, le->sb,
+                                                               le->sr, le->S, cond, has_cond, P2(le));
+}
+
+
 // tracked products A u, A du, A ddu of a block's start state (checkpoint c),
 // then the first step's preparation
 static void track_block_start(TopoLE *le, int c) {
@@ -1415,8 +1406,8 @@ static void track_anchor(TopoLE *le, int c, int j) {
                                                       fwd_prep_args(le));
 }
 
-// Mixed path: right-hand side and initial residual in one K-only pass
-// (PolRhsInit) from what the previous corrector prepared; the corrector
+// Mixed path: right-hand side and initial residual from one K-only pass and a
+// streaming kernel (fwd_rhs_init) on what the previous corrector prepared; the corrector
 // tracks the products of the new state and prepares the next step
 // (k_newmark_track).  Plain FP64 path: right-hand side from the stored
 // states, the initial residual b - A x0, the corrector.

@@ -485,7 +485,7 @@ __device__ __forceinline__ double load_signal(int which, double t) {
 //   b = N (f(t) + B1 u- + B2 du- + B3 ddu-),  B_i = N (cMi M + cKi K) N
 // staged as vK = sum cKi (u-,du-,ddu-)_i and vM = sum cMi (...)_i so that one
 // element pass gives K vK + M vM.  Also writes the initial guess x0 (the
-// Newmark predictor, see PolRhsInit).
+// Newmark predictor, see fwd_prep_args).
 // ---------------------------------------------------------------------------
 template <class T>
 struct PolRhsFwd {
@@ -559,70 +559,6 @@ struct PolRhsFwd {
         }
     }
     __device__ void finish(const double *) const {}
-};
-
-// ---------------------------------------------------------------------------
-// Forward step right-hand side and initial residual in one K-only pass
-// (mixed path).  With A = sK K + sM M the step operator and the tracked
-// products AS_i = A s_i of the previous state s = (u-, du-, ddu-),
-// M s_i = (AS_i - sK K s_i) / sM, so
-//   b = f + sum_i B_i s_i = f + sum_i (cM_i / sM) AS_i + K (sum_i c'_i s_i),
-//   c'_i = cK_i - cM_i sK / sM
-// (SolveStateBlock, LinearElasticity.cc:1317-1361).  The corrector of the
-// previous step (k_newmark_track, or k_fwd_prep at a block start) has left
-// KS = sum c'_i s_i, BT = sum (cM_i/sM) AS_i in b, the initial guess x0 (the
-// predictor) in x and A x0 (the predictor applied to the tracked products) in
-// r, so this pass forms b = f + BT + K KS and r0 = b - A x0 with b.b and r.r,
-// and sets up the FCG state.
-// ---------------------------------------------------------------------------
-template <class T>
-struct PolRhsInit {
-    static constexpr int NIN = 1, NRED = 2;
-    static constexpr bool HAS_K = true, HAS_M = false;
-    const uint8_t *fixed;
-    Weights<T> w;                       // kf, sK = 1
-    const double *KS;
-    const double *rhs0;
-    double load_scale;
-    int loadsignal;
-    long long load2_dof;
-    double load2_phase;
-    const StepCtx *st;
-    double *b, *r;                      // in: BT and A x0; out: b and r0
-    SolveScalars *S;
-    cudaGraphConditionalHandle cond;
-    int has_cond;
-    Partials<2> part;
-    __device__ void load(long long n, T v[1][3]) const {
-        v[0][0] = T(KS[3 * n]);
-        v[0][1] = T(KS[3 * n + 1]);
-        v[0][2] = T(KS[3 * n + 2]);
-        mask3(fixed[n], v[0]);
-    }
-    __device__ void coef(long long e, T &kc, T &mc) const { w.get(e, kc, mc); }
-    __device__ void epilogue(long long n, int, int, int, const T y[3], double red[2]) const {
-        const int t = st->tsc * st->block + st->j + 1;
-        const double s = load_signal(loadsignal, t * st->dt) * load_scale;
-        const uint8_t f = fixed[n];
-        for (int c = 0; c < 3; c++) {
-            const long long i = 3 * n + c;
-            if ((f >> c) & 1) {
-                b[i] = 0.0;
-                r[i] = 0.0;
-                continue;
-            }
-            const double f2 = (i == load2_dof) ? load2_signal(load2_phase, t * st->dt) * load_scale : 0.0;
-            const double bv = rhs0[i] * s + f2 + b[i] + todbl(y[c]);
-            const double rv = bv - r[i];
-            b[i] = bv;
-            r[i] = rv;
-            red[0] += bv * bv;
-            red[1] += rv * rv;
-        }
-    }
-    // x0 is never accepted without a true residual: A u+ = b - r must hold
-    // for the stored u+, and r0 here rests on the tracked products
-    __device__ void finish(const double t[2]) const { init_finish(S, t, true, cond, has_cond, false); }
 };
 
 }  // namespace topo
