@@ -219,21 +219,19 @@ struct PolPQ32 {
     }
 };
 
-// r = b - (N A N + I - N) x, FP64-accurate (T = double or double-float),
-// r32 = (float) r; runs only when a replacement is due; decides convergence
-// and drives the graph condition
+// Residual replacement of the mixed FCG, part 1: y = (N A N) x, FP64-accurate
+// (T = double-float), only when a replacement is due (the whole grid exits
+// otherwise); k_replace_finish forms r = b - (N A N + I - N) x, decides
+// convergence and drives the graph condition.
 template <class T>
-struct PolReplace {
-    static constexpr int NIN = 1, NRED = 1;
+struct PolReplaceProduct {
+    static constexpr int NIN = 1, NRED = 0;
     static constexpr bool HAS_K = true, HAS_M = true;
     const uint8_t *fixed;
     Weights<T> w;
-    const double *x, *b;
-    double *r;
-    float *r32;
-    SolveScalars *S;
-    cudaGraphConditionalHandle cond;
-    int has_cond;
+    const double *x;
+    double *y;
+    const SolveScalars *S;
     Partials<1> part;
     __device__ bool skip() const { return S->need_replace == 0; }
     __device__ void load(long long n, T v[1][3]) const {
@@ -243,36 +241,36 @@ struct PolReplace {
         mask3(fixed[n], v[0]);
     }
     __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
-    __device__ void epilogue(long long n, int, int, int, const T y[3], double red[1]) const {
-        uint8_t f = fixed[n];
-        for (int c = 0; c < 3; c++) {
-            double xv = x[3 * n + c];
-            double rv = b[3 * n + c] - (((f >> c) & 1) ? xv : todbl(y[c]));
-            r[3 * n + c] = rv;
-            red[0] += rv * rv;
-        }
+    __device__ void epilogue(long long n, int, int, int, const T yv[3], double *) const {
+        y[3 * n] = todbl(yv[0]);
+        y[3 * n + 1] = todbl(yv[1]);
+        y[3 * n + 2] = todbl(yv[2]);
     }
-    __device__ void finish(const double t[1]) const {
-        S->rr = t[0];
-        S->need_replace = 0;
-        S->restart = 1;
-        S->inner_it = 0;
-        S->replacements += 1;
-        S->sigma = (t[0] > 0.0) ? sqrt(S->ndof / t[0]) : 1.0;
-        S->rr_ref = t[0] * S->sigma * S->sigma;
-        S->rescale = 1;
-        if (!isfinite(t[0])) {
-            S->status = TOPO_ERR_NAN;
-            S->done = 1;
-        } else if (t[0] <= S->tol2 * S->bb) {
-            S->done = 1;
-        } else if (S->it >= S->maxit) {
-            S->status = TOPO_ERR_NOT_CONVERGED;
-            S->done = 1;
-        }
-        if (has_cond) cudaGraphSetConditional(cond, S->done ? 0u : 1u);
-    }
+    __device__ void finish(const double *) const {}
 };
+
+// solver state after a residual replacement with true residual norm^2 rr
+__device__ __forceinline__ void replace_finish(SolveScalars *S, double rr, cudaGraphConditionalHandle cond,
+                                               int has_cond) {
+    S->rr = rr;
+    S->need_replace = 0;
+    S->restart = 1;
+    S->inner_it = 0;
+    S->replacements += 1;
+    S->sigma = (rr > 0.0) ? sqrt(S->ndof / rr) : 1.0;
+    S->rr_ref = rr * S->sigma * S->sigma;
+    S->rescale = 1;
+    if (!isfinite(rr)) {
+        S->status = TOPO_ERR_NAN;
+        S->done = 1;
+    } else if (rr <= S->tol2 * S->bb) {
+        S->done = 1;
+    } else if (S->it >= S->maxit) {
+        S->status = TOPO_ERR_NOT_CONVERGED;
+        S->done = 1;
+    }
+    if (has_cond) cudaGraphSetConditional(cond, S->done ? 0u : 1u);
+}
 
 // ---------------------------------------------------------------------------
 // Chebyshev-Jacobi smoothing step (one operator application):
