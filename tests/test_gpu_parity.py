@@ -134,6 +134,23 @@ def test_long_horizon_tracked_products(gpu, ncp, tsc, uniform):
     assert _rel(le.state(1, tsc - 1), DU) < 1e-6
 
 
+@pytest.mark.parametrize("objective,mixed", [(3, False), (3, True), (0, True), (4, False)])
+def test_backward_euler_integrator(gpu, objective, mixed):
+    # ti = 0: the reference's backward-Euler constants (LinearElasticity.cc:189-196)
+    # through the same forward/adjoint kernels
+    n = (8, 4, 4)
+    kw = dict(ncp=2, tsc=5, t1=0.5, ti=0, objective=objective, loadsignal=1, dalpha=0.01, dbeta=0.01)
+    rng = np.random.default_rng(30 + objective)
+    x = 0.1 + 0.5 * rng.random(np.prod(n))
+    le = _le(n, nlvls=2, mixed=mixed, rtol=1e-12, sens_fp32=False, **kw)
+    fx, df = _run_gpu(le, x)
+    ref = O.LinearElasticity(*n, **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert rc == 0
+    assert abs(fx - fx_r) <= 1e-10 * abs(fx_r), (fx, fx_r)
+    assert _rel(df, df_r) < 1e-9
+
+
 @pytest.mark.parametrize("objective", range(7))
 def test_fp32_sensitivities_every_objective(gpu, objective):
     # FP32 element math of the sensitivity kernel for every objective, on the
