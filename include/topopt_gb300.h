@@ -207,6 +207,29 @@ int topo_filter_gradients_dev(topo_pdefilt *f, const double *xTilde_dev, double 
 int topo_filter_mnd(topo_pdefilt *f, const double *x, double *mnd);
 int topo_filter_mnd_dev(topo_pdefilt *f, const double *x_dev, double *mnd);
 
+/* Filter (Filter.h:34-92) for filterType 0 (sensitivity filter) and 1
+ * (density filter): the distance-weighted element filter H of Filter::SetUp
+ * (Filter.cc:302-531; identity when its stencil ElemConn is 1) and Hs = H 1 */
+typedef struct topo_densfilt topo_densfilt;
+int topo_densfilt_create(topo_densfilt **out, int nelx, int nely, int nelz, double hx, double hy, double hz,
+                         int filter_type, double rmin);
+void topo_densfilt_destroy(topo_densfilt *f);
+/* Filter::FilterProject (Filter.cc:60-119): filter 1 xTilde = (H x) ./ Hs,
+ * filter 0 xTilde = x; then the optional smoothed Heaviside projection */
+int topo_densfilt_filter_project(topo_densfilt *f, const double *x, double *xTilde, double *xPhys, int projection,
+                                 double beta, double eta);
+int topo_densfilt_filter_project_dev(topo_densfilt *f, const double *x_dev, double *xTilde_dev, double *xPhys_dev,
+                                     int projection, double beta, double eta);
+/* Filter::Gradients (Filter.cc:122-206): projection chain rule, then
+ * filter 1: dfdx and dgdx[m*nel] <- H (v ./ Hs); filter 0: dfdx <- (H (dfdx .* x) ./ Hs) ./ x */
+int topo_densfilt_gradients(topo_densfilt *f, const double *x, const double *xTilde, double *dfdx, int m,
+                            double *dgdx, int projection, double beta, double eta);
+int topo_densfilt_gradients_dev(topo_densfilt *f, const double *x_dev, const double *xTilde_dev, double *dfdx_dev,
+                                int m, double *dgdx_dev, int projection, double beta, double eta);
+/* Filter::GetMND (Filter.cc:208-227) */
+int topo_densfilt_mnd(topo_densfilt *f, const double *x, double *mnd);
+int topo_densfilt_mnd_dev(topo_densfilt *f, const double *x_dev, double *mnd);
+
 /* MMA (MMA.h:9-120), design variables resident on the device */
 int topo_mma_create(topo_mma **out, int n, int m, const double *a, const double *c, const double *d);
 void topo_mma_destroy(topo_mma *mma);

@@ -57,6 +57,11 @@ def lib():
                                             C.c_double, C.c_double])
         L.oracle_filter_gradients.argtypes = ([C.c_int] * 3 + [C.c_double] * 4 + [dp, dp, C.c_int, dp, C.c_int,
                                               C.c_double, C.c_double, C.c_double])
+        L.oracle_dens_filter_apply.argtypes = [C.c_int] * 3 + [C.c_double] * 4 + [dp, dp]
+        L.oracle_dens_filter_project.argtypes = ([C.c_int] * 3 + [C.c_double] * 3 + [C.c_int, C.c_double] +
+                                                 [dp, dp, dp, C.c_int, C.c_double, C.c_double])
+        L.oracle_dens_filter_gradients.argtypes = ([C.c_int] * 3 + [C.c_double] * 3 + [C.c_int, C.c_double] +
+                                                   [dp, dp, dp, C.c_int, dp, C.c_int, C.c_double, C.c_double])
         L.oracle_filter_mnd.argtypes = [C.c_int, dp]
         L.oracle_filter_mnd.restype = C.c_double
         L.oracle_increase_beta.argtypes = [dp, C.c_double, C.c_double, C.c_int, C.c_double]
@@ -223,6 +228,37 @@ def filter_gradients(nelx, nely, nelz, xTilde, dfdx, dgdx, rmin, projection, bet
     m = dg.size // xt.size
     lib().oracle_filter_gradients(nelx + 1, nely + 1, nelz + 1, h[0], h[1], h[2], rmin, _p(xt), _p(df), m, _p(dg),
                                   int(projection), beta, eta, rtol)
+    return df, dg
+
+
+def dens_filter_apply(nelx, nely, nelz, v, R, h=(1.0, 1.0, 1.0)):
+    """H v of the filterType 0/1 filter (Filter.cc:302-531)."""
+    v = _f64(v)
+    out = np.zeros_like(v)
+    lib().oracle_dens_filter_apply(nelx, nely, nelz, h[0], h[1], h[2], R, _p(v), _p(out))
+    return out
+
+
+def dens_filter_project(nelx, nely, nelz, ftype, x, R, projection, beta, eta, h=(1.0, 1.0, 1.0)):
+    """Filter::FilterProject for filterType 0/1 (Filter.cc:60-119)."""
+    x = _f64(x)
+    xt = np.zeros_like(x)
+    xp = np.zeros_like(x)
+    lib().oracle_dens_filter_project(nelx, nely, nelz, h[0], h[1], h[2], ftype, R, _p(x), _p(xt), _p(xp),
+                                     int(projection), beta, eta)
+    return xt, xp
+
+
+def dens_filter_gradients(nelx, nely, nelz, ftype, x, xTilde, dfdx, dgdx, R, projection, beta, eta,
+                          h=(1.0, 1.0, 1.0)):
+    """Filter::Gradients for filterType 0/1 (Filter.cc:122-206)."""
+    x = _f64(x)
+    xt = _f64(xTilde)
+    df = _f64(dfdx).copy()
+    dg = _f64(dgdx).copy()
+    m = dg.size // xt.size
+    lib().oracle_dens_filter_gradients(nelx, nely, nelz, h[0], h[1], h[2], ftype, R, _p(x), _p(xt), _p(df), m,
+                                       _p(dg), int(projection), beta, eta)
     return df, dg
 
 

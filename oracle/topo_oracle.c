@@ -1031,6 +1031,96 @@ void oracle_filter_gradients(int nx, int ny, int nz, double hx, double hy, doubl
     free(tmp);
 }
 
+/* Filter::SetUp, filterType 0/1 (Filter.cc:302-531): out = H in.  The
+ * stencil half-width is ElemConn = max_a(ceil(R/h_a) - 1), at least 1; the
+ * neighbour range along axis a is [max(i - ElemConn, 0),
+ * min(i + ElemConn, n_a - 1, i + ceil(R/h_a) - 1)] (:467-469); entries
+ * R - dist for element-centre distances dist < R (:478-490); with
+ * ElemConn == 1 H is the identity (:451-459). */
+void oracle_dens_filter_apply(int ex, int ey, int ez, double hx, double hy, double hz, double R, const double *in,
+                              double *out) {
+    int cx = (int)ceil(R / hx) - 1, cy = (int)ceil(R / hy) - 1, cz = (int)ceil(R / hz) - 1;
+    int sw = cx > cy ? cx : cy;
+    if (cz > sw) sw = cz;
+    if (sw == 0) sw = 1;
+    long long nel = (long long)ex * ey * ez;
+    if (sw == 1) {
+        for (long long e = 0; e < nel; e++) out[e] = in[e];
+        return;
+    }
+    for (int k = 0; k < ez; k++)
+        for (int j = 0; j < ey; j++)
+            for (int i = 0; i < ex; i++) {
+                double acc = 0.0;
+                int k1 = k + sw < ez - 1 ? k + sw : ez - 1, j1 = j + sw < ey - 1 ? j + sw : ey - 1,
+                    i1 = i + sw < ex - 1 ? i + sw : ex - 1;
+                if (k + cz < k1) k1 = k + cz;
+                if (j + cy < j1) j1 = j + cy;
+                if (i + cx < i1) i1 = i + cx;
+                for (int k2 = (k - sw > 0 ? k - sw : 0); k2 <= k1; k2++)
+                    for (int j2 = (j - sw > 0 ? j - sw : 0); j2 <= j1; j2++)
+                        for (int i2 = (i - sw > 0 ? i - sw : 0); i2 <= i1; i2++) {
+                            /* element centres h/2 + i h (DMDASetUniformCoordinates, :420) */
+                            double d0 = (hx / 2 + i * hx) - (hx / 2 + i2 * hx);
+                            double d1 = (hy / 2 + j * hy) - (hy / 2 + j2 * hy);
+                            double d2 = (hz / 2 + k * hz) - (hz / 2 + k2 * hz);
+                            double dist = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+                            if (dist < R) acc += (R - dist) * in[i2 + (long long)ex * (j2 + (long long)ey * k2)];
+                        }
+                out[i + (long long)ex * (j + (long long)ey * k)] = acc;
+            }
+}
+
+/* Filter::FilterProject, filterType 0/1 (Filter.cc:60-119) */
+void oracle_dens_filter_project(int ex, int ey, int ez, double hx, double hy, double hz, int ftype, double R,
+                                const double *x, double *xTilde, double *xPhys, int projection, double beta,
+                                double eta) {
+    long long nel = (long long)ex * ey * ez;
+    if (ftype == 1) {
+        double *one = vnew(nel), *hs = vnew(nel);
+        for (long long e = 0; e < nel; e++) one[e] = 1.0;
+        oracle_dens_filter_apply(ex, ey, ez, hx, hy, hz, R, one, hs);
+        oracle_dens_filter_apply(ex, ey, ez, hx, hy, hz, R, x, xTilde);
+        for (long long e = 0; e < nel; e++) xTilde[e] /= hs[e];
+        free(one);
+        free(hs);
+    } else {
+        memcpy(xTilde, x, sizeof(double) * nel);
+    }
+    for (long long e = 0; e < nel; e++) xPhys[e] = projection ? smooth_projection(xTilde[e], beta, eta) : xTilde[e];
+}
+
+/* Filter::Gradients, filterType 0/1 (Filter.cc:122-206) */
+void oracle_dens_filter_gradients(int ex, int ey, int ez, double hx, double hy, double hz, int ftype, double R,
+                                  const double *x, const double *xTilde, double *dfdx, int m, double *dgdx,
+                                  int projection, double beta, double eta) {
+    long long nel = (long long)ex * ey * ez;
+    if (projection) {
+        for (long long e = 0; e < nel; e++) {
+            double d = chainrule_smooth_projection(xTilde[e], beta, eta);
+            dfdx[e] *= d;
+            for (int j = 0; j < m; j++) dgdx[(size_t)j * nel + e] *= d;
+        }
+    }
+    double *one = vnew(nel), *hs = vnew(nel), *tmp = vnew(nel);
+    for (long long e = 0; e < nel; e++) one[e] = 1.0;
+    oracle_dens_filter_apply(ex, ey, ez, hx, hy, hz, R, one, hs);
+    if (ftype == 0) { /* sensitivities only: (H (df .* x) ./ Hs) ./ x */
+        for (long long e = 0; e < nel; e++) tmp[e] = dfdx[e] * x[e];
+        oracle_dens_filter_apply(ex, ey, ez, hx, hy, hz, R, tmp, dfdx);
+        for (long long e = 0; e < nel; e++) dfdx[e] = (dfdx[e] / hs[e]) / x[e];
+    } else { /* H (v ./ Hs) for df and every dg */
+        for (int j = -1; j < m; j++) {
+            double *v = j < 0 ? dfdx : dgdx + (size_t)j * nel;
+            for (long long e = 0; e < nel; e++) tmp[e] = v[e] / hs[e];
+            oracle_dens_filter_apply(ex, ey, ez, hx, hy, hz, R, tmp, v);
+        }
+    }
+    free(one);
+    free(hs);
+    free(tmp);
+}
+
 /* Filter::GetMND, Filter.cc:208-227 */
 double oracle_filter_mnd(int n, const double *x) {
     double s = 0.0;

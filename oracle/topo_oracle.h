@@ -92,6 +92,17 @@ void oracle_filter_gradients(int nx, int ny, int nz, double hx, double hy, doubl
                              const double *xTilde, double *dfdx, int m, double *dgdx, int projection,
                              double beta, double eta, double rtol);
 double oracle_filter_mnd(int n, const double *x);
+/* Filter.cc:60-206 and :302-531 for filterType 0 (sensitivity filter) and 1
+ * (density filter) on an ex*ey*ez element grid: H with weights R - dist
+ * between element centres, Hs = H 1 */
+void oracle_dens_filter_apply(int ex, int ey, int ez, double hx, double hy, double hz, double R, const double *in,
+                              double *out);
+void oracle_dens_filter_project(int ex, int ey, int ez, double hx, double hy, double hz, int ftype, double R,
+                                const double *x, double *xTilde, double *xPhys, int projection, double beta,
+                                double eta);
+void oracle_dens_filter_gradients(int ex, int ey, int ez, double hx, double hy, double hz, int ftype, double R,
+                                  const double *x, const double *xTilde, double *dfdx, int m, double *dgdx,
+                                  int projection, double beta, double eta);
 int oracle_increase_beta(double *beta, double betaFinal, double gx, int itr, double ch);
 
 /* MMA (MMA.cc) */

@@ -240,3 +240,31 @@ def test_sommg_basis_and_reduced_matrices():
     assert np.abs(Q[:, N == 0.0]).max() == 0.0  # the basis vanishes on clamped DOFs
     KQ = np.stack([le.apply_KM(q)[0] for q in Q])
     assert np.abs(Q @ KQ.T - Kr).max() < 1e-12 * np.abs(Kr).max()
+
+
+def test_density_and_sensitivity_filter_restatement():
+    # Filter.cc:302-531: stencil ElemConn = max_a(ceil(R/h_a) - 1) >= 1, identity
+    # when ElemConn == 1, weights R - dist between element centres
+    n = (6, 5, 4)
+    nel = int(np.prod(n))
+    rng = np.random.default_rng(12)
+    x = 0.2 + 0.6 * rng.random(nel)
+    assert np.array_equal(O.dens_filter_apply(*n, x, 2.0), x)  # R = 2 on unit elements: identity
+    H = np.stack([O.dens_filter_apply(*n, np.eye(nel)[k], 3.0) for k in range(nel)], 1)
+    assert np.abs(H - H.T).max() == 0.0  # cubic elements: symmetric
+    assert H[0, 0] == 3.0 and H[0, 1] == 2.0 and H[0, 2] == 1.0  # face neighbours at 1 and 2
+    assert abs(H[0, 1 + 6] - (3.0 - np.sqrt(2.0))) < 1e-15  # edge neighbour
+    hs = H.sum(1)
+    xt, xp = O.dens_filter_project(*n, 1, x, 3.0, False, 1.0, 0.5)
+    assert np.abs(xt - H @ x / hs).max() < 1e-14 and np.array_equal(xt, xp)
+    xt0, _ = O.dens_filter_project(*n, 0, x, 3.0, False, 1.0, 0.5)
+    assert np.array_equal(xt0, x)
+    df = rng.standard_normal(nel)
+    dg = rng.standard_normal(nel)
+    d1, g1 = O.dens_filter_gradients(*n, 1, x, xt, df, dg, 3.0, False, 1.0, 0.5)
+    assert np.abs(d1 - H @ (df / hs)).max() < 1e-13 and np.abs(g1 - H @ (dg / hs)).max() < 1e-13
+    d0, g0 = O.dens_filter_gradients(*n, 0, x, x, df, dg, 3.0, False, 1.0, 0.5)
+    assert np.abs(d0 - (H @ (df * x)) / hs / x).max() < 1e-12 and np.array_equal(g0, dg)
+    # anisotropic elements: ElemConn from the smallest size, per-axis upper limits
+    Ha = np.stack([O.dens_filter_apply(*n, np.eye(nel)[k], 2.5, h=(1.0, 2.0, 1.0)) for k in range(nel)], 1)
+    assert Ha[0, 0] == 2.5 and Ha[0, 6] == 0.5 and Ha[6, 0] == 0.5

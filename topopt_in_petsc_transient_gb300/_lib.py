@@ -62,6 +62,9 @@ EXPORTS = [
     "topo_pdefilt_create", "topo_pdefilt_destroy", "topo_pdefilt_filter_project", "topo_pdefilt_filter_project_dev",
     "topo_filter_project", "topo_filter_project_dev", "topo_filter_gradients", "topo_filter_gradients_dev",
     "topo_filter_mnd", "topo_filter_mnd_dev",
+    "topo_densfilt_create", "topo_densfilt_destroy", "topo_densfilt_filter_project",
+    "topo_densfilt_filter_project_dev", "topo_densfilt_gradients", "topo_densfilt_gradients_dev",
+    "topo_densfilt_mnd", "topo_densfilt_mnd_dev",
     "topo_mma_create", "topo_mma_destroy", "topo_mma_set_asymptotes", "topo_mma_set_outer_movelimit",
     "topo_mma_set_outer_movelimit_dev", "topo_mma_design_change",
     "topo_mma_update", "topo_mma_update_dev", "topo_mma_design_change_dev", "topo_mma_kkt_residual_dev",
@@ -113,6 +116,14 @@ def load(path=None):
         "topo_filter_gradients_dev": (ip, [vp, vp, vp, ip, vp, ip, d, d]),
         "topo_filter_mnd": (ip, [vp, vp, dp]),
         "topo_filter_mnd_dev": (ip, [vp, vp, dp]),
+        "topo_densfilt_create": (ip, [pp, ip, ip, ip, d, d, d, ip, d]),
+        "topo_densfilt_destroy": (None, [vp]),
+        "topo_densfilt_filter_project": (ip, [vp, vp, vp, vp, ip, d, d]),
+        "topo_densfilt_filter_project_dev": (ip, [vp, vp, vp, vp, ip, d, d]),
+        "topo_densfilt_gradients": (ip, [vp, vp, vp, vp, ip, vp, ip, d, d]),
+        "topo_densfilt_gradients_dev": (ip, [vp, vp, vp, vp, ip, vp, ip, d, d]),
+        "topo_densfilt_mnd": (ip, [vp, vp, dp]),
+        "topo_densfilt_mnd_dev": (ip, [vp, vp, dp]),
         "topo_mma_create": (ip, [pp, ip, ip, vp, vp, vp]),
         "topo_mma_destroy": (None, [vp]),
         "topo_mma_set_asymptotes": (ip, [vp, d, d, d]),

@@ -204,14 +204,29 @@ class PDEFilt:
 
 
 class Filter:
-    """Filter (Filter.h:34-92) for filterType 2 (PDE filter) with the smoothed
-    Heaviside projection; filter types 0/1 are not part of this build."""
+    """Filter (Filter.h:34-92) with the smoothed Heaviside projection:
+    filterType 0 (sensitivity filter), 1 (density filter) and 2 (PDE filter)."""
 
     def __init__(self, nelx, nely, nelz, filterT, Rin, h=(1.0, 1.0, 1.0), rtol=1e-10, maxit=5000):
-        if filterT != 2:
-            raise TopoError(1, "Filter", "only the PDE filter (filter = 2) is built for the GPU path")
-        self.pdef = PDEFilt(nelx, nely, nelz, Rin, h=h, rtol=rtol, maxit=maxit)
-        self.nel = self.pdef.nel
+        if filterT not in (0, 1, 2):
+            raise TopoError(1, "Filter", "filterType must be 0, 1 or 2")
+        self.filterT = filterT
+        self.dens = None
+        self.pdef = None
+        self.nel = nelx * nely * nelz
+        if filterT == 2:
+            self.pdef = PDEFilt(nelx, nely, nelz, Rin, h=h, rtol=rtol, maxit=maxit)
+        else:
+            hh = C.c_void_p()
+            check(_lib.load().topo_densfilt_create(C.byref(hh), nelx, nely, nelz, h[0], h[1], h[2], filterT, Rin),
+                  "Filter")
+            self.dens = hh
+
+    def __del__(self):
+        h = getattr(self, "dens", None)
+        if h is not None and h.value:
+            _lib.load().topo_densfilt_destroy(h)
+            self.dens = None
 
     def FilterProject(self, x, xTilde, xPhys, projectionFilter, beta, eta):
         """Filter::FilterProject (Filter.cc:60-119)."""
@@ -219,21 +234,30 @@ class Filter:
         d = [_addr(v, self.nel, n) for v, n in ((x, "x"), (xTilde, "xTilde"), (xPhys, "xPhys"))]
         if len({t[0] for t in d}) != 1:
             raise TypeError("x, xTilde, xPhys must all be host or all be device arrays")
-        f = L.topo_filter_project_dev if d[0][0] else L.topo_filter_project
-        check(f(self.pdef._h, d[0][1], d[1][1], d[2][1], int(bool(projectionFilter)), beta, eta),
-              "Filter::FilterProject")
+        if self.dens is not None:
+            f = L.topo_densfilt_filter_project_dev if d[0][0] else L.topo_densfilt_filter_project
+            h = self.dens
+        else:
+            f = L.topo_filter_project_dev if d[0][0] else L.topo_filter_project
+            h = self.pdef._h
+        check(f(h, d[0][1], d[1][1], d[2][1], int(bool(projectionFilter)), beta, eta), "Filter::FilterProject")
         return 0
 
     def Gradients(self, x, xTilde, dfdx, m, dgdx, projectionFilter, beta, eta):
         """Filter::Gradients (Filter.cc:122-206); dfdx and dgdx (m x nel) in place."""
         L = _lib.load()
-        d = [_addr(v, n_, nm) for v, n_, nm in ((xTilde, self.nel, "xTilde"), (dfdx, self.nel, "dfdx"),
-                                                 (dgdx, self.nel * m, "dgdx"))]
+        d = [_addr(v, n_, nm) for v, n_, nm in ((x, self.nel, "x"), (xTilde, self.nel, "xTilde"),
+                                                 (dfdx, self.nel, "dfdx"), (dgdx, self.nel * m, "dgdx"))]
         if len({t[0] for t in d}) != 1:
-            raise TypeError("xTilde, dfdx, dgdx must all be host or all be device arrays")
-        f = L.topo_filter_gradients_dev if d[0][0] else L.topo_filter_gradients
-        check(f(self.pdef._h, d[0][1], d[1][1], m, d[2][1], int(bool(projectionFilter)), beta, eta),
-              "Filter::Gradients")
+            raise TypeError("x, xTilde, dfdx, dgdx must all be host or all be device arrays")
+        if self.dens is not None:
+            f = L.topo_densfilt_gradients_dev if d[0][0] else L.topo_densfilt_gradients
+            check(f(self.dens, d[0][1], d[1][1], d[2][1], m, d[3][1], int(bool(projectionFilter)), beta, eta),
+                  "Filter::Gradients")
+        else:
+            f = L.topo_filter_gradients_dev if d[0][0] else L.topo_filter_gradients
+            check(f(self.pdef._h, d[1][1], d[2][1], m, d[3][1], int(bool(projectionFilter)), beta, eta),
+                  "Filter::Gradients")
         return 0
 
     def GetMND(self, x):
@@ -241,8 +265,12 @@ class Filter:
         L = _lib.load()
         dev, a = _addr(x, self.nel, "x")
         out = C.c_double()
-        f = L.topo_filter_mnd_dev if dev else L.topo_filter_mnd
-        check(f(self.pdef._h, a, C.byref(out)), "Filter::GetMND")
+        if self.dens is not None:
+            f = L.topo_densfilt_mnd_dev if dev else L.topo_densfilt_mnd
+            check(f(self.dens, a, C.byref(out)), "Filter::GetMND")
+        else:
+            f = L.topo_filter_mnd_dev if dev else L.topo_filter_mnd
+            check(f(self.pdef._h, a, C.byref(out)), "Filter::GetMND")
         return out.value
 
     @staticmethod
