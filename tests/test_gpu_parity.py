@@ -1,11 +1,13 @@
 """GPU parity: the sm_103a library, called through the C ABI, against the
 FP64 oracle on the same seeded inputs.
 
-Tolerances: plain FP64 path (FP64 multigrid inside FP64 flexible CG, solves
-to rtol 1e-12): objective 1e-10 relative, sensitivities 1e-9 of max|dfdx|.
-Mixed path (FP32 multigrid inside FP64 flexible CG): same solve tolerance on
-the FP64 residual, so the same bounds hold; the FP32 only changes iteration
-counts.
+Tolerances: plain FP64 path (FP64 preconditioner inside FP64 flexible CG,
+solves to rtol 1e-12): objective 1e-10 relative, sensitivities 1e-9 of
+max|dfdx|.  Mixed path (FP32 flexible-CG recurrence with an FP32 Kronecker or
+multigrid preconditioner, convergence decided on FP64-accurate residuals):
+the same bounds at the same solve tolerance; FP32 sensitivity element math
+and the default tolerance rtol 1e-10 are tested at the looser bounds each
+test states.
 """
 import numpy as np
 import pytest
@@ -354,8 +356,8 @@ def test_design_iteration_with_density_filter(gpu):
     from topopt_in_petsc_transient_gb300 import TopOpt, design_iteration
     opt = TopOpt(nelx=16, nely=8, nelz=8, nlvls=2, ncp=1, tsc=4, t1=0.02, objective=3, loadsignal=1, filter=1,
                  rmin=3.0, dalpha=0.0, dbeta=1e-3).setup()
-    fx, gx, ch, mnd = design_iteration(opt)
-    assert np.isfinite(fx) and np.isfinite(gx) and 0.0 < ch <= 0.2 + 1e-12 and 0.0 <= mnd <= 1.0
+    fx, fxs, gx, ch, mnd = design_iteration(opt)
+    assert np.isfinite(fx) and np.isfinite(fxs) and np.isfinite(gx) and 0.0 < ch <= 0.2 + 1e-12 and 0.0 <= mnd <= 1.0
 
 
 def test_solver_failures_are_reported(gpu):

@@ -134,7 +134,7 @@ class TopOpt:
 
 def design_iteration(opt: TopOpt):
     """One iteration of the main.cc optimisation loop (main.cc:76-160);
-    returns (fx_true, gx0, ch, mnd)."""
+    returns (fx_true, fx_scaled, gx0, ch, mnd)."""
     opt.itr += 1
     ph = opt.physics
     ph.CompleteInitialState(opt.xPhys, opt.Emin, opt.Emax, opt.Rmin, opt.Rmax, opt.penalK, opt.penalM)
