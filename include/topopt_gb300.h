@@ -233,6 +233,17 @@ int topo_densfilt_mnd_dev(topo_densfilt *f, const double *x_dev, double *mnd);
 /* MMA (MMA.h:9-120), design variables resident on the device */
 int topo_mma_create(topo_mma **out, int n, int m, const double *a, const double *c, const double *d);
 void topo_mma_destroy(topo_mma *mma);
+/* restart constructors MMA(n, m, itr, xo1, xo2, U, L[, a, c, d]) (MMA.h:16-19,
+ * MMA.cc:6-178): iteration counter and the histories and asymptotes of an
+ * earlier run; a, c, d may be NULL (defaults 0, 1000, 0) */
+int topo_mma_create_restart(topo_mma **out, int n, int m, int itr, const double *xo1, const double *xo2,
+                            const double *U, const double *L, const double *a, const double *c, const double *d);
+int topo_mma_create_restart_dev(topo_mma **out, int n, int m, int itr, const double *xo1_dev, const double *xo2_dev,
+                                const double *U_dev, const double *L_dev, const double *a, const double *c,
+                                const double *d);
+/* MMA::Restart (MMA.cc:307-350): xo1, xo2, U, L for a later restart */
+int topo_mma_restart(topo_mma *mma, double *xo1, double *xo2, double *U, double *L);
+int topo_mma_restart_dev(topo_mma *mma, double *xo1_dev, double *xo2_dev, double *U_dev, double *L_dev);
 int topo_mma_set_asymptotes(topo_mma *mma, double init, double decrease, double increase);
 /* MMA::SetOuterMovelimit (MMA.cc:374-393) */
 int topo_mma_set_outer_movelimit(topo_mma *mma, double Xmin, double Xmax, double movlim, const double *x,

@@ -307,6 +307,42 @@ def test_mma_matches_oracle(gpu):
         assert _rel(xg.cpu().numpy(), xo) < 1e-10, it
 
 
+def test_mma_restart_continues_bitwise(gpu):
+    # MMA::Restart and the restart constructor MMA(n, m, itr, xo1, xo2, U, L)
+    # (MMA.h:16-27): three updates, restart, a fourth update equals four
+    # uninterrupted updates bit for bit (host and device restart arrays)
+    from topopt_in_petsc_transient_gb300 import MMA
+    n = 1500
+    rng = np.random.default_rng(19)
+    c = rng.random(n)
+
+    def step(mg, xg, it):
+        lo, hi = torch.zeros_like(xg), torch.zeros_like(xg)
+        xh = xg.cpu().numpy()
+        df = torch.tensor(2 * (xh - c) * (1 + 0.1 * it), device="cuda")
+        g = np.array([xh.mean() - 0.4])
+        mg.SetOuterMovelimit(0.0, 1.0, 0.2, xg, lo, hi)
+        mg.Update(xg, df, g, torch.full_like(xg, 1.0 / n), lo, hi)
+
+    ref = MMA(n, 1)
+    ref.SetAsymptotes(0.1, 0.6, 1.05)
+    xr = torch.full((n,), 0.5, dtype=torch.float64, device="cuda")
+    for it in range(4):
+        step(ref, xr, it)
+    for device in (True, False):
+        a = MMA(n, 1)
+        a.SetAsymptotes(0.1, 0.6, 1.05)
+        xa = torch.full((n,), 0.5, dtype=torch.float64, device="cuda")
+        for it in range(3):
+            step(a, xa, it)
+        st = [torch.zeros_like(xa) for _ in range(4)] if device else [np.zeros(n) for _ in range(4)]
+        a.Restart(*st)
+        b = MMA(n, 1, itr=3, xo1=st[0], xo2=st[1], U=st[2], L=st[3])
+        b.SetAsymptotes(0.1, 0.6, 1.05)
+        step(b, xa, 3)
+        assert torch.equal(xa, xr)
+
+
 def test_sommg_basis_solves_descend_the_multigrid_hierarchy(gpu):
     # the shifted operator K - om^2 M has negative element-wise lower bounds;
     # they must not make the V-cycle stop at the fine level (a one-level

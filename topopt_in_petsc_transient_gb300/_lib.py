@@ -65,7 +65,8 @@ EXPORTS = [
     "topo_densfilt_create", "topo_densfilt_destroy", "topo_densfilt_filter_project",
     "topo_densfilt_filter_project_dev", "topo_densfilt_gradients", "topo_densfilt_gradients_dev",
     "topo_densfilt_mnd", "topo_densfilt_mnd_dev",
-    "topo_mma_create", "topo_mma_destroy", "topo_mma_set_asymptotes", "topo_mma_set_outer_movelimit",
+    "topo_mma_create", "topo_mma_create_restart", "topo_mma_create_restart_dev", "topo_mma_restart",
+    "topo_mma_restart_dev", "topo_mma_destroy", "topo_mma_set_asymptotes", "topo_mma_set_outer_movelimit",
     "topo_mma_set_outer_movelimit_dev", "topo_mma_design_change",
     "topo_mma_update", "topo_mma_update_dev", "topo_mma_design_change_dev", "topo_mma_kkt_residual_dev",
     "topo_kernel_launches", "topo_last_error", "topo_status_str",
@@ -125,6 +126,10 @@ def load(path=None):
         "topo_densfilt_mnd": (ip, [vp, vp, dp]),
         "topo_densfilt_mnd_dev": (ip, [vp, vp, dp]),
         "topo_mma_create": (ip, [pp, ip, ip, vp, vp, vp]),
+        "topo_mma_create_restart": (ip, [pp, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp]),
+        "topo_mma_create_restart_dev": (ip, [pp, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp]),
+        "topo_mma_restart": (ip, [vp, vp, vp, vp, vp]),
+        "topo_mma_restart_dev": (ip, [vp, vp, vp, vp, vp]),
         "topo_mma_destroy": (None, [vp]),
         "topo_mma_set_asymptotes": (ip, [vp, d, d, d]),
         "topo_mma_set_outer_movelimit": (ip, [vp, d, d, d, vp, vp, vp]),

@@ -386,6 +386,63 @@ int topo_mma_create(topo_mma **out, int n, int m, const double *a, const double 
     return TOPO_OK;
 }
 
+int topo_mma_create_restart_dev(topo_mma **out, int n, int m, int itr, const double *xo1_dev, const double *xo2_dev,
+                                const double *U_dev, const double *L_dev, const double *a, const double *c,
+                                const double *d) {
+    if (!out || !xo1_dev || !xo2_dev || !U_dev || !L_dev) return TOPO_ERR_ARG;
+    int rc = topo_mma_create(out, n, m, a, c, d);
+    if (rc) return rc;
+    rc = mma_restart_set_dev((*out)->impl, itr, xo1_dev, xo2_dev, U_dev, L_dev);
+    if (rc) {
+        topo_mma_destroy(*out);
+        *out = nullptr;
+    }
+    return rc;
+}
+
+int topo_mma_create_restart(topo_mma **out, int n, int m, int itr, const double *xo1, const double *xo2,
+                            const double *U, const double *L, const double *a, const double *c, const double *d) {
+    if (!out || !xo1 || !xo2 || !U || !L) return TOPO_ERR_ARG;
+    int rc = topo_mma_create(out, n, m, a, c, d);
+    if (rc) return rc;
+    topo_mma *h = *out;
+    size_t b = sizeof(double) * (size_t)n;
+    // staging: x, df, lo, hi and the first constraint-gradient slot hold the four vectors
+    if (cudaMemcpy(h->d_x, xo1, b, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->d_df, xo2, b, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->d_lo, U, b, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->d_hi, L, b, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("MMA restart: host-to-device copy failed");
+        topo_mma_destroy(h);
+        *out = nullptr;
+        return TOPO_ERR_CUDA;
+    }
+    rc = mma_restart_set_dev(h->impl, itr, h->d_x, h->d_df, h->d_lo, h->d_hi);
+    if (rc) {
+        topo_mma_destroy(h);
+        *out = nullptr;
+    }
+    return rc;
+}
+
+int topo_mma_restart_dev(topo_mma *mma, double *xo1_dev, double *xo2_dev, double *U_dev, double *L_dev) {
+    if (!mma || !xo1_dev || !xo2_dev || !U_dev || !L_dev) return TOPO_ERR_ARG;
+    return mma_restart_get_dev(mma->impl, xo1_dev, xo2_dev, U_dev, L_dev);
+}
+
+int topo_mma_restart(topo_mma *mma, double *xo1, double *xo2, double *U, double *L) {
+    if (!mma || !xo1 || !xo2 || !U || !L) return TOPO_ERR_ARG;
+    int rc = mma_restart_get_dev(mma->impl, mma->d_x, mma->d_df, mma->d_lo, mma->d_hi);
+    if (rc) return rc;
+    size_t b = sizeof(double) * (size_t)mma->n;
+    ACK(cudaMemcpy(xo1, mma->d_x, b, cudaMemcpyDeviceToHost));
+    ACK(cudaMemcpy(xo2, mma->d_df, b, cudaMemcpyDeviceToHost));
+    ACK(cudaMemcpy(U, mma->d_lo, b, cudaMemcpyDeviceToHost));
+    ACK(cudaMemcpy(L, mma->d_hi, b, cudaMemcpyDeviceToHost));
+    return TOPO_OK;
+}
+
 void topo_mma_destroy(topo_mma *mma) {
     if (!mma) return;
     mma_destroy(mma->impl);

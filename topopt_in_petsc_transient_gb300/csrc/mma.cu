@@ -499,6 +499,36 @@ int mma_kkt_dev(TopoMMA *mm, const double *x, const double *dfdx, const double *
     return TOPO_OK;
 }
 
+int mma_restart_set_dev(TopoMMA *mm, int itr, const double *xo1, const double *xo2, const double *U,
+                        const double *L) {
+    if (itr < 0) {
+        set_error("MMA restart: negative iteration counter");
+        return TOPO_ERR_ARG;
+    }
+    // the reference accepts itr < 3 with a warning ("NOT A LEGAL RESTART POINT")
+    const size_t b = sizeof(double) * (size_t)mm->n;
+    cudaStream_t s = mm->stream;
+    MCK(cudaMemcpyAsync(mm->xo1, xo1, b, cudaMemcpyDeviceToDevice, s));
+    MCK(cudaMemcpyAsync(mm->xo2, xo2, b, cudaMemcpyDeviceToDevice, s));
+    MCK(cudaMemcpyAsync(mm->U, U, b, cudaMemcpyDeviceToDevice, s));
+    MCK(cudaMemcpyAsync(mm->L, L, b, cudaMemcpyDeviceToDevice, s));
+    mm->host.k = itr;
+    MCK(cudaMemcpyAsync(&mm->S->k, &mm->host.k, sizeof(int), cudaMemcpyHostToDevice, s));
+    MCK(cudaStreamSynchronize(s));
+    return TOPO_OK;
+}
+
+int mma_restart_get_dev(TopoMMA *mm, double *xo1, double *xo2, double *U, double *L) {
+    const size_t b = sizeof(double) * (size_t)mm->n;
+    cudaStream_t s = mm->stream;
+    MCK(cudaMemcpyAsync(xo1, mm->xo1, b, cudaMemcpyDeviceToDevice, s));
+    MCK(cudaMemcpyAsync(xo2, mm->xo2, b, cudaMemcpyDeviceToDevice, s));
+    MCK(cudaMemcpyAsync(U, mm->U, b, cudaMemcpyDeviceToDevice, s));
+    MCK(cudaMemcpyAsync(L, mm->L, b, cudaMemcpyDeviceToDevice, s));
+    MCK(cudaStreamSynchronize(s));
+    return TOPO_OK;
+}
+
 int mma_n(const TopoMMA *mm) { return mm->n; }
 int mma_m(const TopoMMA *mm) { return mm->m; }
 void *mma_stream(TopoMMA *mm) { return mm->stream; }

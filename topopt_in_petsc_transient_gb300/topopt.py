@@ -288,17 +288,37 @@ class Filter:
 
 
 class MMA:
-    """MMA (MMA.h:9-120) with design vectors on the device."""
+    """MMA (MMA.h:9-120) with design vectors on the device.  The four
+    reference constructors: MMA(n, m, x[, a, c, d]) and the restart forms
+    MMA(n, m, itr=..., xo1=..., xo2=..., U=..., L=...[, a, c, d]) (MMA.h:12-19)."""
 
-    def __init__(self, n, m, x=None, a=None, c=None, d=None):
-        L = _lib.load()
+    def __init__(self, n, m, x=None, a=None, c=None, d=None, itr=None, xo1=None, xo2=None, U=None, L=None):
+        lib = _lib.load()
         a = np.zeros(m) if a is None else np.ascontiguousarray(a, dtype=np.float64)
         c = np.full(m, 1000.0) if c is None else np.ascontiguousarray(c, dtype=np.float64)
         d = np.zeros(m) if d is None else np.ascontiguousarray(d, dtype=np.float64)
         h_ = C.c_void_p()
-        check(L.topo_mma_create(C.byref(h_), n, m, a.ctypes.data, c.ctypes.data, d.ctypes.data), "MMA")
+        if itr is None:
+            check(lib.topo_mma_create(C.byref(h_), n, m, a.ctypes.data, c.ctypes.data, d.ctypes.data), "MMA")
+        else:
+            v = [_addr(t, n, nm) for t, nm in ((xo1, "xo1"), (xo2, "xo2"), (U, "U"), (L, "L"))]
+            if len({t[0] for t in v}) != 1:
+                raise TypeError("xo1, xo2, U, L must all be host or all be device arrays")
+            f = lib.topo_mma_create_restart_dev if v[0][0] else lib.topo_mma_create_restart
+            check(f(C.byref(h_), n, m, int(itr), v[0][1], v[1][1], v[2][1], v[3][1], a.ctypes.data, c.ctypes.data,
+                    d.ctypes.data), "MMA")
         self._h = h_
         self.n, self.m = n, m
+
+    def Restart(self, xo1, xo2, U, L):
+        """MMA::Restart (MMA.cc:307-350): fills xo1, xo2, U, L for a later restart."""
+        v = [_addr(t, self.n, nm) for t, nm in ((xo1, "xo1"), (xo2, "xo2"), (U, "U"), (L, "L"))]
+        if len({t[0] for t in v}) != 1:
+            raise TypeError("xo1, xo2, U, L must all be host or all be device arrays")
+        lib = _lib.load()
+        f = lib.topo_mma_restart_dev if v[0][0] else lib.topo_mma_restart
+        check(f(self._h, v[0][1], v[1][1], v[2][1], v[3][1]), "MMA::Restart")
+        return 0
 
     def __del__(self):
         h = getattr(self, "_h", None)
