@@ -153,6 +153,12 @@ int topo_volume_constraint_noalloc_dev(long long nel, double *gx, double *dgdx_d
 /* inspection (tests / output): which = 0 U, 1 DU, 2 DDU of step j of the
  * resident block (j = -1: block start state); copies 3*nn values to host */
 int topo_le_get_state(topo_le *le, int which, int j, double *out);
+/* checkpoint c (0 <= c < ncp: the state at the start of block c; c = 0 the
+ * initial state of CompleteInitialState) into host arrays of ndof values: the
+ * three vectors the reference writes to cp%04d.dat (LinearElasticity.cc:1134-1136)
+ * and GenerateCheckPoints' later files.  Checkpoints 1..ncp-1 are valid after
+ * GenerateCheckPoints. */
+int topo_le_get_checkpoint(topo_le *le, int c, double *U, double *DU, double *DDU);
 /* weighted products K x and M x with the current densities (no masking) */
 int topo_le_apply_km(topo_le *le, const double *x, double *Kx, double *Mx);
 int topo_le_get_stats(topo_le *le, topo_le_stats *out);
@@ -262,6 +268,15 @@ int topo_mma_design_change_dev(topo_mma *mma, const double *x_dev, double *xold_
 int topo_mma_kkt_residual_dev(topo_mma *mma, const double *x_dev, const double *dfdx_dev, const double *fx,
                               const double *dgdx_dev, const double *xmin_dev, const double *xmax_dev, double *norm2,
                               double *normInf);
+
+/* PETSc binary vector records (VecView / VecLoad with a binary viewer): a
+ * big-endian int32 class id 1211214, int32 length n, n big-endian doubles.
+ * Records are appended to one file (the reference's Restart0x.dat,
+ * RestartSol0x.dat and cp%04d.dat: TopOpt.cc:722-727,
+ * LinearElasticity.cc:1134-1136, :2482-2484).  on_device: v is a device
+ * pointer.  topo_petsc_vec_read reads record `index` (0 = first). */
+int topo_petsc_vec_write(const char *path, int append, const double *v, long long n, int on_device);
+int topo_petsc_vec_read(const char *path, int index, double *v, long long n, int on_device);
 
 /* kernels launched by this library so far (direct launches and graph
  * replays; kernels inside device-side Krylov loops are reported per object by

@@ -69,3 +69,29 @@ def test_default_params_match_reference_defaults(lib):
     assert (p.nx, p.ny, p.nz) == (65, 33, 33)
     assert p.nu == 0.3 and p.nlvls == 4 and p.ncp == 2 and p.tsc == 25 and p.t1 == 50.0
     assert p.dalpha == 1e-4 and p.dbeta == 1e-4 and p.ti == 1 and p.sInt == 1 and p.mInt == 0
+
+
+def test_petsc_binary_vector_records(lib, tmp_path):
+    # VecView / VecLoad binary format: big-endian int32 class id 1211214 and
+    # length, then big-endian doubles; records appended in one file
+    from topopt_in_petsc_transient_gb300 import TopoError, read_petsc_vecs, write_petsc_vecs
+    rng = np.random.default_rng(2)
+    a, b = rng.standard_normal(7), rng.standard_normal(3)
+    p = str(tmp_path / "Restart00.dat")
+    write_petsc_vecs(p, [a, b])
+    raw = open(p, "rb").read()
+    assert len(raw) == 2 * 8 + 8 * (7 + 3)
+    assert raw[:8] == (1211214).to_bytes(4, "big") + (7).to_bytes(4, "big")
+    assert np.array_equal(np.frombuffer(raw[8:64], dtype=">f8"), a)
+    assert raw[64:72] == (1211214).to_bytes(4, "big") + (3).to_bytes(4, "big")
+    assert np.array_equal(np.frombuffer(raw[72:], dtype=">f8"), b)
+    a2, b2 = np.zeros(7), np.zeros(3)
+    read_petsc_vecs(p, [a2, b2])
+    assert np.array_equal(a2, a) and np.array_equal(b2, b)
+    b3 = np.zeros(3)
+    read_petsc_vecs(p, [b3], first=1)
+    assert np.array_equal(b3, b)
+    with pytest.raises(TopoError):
+        read_petsc_vecs(p, [np.zeros(5)])  # length mismatch is an error, not a silent read
+    with pytest.raises(TopoError):
+        read_petsc_vecs(p, [np.zeros(3)], first=2)  # no third record

@@ -343,6 +343,33 @@ def test_mma_restart_continues_bitwise(gpu):
         assert torch.equal(xa, xr)
 
 
+def test_restart_files_continue_the_design_loop(gpu, tmp_path):
+    # TopOpt::WriteRestartFiles and the -restartFileVec branch of
+    # AllocateMMAwithRestart (TopOpt.cc:600-735): three design iterations,
+    # restart files, a fresh TopOpt continued from them matches the
+    # uninterrupted run bit for bit; the HBM checkpoints export as cp%04d.dat
+    from topopt_in_petsc_transient_gb300 import (TopOpt, design_iteration, load_restart, read_petsc_vecs,
+                                                 write_restart_files)
+    kw = dict(nelx=16, nely=8, nelz=8, nlvls=2, ncp=2, tsc=3, t1=0.03, objective=3, loadsignal=1, dalpha=0.0,
+              dbeta=1e-3)
+    a = TopOpt(**kw).setup()
+    for _ in range(3):
+        design_iteration(a)
+    vec = write_restart_files(a, str(tmp_path))
+    assert vec.endswith("Restart00.dat")
+    design_iteration(a)
+    b = TopOpt(**kw).setup()
+    load_restart(b, vec, str(tmp_path / "Restart00_itr_f0.dat"))
+    assert b.itr == 3 and b.fscale == a.fscale
+    design_iteration(b)
+    assert torch.equal(a.x, b.x) and torch.equal(a.xPhys, b.xPhys)
+    a.physics.WriteCheckPoints(str(tmp_path))
+    U, DU, DDU = a.physics.checkpoint(1)
+    got = [np.zeros(U.size) for _ in range(3)]
+    read_petsc_vecs(str(tmp_path / "cp0001.dat"), got)
+    assert np.array_equal(got[0], U) and np.array_equal(got[1], DU) and np.array_equal(got[2], DDU)
+
+
 def test_sommg_basis_solves_descend_the_multigrid_hierarchy(gpu):
     # the shifted operator K - om^2 M has negative element-wise lower bounds;
     # they must not make the V-cycle stop at the fine level (a one-level

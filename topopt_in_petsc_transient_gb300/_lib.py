@@ -56,7 +56,7 @@ EXPORTS = [
     "topo_le_generate_checkpoints",
     "topo_le_compute_objective_sensitivities", "topo_le_compute_objective_sensitivities_dev",
     "topo_le_volume_constraint", "topo_le_volume_constraint_dev",
-    "topo_le_get_state", "topo_le_apply_km", "topo_le_get_stats", "topo_le_time_apply",
+    "topo_le_get_state", "topo_le_get_checkpoint", "topo_le_apply_km", "topo_le_get_stats", "topo_le_time_apply",
     "topo_le_kernel_timing", "topo_volume_constraint_noalloc_dev", "topo_le_reduced_system",
     "topo_box_element_matrices",
     "topo_pdefilt_create", "topo_pdefilt_destroy", "topo_pdefilt_filter_project", "topo_pdefilt_filter_project_dev",
@@ -69,6 +69,7 @@ EXPORTS = [
     "topo_mma_restart_dev", "topo_mma_destroy", "topo_mma_set_asymptotes", "topo_mma_set_outer_movelimit",
     "topo_mma_set_outer_movelimit_dev", "topo_mma_design_change",
     "topo_mma_update", "topo_mma_update_dev", "topo_mma_design_change_dev", "topo_mma_kkt_residual_dev",
+    "topo_petsc_vec_write", "topo_petsc_vec_read",
     "topo_kernel_launches", "topo_last_error", "topo_status_str",
 ]
 
@@ -99,6 +100,7 @@ def load(path=None):
         "topo_le_compute_objective_sensitivities_dev": (ip, [vp, dp, vp]),
         "topo_le_volume_constraint": (ip, [vp, dp, vp, vp, d]),
         "topo_le_volume_constraint_dev": (ip, [vp, dp, vp, vp, d]),
+        "topo_le_get_checkpoint": (ip, [vp, ip, vp, vp, vp]),
         "topo_le_get_state": (ip, [vp, ip, ip, vp]),
         "topo_le_apply_km": (ip, [vp, vp, vp, vp]),
         "topo_le_get_stats": (ip, [vp, C.POINTER(LEStats)]),
@@ -125,6 +127,8 @@ def load(path=None):
         "topo_densfilt_gradients_dev": (ip, [vp, vp, vp, vp, ip, vp, ip, d, d]),
         "topo_densfilt_mnd": (ip, [vp, vp, dp]),
         "topo_densfilt_mnd_dev": (ip, [vp, vp, dp]),
+        "topo_petsc_vec_write": (ip, [C.c_char_p, ip, vp, C.c_longlong, ip]),
+        "topo_petsc_vec_read": (ip, [C.c_char_p, ip, vp, C.c_longlong, ip]),
         "topo_mma_create": (ip, [pp, ip, ip, vp, vp, vp]),
         "topo_mma_create_restart": (ip, [pp, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp]),
         "topo_mma_create_restart_dev": (ip, [pp, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp]),

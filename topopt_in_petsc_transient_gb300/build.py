@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libtopopt_gb300.so")
-SOURCES = ["le.cu", "filter.cu", "densfilt.cu", "mma.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["le.cu", "filter.cu", "densfilt.cu", "mma.cu", "capi.cu", "noalloc.cu", "petscio.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]

@@ -205,6 +205,11 @@ int topo_le_get_state(topo_le *le, int which, int j, double *out) {
     return le_get_state(le->impl, which, j, out);
 }
 
+int topo_le_get_checkpoint(topo_le *le, int c, double *U, double *DU, double *DDU) {
+    if (!le || !U || !DU || !DDU) return TOPO_ERR_ARG;
+    return le_get_checkpoint(le->impl, c, U, DU, DDU);
+}
+
 int topo_le_apply_km(topo_le *le, const double *x, double *Kx, double *Mx) {
     if (!le || !x || !Kx || !Mx) return TOPO_ERR_ARG;
     long long nd = le->ndof;

@@ -2123,6 +2123,24 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
     return TOPO_OK;
 }
 
+int le_get_checkpoint(TopoLE *le, int c, double *U, double *DU, double *DDU) {
+    if (c < 0 || c >= le->p.ncp || le->kb) {
+        set_error("checkpoint index outside 0..ncp-1 (or the reduced path, which keeps no checkpoints)");
+        return TOPO_ERR_ARG;
+    }
+    if (!le->design_ready || (c > 0 && !le->checkpoints_ready)) {
+        set_error("checkpoint requested before CompleteInitialState / GenerateCheckPoints");
+        return TOPO_ERR_STATE;
+    }
+    const long long nd = le->ndof;
+    const double *base = le->cp + (size_t)c * 3 * nd;
+    CK(cudaMemcpyAsync(U, base, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaMemcpyAsync(DU, base + nd, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaMemcpyAsync(DDU, base + 2 * nd, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaStreamSynchronize(le->stream));
+    return TOPO_OK;
+}
+
 int le_get_state(TopoLE *le, int which, int j, double *out) {
     if (which < 0 || which > 2 || j < -1 || j >= le->p.tsc) return TOPO_ERR_ARG;
     long long nd = le->ndof;

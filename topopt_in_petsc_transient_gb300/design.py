@@ -161,3 +161,48 @@ def design_iteration(opt: TopOpt):
         ch = 1.0
     opt.filt.FilterProject(opt.x, opt.xTilde, opt.xPhys, opt.projectionFilter, opt.beta, opt.eta)
     return fx, fxs, gx0, ch, mnd
+
+
+def write_restart_files(opt: TopOpt, directory):
+    """TopOpt::WriteRestartFiles (TopOpt.cc:678-735): MMA::Restart, then x, xPhys,
+    xo1, xo2, U, L into Restart00.dat / Restart01.dat (the two sets alternate)
+    and "itr fscale" into Restart0x_itr_f0.dat.  Returns the vector file."""
+    import os
+
+    import torch
+
+    from .topopt import write_petsc_vecs
+    st = [torch.zeros_like(opt.x) for _ in range(4)]
+    opt.mma.Restart(*st)
+    opt.flip = not getattr(opt, "flip", True)  # TopOpt.cc:535, :691-695
+    tag = "01" if opt.flip else "00"
+    vec = os.path.join(directory, "Restart%s.dat" % tag)
+    write_petsc_vecs(vec, [opt.x, opt.xPhys] + st)
+    with open(os.path.join(directory, "Restart%s_itr_f0.dat" % tag), "w") as f:
+        f.write("%d %1.16e\n" % (opt.itr, opt.fscale))
+    return vec
+
+
+def load_restart(opt: TopOpt, vec_file, itr_file=None, only_load_design=False, load_design=0):
+    """The -restartFileVec branch of TopOpt::AllocateMMAwithRestart
+    (TopOpt.cc:600-670) on a set-up TopOpt: loads x, xPhys, xo1, xo2, U, L.
+    With only_load_design the design seeds a fresh MMA (load_design 2: xPhys
+    becomes x); otherwise xold = x, itr and fscale come from itr_file and MMA
+    continues through its restart constructor."""
+    import torch
+
+    from .topopt import MMA, read_petsc_vecs
+    st = [torch.zeros_like(opt.x) for _ in range(4)]
+    read_petsc_vecs(vec_file, [opt.x, opt.xPhys] + st)
+    if only_load_design:
+        if load_design == 2:
+            opt.x.copy_(opt.xPhys)
+        opt.mma = MMA(opt.nel, opt.m, opt.x)
+    else:
+        opt.xold.copy_(opt.x)
+        with open(itr_file) as f:
+            tok = f.read().split()
+        opt.itr, opt.fscale = int(tok[0]), float(tok[1])
+        opt.mma = MMA(opt.nel, opt.m, itr=opt.itr, xo1=st[0], xo2=st[1], U=st[2], L=st[3])
+    opt.mma.SetAsymptotes(0.1, 0.6, 1.05)  # main.cc:58
+    return opt

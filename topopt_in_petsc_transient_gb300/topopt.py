@@ -35,6 +35,29 @@ def _addr(a, n=None, name="array"):
     return False, a.ctypes.data
 
 
+def write_petsc_vecs(path, vectors, append=False):
+    """The vectors as consecutive PETSc binary records (VecView with a binary
+    viewer; big-endian class id 1211214, length, values), host arrays or CUDA
+    tensors."""
+    import os
+    lib = _lib.load()
+    for k, v in enumerate(vectors):
+        n = v.numel() if _is_dev(v) else np.asarray(v).size
+        dev, a = _addr(v, n, "vector %d" % k)
+        check(lib.topo_petsc_vec_write(os.fsencode(path), int(append or k > 0), a, n, int(dev)), "PETSc vector write")
+
+
+def read_petsc_vecs(path, outs, first=0):
+    """Records first, first + 1, ... of a PETSc binary file into outs (VecLoad);
+    each record must hold as many values as its output."""
+    import os
+    lib = _lib.load()
+    for k, v in enumerate(outs):
+        n = v.numel() if _is_dev(v) else np.asarray(v).size
+        dev, a = _addr(v, n, "vector %d" % k)
+        check(lib.topo_petsc_vec_read(os.fsencode(path), first + k, a, n, int(dev)), "PETSc vector read")
+
+
 class LinearElasticity:
     """LinearElasticity (LinearElasticity.h:23-240) on the GPU.
 
@@ -155,6 +178,22 @@ class LinearElasticity:
         out = np.zeros(self.ndof)
         check(_lib.load().topo_le_get_state(self._h, which, j, out.ctypes.data), "get_state")
         return out
+
+    def checkpoint(self, c):
+        """Checkpoint c (U, DU, DDU: the state at the start of block c)."""
+        U, DU, DDU = np.zeros(self.ndof), np.zeros(self.ndof), np.zeros(self.ndof)
+        check(_lib.load().topo_le_get_checkpoint(self._h, int(c), U.ctypes.data, DU.ctypes.data, DDU.ctypes.data),
+              "checkpoint")
+        return U, DU, DDU
+
+    def WriteCheckPoints(self, directory):
+        """cp%04d.dat of every block in the reference's format (three PETSc
+        binary records U, DU, DDU each, LinearElasticity.cc:1134-1136, :1260-1270),
+        written from the HBM checkpoints."""
+        import os
+        for c in range(self.params.ncp):
+            write_petsc_vecs(os.path.join(directory, "cp%04d.dat" % c), list(self.checkpoint(c)))
+        return 0
 
     def apply_km(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
