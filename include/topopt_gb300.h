@@ -31,6 +31,7 @@ extern "C" {
 typedef struct topo_le topo_le;
 typedef struct topo_pdefilt topo_pdefilt;
 typedef struct topo_mma topo_mma;
+typedef struct topo_mpiio topo_mpiio;
 
 /* Parameters of LinearElasticity(...) (LinearElasticity.h:29) plus the mesh
  * geometry the reference reads off its DMDA (SetUpBC, LinearElasticity.cc:337-391)
@@ -277,6 +278,41 @@ int topo_mma_kkt_residual_dev(topo_mma *mma, const double *x_dev, const double *
  * pointer.  topo_petsc_vec_read reads record `index` (0 = first). */
 int topo_petsc_vec_write(const char *path, int append, const double *v, long long n, int on_device);
 int topo_petsc_vec_read(const char *path, int index, double *v, long long n, int on_device);
+
+/* Result files in the layout of the reference's MPIIO writer, the input of
+ * bin2vtu.py (bin2vtu.py:18-150): one domain of 8-node hexahedra in DMDA
+ * natural order.  Replaces MPIIO::MPIIO + Allocate + writePoints + writeCells
+ * (MPIIO.cc:32-150, :409-717): topo_mpiio_create truncates `filename` and
+ * writes the banner "TopOpt result version 1.1\n\x01", the native uint64
+ * header {1, nn, nel, npf, ncf, 8}, the '\x01'-terminated point and cell field
+ * names, the float32 node coordinates (uniform on the box xc = {xmin, xmax,
+ * ymin, ymax, zmin, zmax} with nx*ny*nz nodes, DMDASetUniformCoordinates)
+ * and the uint64 connectivity, offsets and VTK types (12) of the cells.
+ * `slots` (>= 2; 0 = 4) datasets may be queued: each is converted to float32
+ * on the device straight into mapped pinned host memory and appended by a
+ * writer thread while the caller goes on. */
+int topo_mpiio_create(topo_mpiio **out, int nx, int ny, int nz, const double *xc, int npf, const char *pnames,
+                      int ncf, const char *cnames, const char *filename, int slots);
+/* flushes the queued datasets, closes the file */
+void topo_mpiio_destroy(topo_mpiio *io);
+/* MPIIO::WriteVTK (MPIIO.cc:152-406) = writePointFields + writeCellFields
+ * (MPIIO.cc:724-935): appends uint64 itr, the point fields (3 * n_nodal of them:
+ * component c of DOF-interleaved nodal vector v is field 3 v + c, nn float32
+ * values each) and the cell fields (n_cells arrays of nel float32).  n_nodal = 0
+ * repeats the point fields of the previous dataset (zeros before the first):
+ * the design-only WriteVTK re-emits its work array.  on_device: the arrays are
+ * device pointers read on `stream` (a cudaStream_t, NULL = legacy stream). */
+int topo_mpiio_write(topo_mpiio *io, unsigned long long itr, const double *const *nodal, int n_nodal,
+                     const double *const *cells, int n_cells, int on_device, void *stream);
+/* waits until every queued dataset is in the file */
+int topo_mpiio_flush(topo_mpiio *io);
+/* attaches (io != NULL) or detaches the physics output of LinearElasticity:
+ * the `write, output` arguments of CompleteInitialState (U at itr 0),
+ * GenerateCheckPoints (every step tsc*c + j + 1 when ncp > 1) and
+ * ComputeObjectiveSensitivities (every step when ncp == 1), each dataset the
+ * displacement and xPhys (LinearElasticity.cc:1087-1114, :1220-1252,
+ * :1736-1742).  The writer must have 3 point fields and 1 cell field. */
+int topo_le_set_output(topo_le *le, topo_mpiio *io);
 
 /* kernels launched by this library so far (direct launches and graph
  * replays; kernels inside device-side Krylov loops are reported per object by

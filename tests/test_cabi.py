@@ -95,3 +95,81 @@ def test_petsc_binary_vector_records(lib, tmp_path):
         read_petsc_vecs(p, [np.zeros(5)])  # length mismatch is an error, not a silent read
     with pytest.raises(TopoError):
         read_petsc_vecs(p, [np.zeros(3)], first=2)  # no third record
+
+
+def test_mpiio_result_file_layout(lib, tmp_path):
+    # MPIIO layout read back the way bin2vtu.py reads it: banner, header,
+    # names, float32 DMDA coordinates, hex8 cells in DMDAGetElements_3D order,
+    # then datasets of uint64 itr + field-major float32 point and cell fields
+    from mpiio_reader import point_fields_of, read_result_file
+
+    from topopt_in_petsc_transient_gb300 import MPIIO, TopoError
+    nelx, nely, nelz = 3, 2, 4
+    nx, ny, nz = nelx + 1, nely + 1, nelz + 1
+    nn, nel = nx * ny * nz, nelx * nely * nelz
+    xc = (-1.0, 2.0, 0.0, 0.7, 5.0, 6.3)
+    rng = np.random.default_rng(7)
+    p = str(tmp_path / "outputPhysics0_00000.dat")
+    io = MPIIO((nelx, nely, nelz), 3, "ux, uy, uz", 1, "xPhys", p, xc=xc)
+    U = [rng.standard_normal(3 * nn) for _ in range(3)]
+    xp = rng.random(nel)
+    for t in range(3):
+        io.WriteVTK(U[t], xp, 10 * t)
+    with pytest.raises(TopoError):
+        io.WriteVTK(U[0], U[1], U[2], xp, xp, xp, 9)  # 9 point fields on a 3-field file
+    io.Flush()
+    r = read_result_file(p)
+    assert r["banner"] == "TopOpt result version 1.1\n"
+    assert (r["nPointsT"], r["nCellsT"], r["nPFields"], r["nCFields"], r["nodesPerElement"]) == (nn, nel, 3, 1, 8)
+    assert r["pointFieldNames"] == ["ux", "uy", "uz"] and r["cellFieldNames"] == ["xPhys"]
+    # DMDASetUniformCoordinates: xmin + i (xmax - xmin) / (n - 1), natural node order
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    ref = np.stack([xc[0] + i * ((xc[1] - xc[0]) / (nx - 1)), xc[2] + j * ((xc[3] - xc[2]) / (ny - 1)),
+                    xc[4] + k * ((xc[5] - xc[4]) / (nz - 1))], axis=-1).reshape(-1, 3).astype(np.float32)
+    assert np.array_equal(r["points"], ref)
+    # hex8 cells: n0, n0+x, n0+x+y, n0+y, then the same four one node layer up
+    ek, ej, ei = np.meshgrid(np.arange(nelz), np.arange(nely), np.arange(nelx), indexing="ij")
+    n0 = (ei + nx * (ej + ny * ek)).reshape(-1)
+    quad = np.stack([n0, n0 + 1, n0 + 1 + nx, n0 + nx], axis=1)
+    assert np.array_equal(r["cells"], np.concatenate([quad, quad + nx * ny], axis=1).astype(np.uint64))
+    assert np.array_equal(r["offsets"], 8 * np.arange(1, nel + 1, dtype=np.uint64))
+    assert np.all(r["types"] == 12)
+    assert [d[0] for d in r["datasets"]] == [0, 10, 20]
+    for t, (_, pf, cf) in enumerate(r["datasets"]):
+        assert np.array_equal(pf, point_fields_of(U[t]))
+        assert np.array_equal(cf[0], xp.astype(np.float32))
+    del io
+
+    # design file (main.cc:42): no point fields, x / xTilde / xPhys per iteration
+    p = str(tmp_path / "outputDesign_00000.dat")
+    io = MPIIO((nelx, nely, nelz), 0, "", 3, "x, xTilde, xPhys", p)
+    X = [rng.random(nel) for _ in range(3)]
+    io.WriteVTK(X[0], X[1], X[2], 1)
+    with pytest.raises(TopoError):
+        io.WriteVTK(U[0], xp, 2)  # displacement on a design-only file
+    io.WriteVTK(X[2], X[0], X[1], 2)
+    del io
+    r = read_result_file(p)
+    assert r["nPFields"] == 0 and r["pointFieldNames"] == [""]
+    assert r["cellFieldNames"] == ["x", "xTilde", "xPhys"]
+    assert np.array_equal(r["points"][-1], np.array([nelx, nely, nelz], dtype=np.float32))  # default box
+    assert [d[0] for d in r["datasets"]] == [1, 2]
+    assert np.array_equal(r["datasets"][0][2], np.stack(X).astype(np.float32))
+    assert np.array_equal(r["datasets"][1][2], np.stack([X[2], X[0], X[1]]).astype(np.float32))
+
+    # all-fields overload (U, DU, DDU, x, xTilde, xPhys), then the design-only
+    # overload, which repeats the previous point fields (zeros before any)
+    p = str(tmp_path / "outputAll_00000.dat")
+    io = MPIIO((nelx, nely, nelz), 9, "ux, uy, uz, vx, vy, vz, ax, ay, az", 3, "x, xTilde, xPhys", p, slots=2)
+    io.WriteVTK(X[0], X[1], X[2], 0)
+    io.WriteVTK(U[0], U[1], U[2], X[0], X[1], X[2], 1)
+    io.WriteVTK(X[1], X[2], X[0], 2)
+    io.WriteVTK(X[2], X[1], X[0], 3)
+    io.Flush()
+    r = read_result_file(p)
+    assert len(r["pointFieldNames"]) == 9 and r["pointFieldNames"][3] == "vx"
+    pf = [d[1] for d in r["datasets"]]
+    assert np.array_equal(pf[0], np.zeros((9, nn), np.float32))
+    assert np.array_equal(pf[1], point_fields_of(*U))
+    assert np.array_equal(pf[2], pf[1]) and np.array_equal(pf[3], pf[1])
+    assert np.array_equal(r["datasets"][2][2], np.stack([X[1], X[2], X[0]]).astype(np.float32))

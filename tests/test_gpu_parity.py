@@ -375,6 +375,116 @@ def test_restart_files_continue_the_design_loop(gpu, tmp_path):
     assert np.array_equal(got[0], U) and np.array_equal(got[1], DU) and np.array_equal(got[2], DDU)
 
 
+@pytest.mark.parametrize("ncp,tsc,reduction", [(2, 3, False), (1, 4, False), (2, 3, True)])
+def test_physics_output_files(gpu, tmp_path, ncp, tsc, reduction):
+    # the `write, output` arguments of CompleteInitialState (dataset 0),
+    # GenerateCheckPoints (every step when ncp > 1) and
+    # ComputeObjectiveSensitivities (every step when ncp == 1): each dataset is
+    # the float32 displacement of one step and xPhys, bitwise the device states
+    from mpiio_reader import point_fields_of, read_result_file
+
+    from topopt_in_petsc_transient_gb300 import MPIIO, TopoError
+    n = (8, 4, 4)
+    rng = np.random.default_rng(11)
+    x = 0.3 + 0.1 * (2 * rng.random(np.prod(n)) - 1)
+    kw = dict(ncp=ncp, tsc=tsc, t1=0.02 * ncp * tsc, objective=3, loadsignal=1, dalpha=1e-3, dbeta=1e-3)
+    red = dict(reduction=True, basis=4, omega0=0.01, rtol=1e-13) if reduction else {}
+    le = _le(n, nlvls=2, **kw, **red)
+    p = str(tmp_path / "outputPhysics0_00000.dat")
+    io = MPIIO(le, 3, "ux, uy, uz", 1, "xPhys", p)
+    with pytest.raises(TopoError):  # a design-only writer cannot take the physics output
+        le.CompleteInitialState(x, *M6, write=True, output=MPIIO(le, 0, "", 3, "x, xTilde, xPhys",
+                                                                  str(tmp_path / "d.dat")))
+    xd = torch.tensor(x, dtype=torch.float64, device="cuda")
+    df = torch.zeros_like(xd)
+    le.CompleteInitialState(xd, *M6, write=True, output=io)
+    le.GenerateCheckPoints(True, xd, io)
+    io.Flush()
+    r = read_result_file(p)
+    T = ncp * tsc
+    expect = T + 1 if ncp > 1 else 1
+    assert [d[0] for d in r["datasets"]] == list(range(expect))
+    if ncp > 1:  # the last block is resident after GenerateCheckPoints
+        for j in range(tsc):
+            assert np.array_equal(r["datasets"][T - tsc + j + 1][1], point_fields_of(le.state(0, j)))
+        if not reduction:
+            assert np.array_equal(r["datasets"][0][1], point_fields_of(le.checkpoint(0)[0]))
+            assert np.array_equal(r["datasets"][tsc][1], point_fields_of(le.checkpoint(1)[0]))
+    le.ComputeObjectiveSensitivities(df, write=True, output=io)
+    io.Flush()
+    r = read_result_file(p)
+    assert [d[0] for d in r["datasets"]] == list(range(T + 1))  # ncp == 1: the steps come from here
+    if ncp == 1:
+        for j in range(tsc):
+            assert np.array_equal(r["datasets"][j + 1][1], point_fields_of(le.state(0, j)))
+    for _, pf, cf in r["datasets"]:
+        assert np.array_equal(cf[0], x.astype(np.float32))
+        assert np.all(np.isfinite(pf))
+    assert np.abs(r["datasets"][-1][1]).max() > 0.0
+    # without write nothing is added
+    le.CompleteInitialState(xd, *M6, write=False, output=io)
+    io.Flush()
+    assert len(read_result_file(p)["datasets"]) == T + 1
+
+
+def test_result_file_overloads_from_device_tensors(gpu, tmp_path):
+    # MPIIO::WriteVTK overloads with CUDA tensors: the float32 conversion and
+    # the DOF-interleaved to field-major scatter run on the device, straight
+    # into the pinned records; a ring of two records wraps several times
+    from mpiio_reader import point_fields_of, read_result_file
+
+    from topopt_in_petsc_transient_gb300 import MPIIO
+    n = (5, 3, 2)
+    nn, nel = 6 * 4 * 3, 30
+    g = torch.Generator(device="cuda").manual_seed(5)
+    dev = dict(dtype=torch.float64, device="cuda", generator=g)
+    p = str(tmp_path / "outputAll_00000.dat")
+    io = MPIIO(n, 9, "ux, uy, uz, vx, vy, vz, ax, ay, az", 3, "x, xTilde, xPhys", p, slots=2)
+    hist = []
+    for t in range(7):
+        U = [torch.randn(3 * nn, **dev) for _ in range(3)]
+        X = [torch.rand(nel, **dev) for _ in range(3)]
+        if t % 3 == 2:
+            io.WriteVTK(*X, t)  # design-only overload: previous point fields again
+            hist.append((hist[-1][0], X))
+        else:
+            io.WriteVTK(*U, *X, t)
+            hist.append((U, X))
+    del io
+    r = read_result_file(p)
+    assert [d[0] for d in r["datasets"]] == list(range(7))
+    for (U, X), (_, pf, cf) in zip(hist, r["datasets"]):
+        assert np.array_equal(pf, point_fields_of(*[u.cpu().numpy() for u in U]))
+        assert np.array_equal(cf, np.stack([v.cpu().numpy() for v in X]).astype(np.float32))
+
+
+def test_design_loop_result_files(gpu, tmp_path):
+    # main.cc:38-49, :102-105, :163-176: the design fields every iteration,
+    # the physics of the first iteration, the physics of the final design
+    from mpiio_reader import read_result_file
+
+    from topopt_in_petsc_transient_gb300 import TopOpt, design_iteration, final_physics_output
+    opt = TopOpt(nelx=8, nely=4, nelz=4, nlvls=2, ncp=2, tsc=3, t1=0.06, objective=3, loadsignal=1, dalpha=1e-3,
+                 dbeta=1e-3, outputDesign=True, outputPhysics0=True, outputPhysics1=True,
+                 workdir=str(tmp_path)).setup()
+    xp0 = opt.xPhys.cpu().numpy().astype(np.float32)
+    for _ in range(2):
+        design_iteration(opt)
+    final_physics_output(opt)
+    d = read_result_file(str(tmp_path / "outputDesign_00000.dat"))
+    assert d["cellFieldNames"] == ["x", "xTilde", "xPhys"] and d["nPFields"] == 0
+    assert [t[0] for t in d["datasets"]] == [1, 2]
+    assert np.array_equal(d["datasets"][0][2][2], xp0)
+    p0 = read_result_file(str(tmp_path / "outputPhysics0_00000.dat"))
+    assert [t[0] for t in p0["datasets"]] == list(range(7))  # first iteration only
+    assert all(np.array_equal(t[2][0], xp0) for t in p0["datasets"])
+    p1 = read_result_file(str(tmp_path / "outputPhysics1_00000.dat"))
+    assert [t[0] for t in p1["datasets"]] == list(range(7))
+    xpf = opt.xPhys.cpu().numpy().astype(np.float32)
+    assert all(np.array_equal(t[2][0], xpf) for t in p1["datasets"])
+    assert not np.array_equal(xpf, xp0)
+
+
 def test_sommg_basis_solves_descend_the_multigrid_hierarchy(gpu):
     # the shifted operator K - om^2 M has negative element-wise lower bounds;
     # they must not make the V-cycle stop at the fine level (a one-level

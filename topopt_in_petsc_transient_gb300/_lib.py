@@ -70,6 +70,7 @@ EXPORTS = [
     "topo_mma_set_outer_movelimit_dev", "topo_mma_design_change",
     "topo_mma_update", "topo_mma_update_dev", "topo_mma_design_change_dev", "topo_mma_kkt_residual_dev",
     "topo_petsc_vec_write", "topo_petsc_vec_read",
+    "topo_mpiio_create", "topo_mpiio_destroy", "topo_mpiio_write", "topo_mpiio_flush", "topo_le_set_output",
     "topo_kernel_launches", "topo_last_error", "topo_status_str",
 ]
 
@@ -129,6 +130,11 @@ def load(path=None):
         "topo_densfilt_mnd_dev": (ip, [vp, vp, dp]),
         "topo_petsc_vec_write": (ip, [C.c_char_p, ip, vp, C.c_longlong, ip]),
         "topo_petsc_vec_read": (ip, [C.c_char_p, ip, vp, C.c_longlong, ip]),
+        "topo_mpiio_create": (ip, [pp, ip, ip, ip, dp, ip, C.c_char_p, ip, C.c_char_p, C.c_char_p, ip]),
+        "topo_mpiio_destroy": (None, [vp]),
+        "topo_mpiio_write": (ip, [vp, C.c_ulonglong, pp, ip, pp, ip, ip, vp]),
+        "topo_mpiio_flush": (ip, [vp]),
+        "topo_le_set_output": (ip, [vp, vp]),
         "topo_mma_create": (ip, [pp, ip, ip, vp, vp, vp]),
         "topo_mma_create_restart": (ip, [pp, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp]),
         "topo_mma_create_restart_dev": (ip, [pp, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp]),

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libtopopt_gb300.so")
-SOURCES = ["le.cu", "filter.cu", "densfilt.cu", "mma.cu", "capi.cu", "noalloc.cu", "petscio.cu"]
+SOURCES = ["le.cu", "filter.cu", "densfilt.cu", "mma.cu", "capi.cu", "noalloc.cu", "petscio.cu", "mpiio.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]
@@ -52,7 +52,7 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcuda"]
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcuda", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

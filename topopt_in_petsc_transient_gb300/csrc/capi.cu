@@ -210,6 +210,11 @@ int topo_le_get_checkpoint(topo_le *le, int c, double *U, double *DU, double *DD
     return le_get_checkpoint(le->impl, c, U, DU, DDU);
 }
 
+int topo_le_set_output(topo_le *le, topo_mpiio *io) {
+    if (!le) return TOPO_ERR_ARG;
+    return le_set_output(le->impl, io);
+}
+
 int topo_le_apply_km(topo_le *le, const double *x, double *Kx, double *Mx) {
     if (!le || !x || !Kx || !Mx) return TOPO_ERR_ARG;
     long long nd = le->ndof;

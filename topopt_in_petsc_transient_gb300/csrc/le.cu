@@ -23,6 +23,7 @@
 
 #include "le.h"
 #include "kron.cuh"
+#include "mpiio.h"
 #include "sommg.cuh"
 
 namespace topo {
@@ -348,6 +349,7 @@ struct TopoLE {
     int *rstatus = nullptr;
     Arena arena;
     cudaStream_t stream = nullptr;
+    topo_mpiio *out = nullptr;  // attached physics output (topo_le_set_output), not owned
 
     // fine-level data
     double *N_host_dummy = nullptr;
@@ -1994,6 +1996,52 @@ int le_reduced_system(TopoLE *le, double *Q, double *Kr, double *Mr, double *Pr)
     return TOPO_OK;
 }
 
+// Physics output: the `write, output` arguments of CompleteInitialState,
+// GenerateCheckPoints and ComputeObjectiveSensitivities.  Every dataset is the
+// displacement of one time step and xPhys (MPIIO::WriteVTK(da, U, xPhys, itr),
+// MPIIO.cc:215-268), converted on the device straight into the writer's
+// pinned records on this object's stream.
+static int out_state(TopoLE *le, unsigned long long itr, const double *u) {
+    const double *x = le->xPhys;
+    return mpiio_write(le->out, itr, &u, 1, &x, 1, 1, le->stream);
+}
+
+// steps tsc*c + 1 .. tsc*(c + 1) of the resident forward block c
+// (LinearElasticity.cc:1220-1252, :1736-1742)
+static int out_block(TopoLE *le, int c) {
+    const int tsc = le->p.tsc;
+    for (int j = 0; j < tsc; j++) {
+        int rc = out_state(le, (unsigned long long)tsc * c + j + 1, le->Uh + (size_t)j * le->ndof);
+        if (rc) return rc;
+    }
+    return TOPO_OK;
+}
+
+// reduced path: steps t0..t1 of the reduced history lifted to the full space,
+// U = sum_k u_k Q_k (LinearElasticity.cc:1087-1108, :1225-1243)
+static int out_reduced(TopoLE *le, int t0, int t1) {
+    const long long nd = le->ndof;
+    for (int t = t0; t <= t1; t++) {
+        count_launch();
+        k_lift<<<ew_blocks(nd), EW, 0, le->stream>>>(nd, le->kb, le->Q, le->rhist + (size_t)t * 3 * le->kb, le->sp);
+        int rc = out_state(le, (unsigned long long)t, le->sp);
+        if (rc) return rc;
+    }
+    CK(cudaGetLastError());
+    return TOPO_OK;
+}
+
+int le_set_output(TopoLE *le, topo_mpiio *io) {
+    if (io && (mpiio_point_fields(io) != 3 || mpiio_cell_fields(io) != 1 || mpiio_points(io) != le->nn ||
+               mpiio_cells(io) != le->nel)) {
+        set_error("physics output needs a writer of this mesh (" + std::to_string(le->nn) + " nodes, " +
+                  std::to_string(le->nel) + " cells) with 3 point fields (ux, uy, uz) and 1 cell field (xPhys)");
+        return TOPO_ERR_ARG;
+    }
+    le->out = io;
+    return TOPO_OK;
+}
+
 int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, double Emax, double Rmin, double Rmax,
                               double penalK, double penalM) {
     cudaStream_t s = le->stream;
@@ -2014,7 +2062,7 @@ int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, 
         if (rc) return rc;
         le->design_ready = 1;
         le->last_block_resident = le->p.ncp - 1;
-        return TOPO_OK;
+        return le->out ? out_reduced(le, 0, 0) : TOPO_OK;
     }
     int rc = setup_operator(le, 0);
     if (rc) return rc;
@@ -2053,7 +2101,7 @@ int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, 
     le->design_ready = 1;
     le->checkpoints_ready = le->p.ncp <= 1;
     le->last_block_resident = -1;
-    return TOPO_OK;
+    return le->out ? out_state(le, 0, le->cp) : TOPO_OK;  // U0 (LinearElasticity.cc:1087-1114)
 }
 
 int le_generate_checkpoints(TopoLE *le) {
@@ -2061,12 +2109,18 @@ int le_generate_checkpoints(TopoLE *le) {
         set_error("GenerateCheckPoints called before CompleteInitialState");
         return TOPO_ERR_STATE;
     }
-    if (le->p.ncp <= 1 || le->kb) return TOPO_OK;  // the reduced history is complete after CompleteInitialState
+    if (le->p.ncp <= 1) return TOPO_OK;
+    if (le->kb)  // the reduced history is complete after CompleteInitialState
+        return le->out ? out_reduced(le, 1, le->p.ncp * le->p.tsc) : TOPO_OK;
     long long nd = le->ndof;
     int tsc = le->p.tsc;
     for (int c = 0; c < le->p.ncp; c++) {
         int rc = run_block(le, c, 0);
         if (rc) return rc;
+        if (le->out) {
+            rc = out_block(le, c);
+            if (rc) return rc;
+        }
         double *dst = le->cp + (size_t)(c + 1) * 3 * nd;
         CK(cudaMemcpyAsync(dst, le->Uh + (size_t)(tsc - 1) * nd, sizeof(double) * nd, cudaMemcpyDeviceToDevice, le->stream));
         CK(cudaMemcpyAsync(dst + nd, le->DUh + (size_t)(tsc - 1) * nd, sizeof(double) * nd, cudaMemcpyDeviceToDevice,
@@ -2084,7 +2138,13 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
         set_error("ComputeObjectiveSensitivities called before CompleteInitialState");
         return TOPO_ERR_STATE;
     }
-    if (le->kb) return sommg_objective_sensitivities(le, fx, dfdx_dev);
+    if (le->kb) {
+        if (le->out && le->p.ncp == 1) {
+            int rc = out_reduced(le, 1, le->p.tsc);
+            if (rc) return rc;
+        }
+        return sommg_objective_sensitivities(le, fx, dfdx_dev);
+    }
     if (!le->checkpoints_ready) {  // the reverse sweep restarts blocks from checkpoints 1..ncp-1
         set_error("ComputeObjectiveSensitivities with ncp > 1 needs GenerateCheckPoints after CompleteInitialState");
         return TOPO_ERR_STATE;
@@ -2105,6 +2165,10 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
             int rc = run_block(le, c, 0);
             if (rc) return rc;
             le->last_block_resident = c;
+        }
+        if (le->out && le->p.ncp == 1) {  // the forward history of the single block is resident
+            int rc = out_block(le, c);
+            if (rc) return rc;
         }
         int rc = run_block(le, c, 1);
         if (rc) return rc;

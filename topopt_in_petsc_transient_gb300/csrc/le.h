@@ -23,6 +23,7 @@ int le_generate_checkpoints(TopoLE *le);
 int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev);
 int le_get_state(TopoLE *le, int which, int j, double *host_out);
 int le_get_checkpoint(TopoLE *le, int c, double *U, double *DU, double *DDU);
+int le_set_output(TopoLE *le, topo_mpiio *io);
 int le_apply_km(TopoLE *le, const double *x_dev, double *Kx_dev, double *Mx_dev);
 int le_stats(TopoLE *le, LEStats *out);
 long long le_nel(const TopoLE *le);

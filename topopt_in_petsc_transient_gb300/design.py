@@ -4,9 +4,10 @@
 options database (TopOpt.cc:71-518) and the design vectors as device tensors.
 `design_iteration` performs one pass of the optimisation loop of main.cc:82-154
 with the same call order: CompleteInitialState, GenerateCheckPoints,
-ComputeObjectiveSensitivities, VolumeConstraint, Filter::Gradients, objective
-scaling, SetOuterMovelimit, MMA::Update, DesignChange, IncreaseBeta,
-Filter::FilterProject.
+ComputeObjectiveSensitivities, VolumeConstraint, Filter::Gradients, design
+output, objective scaling, SetOuterMovelimit, MMA::Update, DesignChange,
+IncreaseBeta, Filter::FilterProject; `final_physics_output` is the physics
+output of the final design after the loop.
 """
 from dataclasses import dataclass, field
 
@@ -76,6 +77,13 @@ class TopOpt:
     noise: float = 0.0  # initial design V0 + U(-noise, noise) from a generator seeded with seed
     seed: int = 0x7A11
     mass_precond_smooth: int = 0
+    # result files (TopOpt.cc:474-482 -outputDesign/-outputPhysics0/-outputPhysics1,
+    # on by default in the reference, opt-in here) under ./workdir (-workdir)
+    outputDesign: bool = False
+    outputPhysics0: bool = False
+    outputPhysics1: bool = False
+    workdir: str = None
+    xc: tuple = None  # node box (xmin, xmax, ymin, ymax, zmin, zmax); default origin to nel * h
     # state
     fscale: float = 1.0
     itr: int = 0
@@ -126,6 +134,17 @@ class TopOpt:
             mass_precond_smooth=self.mass_precond_smooth, reduction=self.reduction, basis=self.basis,
             omega0=self.omega0, load2_node=self.load2_node, load2_phase=self.load2_phase, out_dof=self.out_dof)
         self.filt = Filter(self.nelx, self.nely, self.nelz, self.filter, self.rmin, h=self.h, rtol=self.filter_rtol)
+        # result files (main.cc:38-49): design fields per iteration, the physics
+        # of the first iteration and of the final design
+        from .topopt import MPIIO
+        kw = dict(xc=self.xc, workdir=self.workdir)
+        self.output1 = MPIIO(self, 0, "", 3, "x, xTilde, xPhys", "outputDesign_00000.dat", **kw) \
+            if self.outputDesign else None
+        self.output2 = MPIIO(self, 3, "ux, uy, uz", 1, "xPhys", "outputPhysics0_00000.dat", **kw) \
+            if self.outputPhysics0 else None
+        self.output3 = MPIIO(self, 3, "ux, uy, uz", 1, "xPhys", "outputPhysics1_00000.dat", **kw) \
+            if self.outputPhysics1 else None
+        self.firstIterWrite = True  # main.cc:69-70
         self.mma = MMA(n, self.m, self.x)
         self.mma.SetAsymptotes(0.1, 0.6, 1.05)  # main.cc:58
         self.filt.FilterProject(self.x, self.xTilde, self.xPhys, self.projectionFilter, self.beta, self.eta)
@@ -137,12 +156,17 @@ def design_iteration(opt: TopOpt):
     returns (fx_true, fx_scaled, gx0, ch, mnd)."""
     opt.itr += 1
     ph = opt.physics
-    ph.CompleteInitialState(opt.xPhys, opt.Emin, opt.Emax, opt.Rmin, opt.Rmax, opt.penalK, opt.penalM)
+    w, out2 = getattr(opt, "firstIterWrite", False), getattr(opt, "output2", None)
+    ph.CompleteInitialState(opt.xPhys, opt.Emin, opt.Emax, opt.Rmin, opt.Rmax, opt.penalK, opt.penalM,
+                            write=w, output=out2)
     if opt.ncp > 1:
-        ph.GenerateCheckPoints()
-    fx = ph.ComputeObjectiveSensitivities(opt.dfdx)
+        ph.GenerateCheckPoints(w, opt.xPhys, out2)
+    fx = ph.ComputeObjectiveSensitivities(opt.dfdx, write=w, output=out2)
     gx0 = ph.VolumeConstraint(opt.dgdx, opt.xPhys, opt.volfrac)
     opt.filt.Gradients(opt.x, opt.xTilde, opt.dfdx, opt.m, opt.dgdx, opt.projectionFilter, opt.beta, opt.eta)
+    opt.firstIterWrite = False
+    if getattr(opt, "output1", None) is not None:  # design output (main.cc:102-105)
+        opt.output1.WriteVTK(opt.x, opt.xTilde, opt.xPhys, opt.itr)
     mnd = opt.filt.GetMND(opt.xPhys)
     if opt.itr == 1:
         opt.fscale = 1.0 / fx
@@ -161,6 +185,23 @@ def design_iteration(opt: TopOpt):
         ch = 1.0
     opt.filt.FilterProject(opt.x, opt.xTilde, opt.xPhys, opt.projectionFilter, opt.beta, opt.eta)
     return fx, fxs, gx0, ch, mnd
+
+
+def final_physics_output(opt: TopOpt):
+    """The physics of the final design into outputPhysics1 (main.cc:163-176):
+    CompleteInitialState, GenerateCheckPoints and ComputeObjectiveSensitivities
+    with write set; returns the objective.  Flushes every result file."""
+    ph = opt.physics
+    out3 = getattr(opt, "output3", None)
+    ph.CompleteInitialState(opt.xPhys, opt.Emin, opt.Emax, opt.Rmin, opt.Rmax, opt.penalK, opt.penalM,
+                            write=True, output=out3)
+    if opt.ncp > 1:
+        ph.GenerateCheckPoints(True, opt.xPhys, out3)
+    fx = ph.ComputeObjectiveSensitivities(opt.dfdx, write=True, output=out3)
+    for out in (getattr(opt, "output1", None), getattr(opt, "output2", None), out3):
+        if out is not None:
+            out.Flush()
+    return fx
 
 
 def write_restart_files(opt: TopOpt, directory):

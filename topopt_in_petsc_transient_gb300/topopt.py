@@ -124,29 +124,63 @@ class LinearElasticity:
             _lib.load().topo_le_destroy(h)
             self._h = None
 
+    def _attach(self, write, output):
+        """Attach `output` (an MPIIO writer) for one call when `write` is set."""
+        io = output._h if (write and output is not None) else None
+        check(_lib.load().topo_le_set_output(self._h, io), "physics output")
+        return io is not None
+
+    def _detach(self, attached):
+        if attached:
+            _lib.load().topo_le_set_output(self._h, None)
+
     def CompleteInitialState(self, xPhys, Emin, Emax, Rmin, Rmax, penalK, penalM, dalpha=None, dbeta=None,
                              write=False, output=None):
-        """LinearElasticity::CompleteInitialState (LinearElasticity.cc:956-1206)."""
+        """LinearElasticity::CompleteInitialState (LinearElasticity.cc:956-1206).
+        With write and an MPIIO output the initial displacement is written as
+        dataset 0 with xPhys (LinearElasticity.cc:1087-1114)."""
         L = _lib.load()
         dev, a = _addr(xPhys, self.nel, "xPhys")
         f = L.topo_le_complete_initial_state_dev if dev else L.topo_le_complete_initial_state
-        check(f(self._h, a, Emin, Emax, Rmin, Rmax, penalK, penalM), "CompleteInitialState")
+        att = self._attach(write, output)
+        try:
+            check(f(self._h, a, Emin, Emax, Rmin, Rmax, penalK, penalM), "CompleteInitialState")
+        finally:
+            self._detach(att)
         return 0
 
     def GenerateCheckPoints(self, write=False, xPhys=None, output=None):
-        """LinearElasticity::GenerateCheckPoints (LinearElasticity.cc:1208-1280)."""
-        check(_lib.load().topo_le_generate_checkpoints(self._h), "GenerateCheckPoints")
+        """LinearElasticity::GenerateCheckPoints (LinearElasticity.cc:1208-1280).
+        With write and an MPIIO output (and ncp > 1) every time step
+        tsc*c + j + 1 is written with the xPhys of CompleteInitialState."""
+        att = self._attach(write, output)
+        try:
+            check(_lib.load().topo_le_generate_checkpoints(self._h), "GenerateCheckPoints")
+        finally:
+            self._detach(att)
         return 0
 
-    def ComputeObjectiveSensitivities(self, dfdx, *args, **kw):
+    def ComputeObjectiveSensitivities(self, dfdx, *args, write=False, output=None):
         """LinearElasticity::ComputeObjectiveSensitivities (LinearElasticity.cc:1625-1908).
 
-        Overwrites dfdx and returns fx (the reference writes *fx)."""
+        Overwrites dfdx and returns fx (the reference writes *fx).  The
+        reference's (xPhys, Emin, Emax, Rmin, Rmax, penalK, penalM, dalpha,
+        dbeta, write, output) may follow dfdx; the material data are those of
+        CompleteInitialState.  With write and an MPIIO output and ncp == 1,
+        every time step is written (LinearElasticity.cc:1736-1742)."""
+        if len(args) > 9:
+            write = args[9]
+        if len(args) > 10:
+            output = args[10]
         L = _lib.load()
         dev, a = _addr(dfdx, self.nel, "dfdx")
         fx = C.c_double()
         f = L.topo_le_compute_objective_sensitivities_dev if dev else L.topo_le_compute_objective_sensitivities
-        check(f(self._h, C.byref(fx), a), "ComputeObjectiveSensitivities")
+        att = self._attach(write, output)
+        try:
+            check(f(self._h, C.byref(fx), a), "ComputeObjectiveSensitivities")
+        finally:
+            self._detach(att)
         return fx.value
 
     def VolumeConstraint(self, dgdx, xPhys, volfrac):
@@ -207,6 +241,92 @@ class LinearElasticity:
         check(_lib.load().topo_le_get_stats(self._h, C.byref(s)), "get_stats")
         return {"cg_iterations": s.cg_iterations, "solves": s.solves, "device_bytes": s.device_bytes,
                 "last_fx": s.last_fx, "graph_body_launches": s.graph_body_launches}
+
+
+class MPIIO:
+    """MPIIO (MPIIO.h:27-100): result files for bin2vtu.py.
+
+    MPIIO(mesh, nPf, pnames, nCf, cnames, filename) follows
+    MPIIO::MPIIO(da_nodes, nPf, pnames, nCf, cnames, filename)
+    (MPIIO.cc:32-150) with the DMDA replaced by `mesh`: an object with
+    nelx/nely/nelz (TopOpt, LinearElasticity) or a tuple (nelx, nely, nelz).
+    `xc` = (xmin, xmax, ymin, ymax, zmin, zmax) of the node box (default:
+    origin to the element counts times the mesh's element size h); `workdir`
+    puts the file at ./workdir/filename like the reference's -workdir option
+    (MPIIO.cc:430-443).  Datasets are converted on the device and appended
+    by a writer thread; Flush() (or deleting the object) waits for the file.
+    """
+
+    def __init__(self, mesh, nPf, pnames, nCf, cnames, filename="output_00000.dat", xc=None, workdir=None,
+                 slots=4):
+        import os
+        if isinstance(mesh, (tuple, list)):
+            nelx, nely, nelz = (int(v) for v in mesh[:3])
+            h = (1.0, 1.0, 1.0)
+        else:
+            nelx, nely, nelz = int(mesh.nelx), int(mesh.nely), int(mesh.nelz)
+            h = getattr(mesh, "h", None)
+            if h is None and hasattr(mesh, "params"):
+                h = (mesh.params.hx, mesh.params.hy, mesh.params.hz)
+            h = tuple(h) if h is not None else (1.0, 1.0, 1.0)
+        if xc is None:
+            xc = (0.0, nelx * h[0], 0.0, nely * h[1], 0.0, nelz * h[2])
+        self.filename = os.path.join(".", workdir, filename) if workdir else filename
+        self.nelx, self.nely, self.nelz = nelx, nely, nelz
+        self.nel = nelx * nely * nelz
+        self.nn = (nelx + 1) * (nely + 1) * (nelz + 1)
+        self.nPf, self.nCf = int(nPf), int(nCf)
+        lib = _lib.load()
+        box = (C.c_double * 6)(*[float(v) for v in xc])
+        h_ = C.c_void_p()
+        check(lib.topo_mpiio_create(C.byref(h_), nelx + 1, nely + 1, nelz + 1, box, self.nPf, pnames.encode(),
+                                    self.nCf, cnames.encode(), os.fsencode(self.filename), int(slots)), "MPIIO")
+        self._h = h_
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().topo_mpiio_destroy(h)
+            self._h = None
+
+    def WriteVTK(self, *args):
+        """MPIIO::WriteVTK (MPIIO.cc:152-406), the overload chosen by the
+        argument count like the reference's C++ overloads:
+          (U, xPhys, itr)                         3 point fields, 1 cell field
+          (x, xTilde, xPhys, itr)                 the previous point fields, 3 cell fields
+          (U, x, xTilde, xPhys, itr)              3 point fields, 3 cell fields
+          (U, DU, DDU, x, xTilde, xPhys, itr)     9 point fields, 3 cell fields
+        Nodal vectors hold 3*nn DOF-interleaved values, cell fields nel; all
+        host numpy float64 or all CUDA float64 tensors (read on torch's
+        current stream)."""
+        split = {3: 1, 4: 0, 5: 1, 7: 3}
+        if len(args) not in split:
+            raise TypeError("WriteVTK takes (U, xPhys, itr), (x, xTilde, xPhys, itr), (U, x, xTilde, xPhys, itr) "
+                            "or (U, DU, DDU, x, xTilde, xPhys, itr)")
+        *arrays, itr = args
+        k = split[len(args)]
+        kinds = set()
+        nodal, cells = [], []
+        for i, a in enumerate(arrays):
+            dev, p = _addr(a, 3 * self.nn if i < k else self.nel, "WriteVTK argument %d" % i)
+            kinds.add(dev)
+            (nodal if i < k else cells).append(p)
+        if len(kinds) > 1:
+            raise TypeError("WriteVTK arrays must all be host arrays or all CUDA tensors")
+        dev = kinds.pop()
+        stream = None
+        if dev:
+            import torch
+            stream = torch.cuda.current_stream().cuda_stream
+        P = C.c_void_p
+        nv = (P * max(k, 1))(*nodal)
+        cv = (P * max(len(cells), 1))(*cells)
+        check(_lib.load().topo_mpiio_write(self._h, int(itr), nv, k, cv, len(cells), int(dev), stream), "WriteVTK")
+        return 0
+
+    def Flush(self):
+        """Waits until every dataset written so far is in the file."""
+        check(_lib.load().topo_mpiio_flush(self._h), "MPIIO flush")
 
 
 class PDEFilt:
