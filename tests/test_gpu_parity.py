@@ -75,6 +75,30 @@ def test_objective_and_sensitivities_match_oracle(gpu, objective, mixed):
     assert _rel(df, df_r) < 1e-9
 
 
+@pytest.mark.parametrize("region,objective,mixed", [(0, 0, False), (1, 3, True), (3, 5, False), (3, 1, True)])
+def test_optimisation_regions_match_oracle(gpu, region, objective, mixed):
+    # SetUpOptimizationRegion (LinearElasticity.cc:222-335) weights every
+    # objective per element: 0 the top column at x = 0 (here under the load of
+    # loadloc 0, with the boundaries 0 supports: roller face x = 0 and the
+    # bottom edge at x = xmax), 1 the mid-height slab |z - zmax/2| < 0.5
+    # (hz = 0.75 puts element centres inside it), 3 the box of half-width 2.5
+    # around (0.75 xmax, ymax/2, zmax/2); region 2 (everything) is every other test
+    n = (16, 8, 8)
+    kw = dict(ncp=2, tsc=4, t1=0.4, objective=objective, loadsignal=1, dalpha=0.01, dbeta=0.01)
+    h = (1.0, 1.0, 0.75 if region == 1 else 1.0)
+    if region == 0:
+        kw.update(t1=8.0, loadsignal=0, boundaries=0, loadloc=0)
+    rng = np.random.default_rng(40 + region)
+    x = 0.1 + 0.5 * rng.random(np.prod(n))
+    le = _le(n, nlvls=2, mixed=mixed, rtol=1e-12, sens_fp32=False, optimizationRegion=region, h=h, **kw)
+    fx, df = _run_gpu(le, x)
+    ref = O.LinearElasticity(*n, optregion=region, hx=h[0], hy=h[1], hz=h[2], **kw)
+    rc, fx_r, df_r = ref.objective_sensitivities(x)
+    assert rc == 0 and fx_r > 0.0
+    assert abs(fx - fx_r) <= 1e-10 * abs(fx_r), (fx, fx_r)
+    assert _rel(df, df_r) < 1e-9
+
+
 @pytest.mark.parametrize("ncp,tsc,graphs", [(1, 12, True), (3, 4, True), (4, 3, False)])
 def test_states_and_checkpointing(gpu, ncp, tsc, graphs):
     n = (16, 8, 8)
