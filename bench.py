@@ -29,11 +29,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "forward+adjoint design iters/s on 1 GB300: mixed vs plain FP64 at equal obj. error"
 
-# DRAM bytes (read + write) per launch from ncu captures summarised under
-# profiles/, keyed by (mesh, kernel name); absent pairs report null
-# DRAM bytes (read + write) per launch of the roofline kernel classes, from
-# one `ncu --set full` capture of each pass on the named mesh (mean over the
-# three Kronecker passes); below the algorithmic bytes where vectors stay in L2
+# DRAM bytes (read + write) per launch of the roofline kernel classes, keyed by
+# (mesh, kernel class), from one `ncu --set full` capture of each pass on the
+# named mesh summarised under profiles/ (mean over the three Kronecker passes);
+# below the algorithmic bytes where vectors stay in L2; absent pairs report null
 TRAFFIC = {
     ("96x48x48", "k_kron_pass<float>"): (5.624e6 + 2.819e6 + 11.22e6) / 3.0,
     ("96x48x48", "k_tile<float,PolPQ32>"): 7.627e6,

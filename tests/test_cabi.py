@@ -173,3 +173,31 @@ def test_mpiio_result_file_layout(lib, tmp_path):
     assert np.array_equal(pf[1], point_fields_of(*U))
     assert np.array_equal(pf[2], pf[1]) and np.array_equal(pf[3], pf[1])
     assert np.array_equal(r["datasets"][2][2], np.stack([X[1], X[2], X[0]]).astype(np.float32))
+
+
+def test_mpiio_rejects_bad_arguments(lib, tmp_path):
+    # argument errors are statuses (TopoError), never partial files or crashes
+    import ctypes as C
+
+    from topopt_in_petsc_transient_gb300 import MPIIO, TopoError
+    with pytest.raises(TopoError):
+        MPIIO((0, 2, 2), 3, "ux, uy, uz", 1, "xPhys", str(tmp_path / "a.dat"))  # no elements along x
+    with pytest.raises(TopoError):
+        MPIIO((2, 2, 2), 3, "ux, uy, uz", 1, "xPhys", str(tmp_path / "missing" / "a.dat"))  # no such folder
+    with pytest.raises(TopoError):
+        MPIIO((2, 2, 2), 3, "ux, uy, uz", 1, "xPhys", str(tmp_path / "a.dat"), slots=1)  # a ring needs two
+    io = MPIIO((2, 2, 2), 3, "ux, uy, uz", 1, "xPhys", str(tmp_path / "a.dat"))
+    with pytest.raises(TypeError):
+        io.WriteVTK(np.zeros(81), 0)  # no overload takes one array
+    with pytest.raises(ValueError):
+        io.WriteVTK(np.zeros(80), np.zeros(8), 0)  # 27 nodes x 3 values required
+    with pytest.raises(TypeError):
+        io.WriteVTK(np.zeros(81, dtype=np.float32), np.zeros(8), 0)  # float64 only
+    box = (C.c_double * 6)(0, 1, 0, 1, 0, 1)
+    h = C.c_void_p()
+    assert lib.topo_mpiio_create(C.byref(h), 3, 3, 3, box, -1, b"", 0, b"", str(tmp_path / "b.dat").encode(), 0) != 0
+    assert lib.topo_mpiio_create(C.byref(h), 3, 3, 3, None, 0, b"", 0, b"", str(tmp_path / "b.dat").encode(), 0) != 0
+    assert lib.topo_mpiio_flush(None) != 0
+    lib.topo_mpiio_destroy(None)  # a null writer is ignored
+    io.Flush()
+    del io
