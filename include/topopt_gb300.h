@@ -102,6 +102,12 @@ typedef struct topo_le_params {
     int load2_node;
     double load2_phase;
     int out_dof;
+    /* form of the FP32 and double-float operator kernels: 0 = bricks of
+     * 7x7x7 output nodes (default), 1 = z-marching slabs of 15x15 output
+     * nodes (fewer recomputed elements and staged nodes per output); FP64
+     * kernels always use bricks.  The form of the most recently created
+     * object applies process-wide */
+    int tile_form;
 } topo_le_params;
 
 typedef struct topo_le_stats {

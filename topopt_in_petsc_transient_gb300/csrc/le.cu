@@ -24,6 +24,7 @@
 #include "le.h"
 #include "kron.cuh"
 #include "mpiio.h"
+#include "slab.cuh"
 #include "sommg.cuh"
 
 namespace topo {
@@ -38,6 +39,10 @@ namespace topo {
     } while (0)
 
 static thread_local std::string g_last_error;
+// form of the FP32 and double-float operator kernels (topo_le_params.tile_form):
+// 0 bricks (tile.cuh), 1 z-marching slabs (slab.cuh); set by le_create,
+// applies process-wide
+static int g_tile_form = 0;
 void set_error(const std::string &s) { g_last_error = s; }
 const char *last_error() { return g_last_error.c_str(); }
 
@@ -254,6 +259,26 @@ constexpr int tile_class() {
 // count; the others launch one CTA per brick
 template <class T, class Pol>
 static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, cudaStream_t s) {
+    // z-marching slabs (slab.cuh) for the FP32 and double-float kernels; the
+    // FP64 ones keep the brick form (their carried corners would spill)
+    if constexpr (!std::is_same<T, double>::value) if (g_tile_form == 1) {
+        static long long slots = 0;
+        const size_t sm = slab_smem_bytes<T, Pol>();
+        if (!slots) {
+            cudaFuncSetAttribute(k_slab<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            int dev = 0, nsm = 0, per_sm = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_slab<T, Pol>, SLAB_THREADS, sm);
+            slots = (long long)std::max(1, per_sm) * std::max(1, nsm);
+        }
+        const SlabShape sh = slab_shape(g, slots);
+        const bool timed = tile_class<T, Pol>() >= 0 && timer_begin(tile_class<T, Pol>(), g.nn(), s);
+        count_launch();
+        k_slab<T, Pol><<<(unsigned)(sh.ncx * sh.ncy * sh.nzr), SLAB_THREADS, sm, s>>>(g, C, pol, sh);
+        timer_end(timed, s);
+        return;
+    }
     static int resident = 0;
     const size_t sm = tile_smem_bytes<T, Pol>();
     if (!resident) {
@@ -433,7 +458,8 @@ int le_create(TopoLE **out, const LEParams *pp) {
     const LEParams &p = *pp;
     if (p.nx < 2 || p.ny < 2 || p.nz < 2 || p.ncp < 1 || p.tsc < 1 || p.nlvls < 1 || p.hx <= 0 || p.hy <= 0 ||
         p.hz <= 0 || p.t1 <= 0 || p.objective < 0 || p.objective > 7 ||
-        p.load2_node >= (long long)p.nx * p.ny * p.nz || p.out_dof >= 3LL * p.nx * p.ny * p.nz) {
+        p.load2_node >= (long long)p.nx * p.ny * p.nz || p.out_dof >= 3LL * p.nx * p.ny * p.nz ||
+        p.tile_form < 0 || p.tile_form > 1) {
         set_error("invalid LinearElasticity parameters");
         return TOPO_ERR_ARG;
     }
@@ -452,6 +478,7 @@ int le_create(TopoLE **out, const LEParams *pp) {
         set_error("mesh dimension not compatible with the number of multigrid levels");
         return TOPO_ERR_ARG;
     }
+    g_tile_form = p.tile_form;
     TopoLE *le = new TopoLE();
     le->p = p;
     le->g = GridDesc{p.nx, p.ny, p.nz, p.nx - 1, p.ny - 1, p.nz - 1};
