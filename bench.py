@@ -139,6 +139,23 @@ def dist_info():
     return ws, rank, local
 
 
+def replica_time(t_local, ws, device):
+    """Job time of N independent replicas: the maximum over the ranks of
+    each rank's timed-region time (an all-reduce MAX on the process group)."""
+    if ws <= 1:
+        return t_local
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_value(steps, ws, t_job):
+    """Whole-job throughput: every replica ran `steps` design iterations."""
+    return ws * steps / t_job
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -192,13 +209,8 @@ def run_gb300(args):
     le_stats1 = opt.physics.stats()
     launches = (L.topo_kernel_launches() - launches0) + (le_stats1["graph_body_launches"] -
                                                           le_stats0["graph_body_launches"])
-    t_total = sum(times)
-    if ws > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_total], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt.item())
-    value = ws * args.steps / t_total
+    t_total = replica_time(sum(times), ws, "cuda")
+    value = replica_value(args.steps, ws, t_total)
     iters_per_solve = ((le_stats1["cg_iterations"] - le_stats0["cg_iterations"]) /
                        max(1, le_stats1["solves"] - le_stats0["solves"]))
 

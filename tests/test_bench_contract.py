@@ -35,3 +35,35 @@ def test_reference_arm_json_line():
 
 def test_reference_arm_other_ranks_exit_silently():
     assert _run({"RANK": "1", "LOCAL_RANK": "1", "WORLD_SIZE": "2"}) == []
+
+
+def _replica_rank(rank, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=2)
+    sys.path.insert(0, ROOT)
+    import bench
+    t = bench.replica_time(1.5 + rank, 2, "cpu")  # rank 1 is the slower replica
+    q.put((rank, t, bench.replica_value(3, 2, t)))
+    dist.destroy_process_group()
+
+
+def test_replicas_take_the_slowest_rank_gloo():
+    # N > 1: the job time is the max over ranks and the value counts every
+    # replica's iterations; two gloo ranks on the CPU
+    import socket
+
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_replica_rank, args=(r, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert got == [(0, 2.5, 2 * 3 / 2.5), (1, 2.5, 2 * 3 / 2.5)]
