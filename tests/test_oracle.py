@@ -163,6 +163,33 @@ def test_adjoint_sensitivities_match_finite_differences(objective):
         assert abs(fd - df[e]) <= 5e-7 * np.abs(df).max(), (objective, e, fd, df[e])
 
 
+@pytest.mark.parametrize("region,objective", [(0, 0), (1, 3), (3, 5)])
+def test_region_weighted_sensitivities_match_finite_differences(region, objective):
+    # SetUpOptimizationRegion (LinearElasticity.cc:222-335): the objective sums
+    # over the region's elements only; region 0 with the boundaries 0 supports
+    # and the load of loadloc 0 on its top edge, region 1 on hz = 0.75 elements
+    # (centres inside the mid-height slab)
+    kw = dict(ncp=2, tsc=4, t1=0.8, objective=objective, loadsignal=1, dalpha=0.01, dbeta=0.01, optregion=region)
+    if region == 0:
+        kw.update(boundaries=0, loadloc=0, loadsignal=0, t1=8.0)
+    if region == 1:
+        kw.update(hz=0.75)
+    le = O.LinearElasticity(4, 2, 2, **kw)
+    rng = np.random.default_rng(20 + region)
+    x = 0.3 + 0.4 * rng.random(le.nel)
+    rc, fx, df = le.objective_sensitivities(x)
+    assert rc == 0 and fx > 0.0
+    full = O.LinearElasticity(4, 2, 2, **dict(kw, optregion=2)).objective_sensitivities(x)[1]
+    assert fx < full  # a strict part of the domain
+    h = 1e-5
+    for e in (0, 5, 10, 15):
+        xp, xm = x.copy(), x.copy()
+        xp[e] += h
+        xm[e] -= h
+        fd = (le.objective_sensitivities(xp)[1] - le.objective_sensitivities(xm)[1]) / (2 * h)
+        assert abs(fd - df[e]) <= 5e-7 * np.abs(df).max(), (region, e, fd, df[e])
+
+
 def test_reference_pulse_objective_fd():
     # reference load signal (Gaussian-modulated cosines, LinearElasticity.cc:597-606), t in [0, 16]
     kw = dict(ncp=4, tsc=10, t1=16.0, objective=0, loadsignal=0, Emax=1e3, Rmax=4.1667e-4, Rmin=4.1667e-7,
