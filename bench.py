@@ -52,7 +52,7 @@ def workload(args):
                 coarse_dense_max=args.coarse_dense_max, coarse_smooth=args.coarse_smooth, sens_fp32=args.sens_fp32,
                 inner_tol=args.inner_tol, inner_maxit=args.inner_maxit, use_graphs=not args.no_graphs,
                 reduction=args.reduction, basis=args.basis, omega0=args.omega0,
-                noise=args.noise, tile_form=args.tile_form, **load2(args))
+                noise=args.noise, tile_form=args.tile_form, kron_form=args.kron_form, **load2(args))
 
 
 def load2(args):
@@ -315,6 +315,7 @@ def run_gb300(args):
                    "dofs": 3 * nn, "elements": nel, "steps_per_design_iter": args.nsteps, "ncp": args.ncp,
                    "rtol": args.rtol, "smooth": args.smooth, "nlvls": args.nlvls,
                    "operator_kernels": "z-marching slabs" if args.tile_form == 1 else "bricks",
+                   "kronecker_passes": "register line segments" if args.kron_form == 1 else "staged lines",
                    "l2": "state history %.1f GB > 129 MB L2; 256 MB L2 flush between timed iterations"
                          % (3 * args.nsteps / args.ncp * 3 * nn * 8 / 1e9),
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
@@ -513,6 +514,8 @@ def main():
     ap.add_argument("--no-cpu", dest="cpu_sample", action="store_false")
     ap.add_argument("--tile-form", dest="tile_form", type=int, default=0,
                     help="operator kernels: 0 bricks of 7x7x7 output nodes, 1 z-marching slabs")
+    ap.add_argument("--kron-form", dest="kron_form", type=int, default=0,
+                    help="Kronecker y/z passes: 0 lines staged in shared memory, 1 register line segments")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -108,6 +108,10 @@ typedef struct topo_le_params {
      * kernels always use bricks.  The form of the most recently created
      * object applies process-wide */
     int tile_form;
+    /* form of the y and z passes of the FP32 Kronecker preconditioner:
+     * 0 = lines staged in shared memory (default), 1 = one thread per line
+     * segment of 16 positions with its window in registers (same outputs) */
+    int kron_form;
 } topo_le_params;
 
 typedef struct topo_le_stats {

@@ -309,4 +309,99 @@ static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
     }
 }
 
+// Line-segment form of the y and z passes (kron_form = 1, FP32): one thread
+// per (x-row value w, line, segment of KSEG positions) loads the KSEG +
+// 2 KRON_B window values of its segment at once -- independent loads,
+// coalesced across consecutive w -- and applies the same tap rows in the same
+// order as kron_line, so its outputs equal the staged passes'.  No shared
+// memory and no barriers; neighbouring segments re-read their 2 KRON_B halo
+// values from L1/L2.
+constexpr int KSEG = 16;
+constexpr int KSEG_THREADS = 256;
+
+__host__ inline long long kron_seg_items(const GridDesc &g, int axis) {
+    const int len = axis == 1 ? g.ny : g.nz;
+    return 3LL * g.nx * (axis == 1 ? g.nz : g.ny) * ((len + KSEG - 1) / KSEG);
+}
+
+template <class T, class R, int AXIS, bool DOT>
+static __global__ void __launch_bounds__(KSEG_THREADS, 2)
+    k_kron_seg(GridDesc g, const R *__restrict__ r, const T *__restrict__ ms, KronBand<T> B,
+               const T *__restrict__ in, T *out, KronDot kd) {
+    const int row = 3 * g.nx;
+    const int len = AXIS == 1 ? g.ny : g.nz;
+    const int nother = AXIS == 1 ? g.nz : g.ny;
+    const int nseg = (len + KSEG - 1) / KSEG;
+    const long long S = AXIS == 1 ? (long long)row : (long long)row * g.ny;
+    const long long items = (long long)row * nother * nseg;
+    double red[2] = {0.0, 0.0};
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < items;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(t % row);
+        const long long rest = t / row;
+        const int other = (int)(rest % nother), seg = (int)(rest / nother);
+        const long long base = AXIS == 1 ? (long long)other * row * g.ny + w : (long long)other * row + w;
+        const int c = w % 3;
+        const int p0 = seg * KSEG;
+        T win[KSEG + 2 * KRON_B];
+#pragma unroll
+        for (int k = 0; k < KSEG + 2 * KRON_B; k++) {
+            int p = p0 - KRON_B + k;
+            p = p < 0 ? 0 : (p > len - 1 ? len - 1 : p);
+            win[k] = in[base + p * S];
+        }
+        const T *mid = B.row(AXIS, c, len / 2);  // interior taps (the staged passes' tint)
+        // output k of the segment: the z pass finishes P^-1 and its dots
+        auto emit = [&](int k, T o) {
+            const int p = p0 + k;
+            if (p >= len) return;
+            const long long q = base + p * S;
+            if (AXIS == 2) {
+                const T m = ms[q], rv = (T)r[q];
+                const T z = m < T(0) ? rv : m * o;
+                out[q] = z;
+                if (DOT) {
+                    red[0] += (double)((float)z * (float)rv);
+                    red[1] += (double)((float)z * kd.q32[q]);
+                }
+            } else {
+                out[q] = o;
+            }
+        };
+        if (p0 >= KRON_B && p0 + KSEG <= len - KRON_B) {
+            T tap[KRON_W];
+#pragma unroll
+            for (int d = 0; d < KRON_W; d++) tap[d] = mid[d];
+#pragma unroll
+            for (int k = 0; k < KSEG; k++) {
+                T acc = T(0);
+#pragma unroll
+                for (int d = 0; d < KRON_W; d++) acc += tap[d] * win[k + d];
+                emit(k, acc);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < KSEG; k++) {
+                const int pos = p0 + k;
+                const T *tp = (pos >= KRON_B && pos < len - KRON_B) ? mid : B.row(AXIS, c, pos < len ? pos : len - 1);
+                T acc = T(0);
+#pragma unroll
+                for (int d = 0; d < KRON_W; d++) acc += tp[d] * win[k + d];
+                emit(k, acc);
+            }
+        }
+    }
+    if constexpr (DOT) {
+        double tot[2];
+        if (grid_reduce<KSEG_THREADS, 2>(red, kd.part, tot)) {
+            SolveScalars *S2 = kd.S;
+            S2->rho = tot[0];
+            S2->gam = tot[1];
+            S2->beta = S2->restart ? 0.0 : -tot[1] / S2->pq;
+            if (!isfinite(S2->beta)) S2->beta = 0.0;
+            S2->rescale = 0;
+        }
+    }
+}
+
 }  // namespace topo

@@ -459,7 +459,7 @@ int le_create(TopoLE **out, const LEParams *pp) {
     if (p.nx < 2 || p.ny < 2 || p.nz < 2 || p.ncp < 1 || p.tsc < 1 || p.nlvls < 1 || p.hx <= 0 || p.hy <= 0 ||
         p.hz <= 0 || p.t1 <= 0 || p.objective < 0 || p.objective > 7 ||
         p.load2_node >= (long long)p.nx * p.ny * p.nz || p.out_dof >= 3LL * p.nx * p.ny * p.nz ||
-        p.tile_form < 0 || p.tile_form > 1) {
+        p.tile_form < 0 || p.tile_form > 1 || p.kron_form < 0 || p.kron_form > 1) {
         set_error("invalid LinearElasticity parameters");
         return TOPO_ERR_ARG;
     }
@@ -1052,6 +1052,28 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     k_kron_x<T, T><<<(unsigned)((nlines + kx - 1) / kx), KRON_THREADS, smx, s>>>(
         g, kx, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
     timer_end(t, s);
+    if constexpr (std::is_same<T, float>::value) {
+        if (le->p.kron_form == 1) {  // y and z passes as register line segments (same outputs)
+            const unsigned gy = (unsigned)((kron_seg_items(g, 1) + KSEG_THREADS - 1) / KSEG_THREADS);
+            const unsigned gz = (unsigned)((kron_seg_items(g, 2) + KSEG_THREADS - 1) / KSEG_THREADS);
+            count_launch();
+            t = timer_begin(TOPO_KT_KRON, g.nn(), s);
+            k_kron_seg<T, T, 1, false><<<gy, KSEG_THREADS, 0, s>>>(g, r, sc, B, w.xa, w.xb, KronDot{});
+            timer_end(t, s);
+            count_launch();
+            t = timer_begin(TOPO_KT_KRON, g.nn(), s);
+            if (mixed && le->p.mass_precond_smooth <= 0) {
+                k_kron_seg<T, T, 2, true><<<gz, KSEG_THREADS, 0, s>>>(g, r, sc, B, w.xb, w.xa,
+                                                                       KronDot{fz->q32, fz->S, fz->part});
+                fz->dotted = true;
+            } else {
+                k_kron_seg<T, T, 2, false><<<gz, KSEG_THREADS, 0, s>>>(g, r, sc, B, w.xb, w.xa, KronDot{});
+            }
+            timer_end(t, s);
+            if (mixed) fz->scaled = true;
+            return w.xa;
+        }
+    }
     count_launch();
     t = timer_begin(TOPO_KT_KRON, g.nn(), s);
     k_kron_yz<T, T, 1, false><<<kron_yz_blocks(g, 1), KRON_THREADS, smy, s>>>(g, r, sc, B, w.xa, w.xb, KronDot{});
