@@ -23,7 +23,7 @@ def test_reference_arm_json_line():
     d = json.loads(lines[0])
     sys.path.insert(0, ROOT)
     import bench
-    assert d["metric"] == bench.METRIC  # the GB300 arm's metric: the driver compares the two lines
+    assert d["metric"] == bench.METRIC  # both arms report the same metric
     assert d["impl"] == "reference" and d["unit"] == "design_iter/s" and d["higher_is_better"] is True
     assert d["n_gpus"] == 1 and d["steps"] == 2 and d["warmup"] == 1
     assert d["value"] > 0.0 and abs(d["ms_per_step"] - 1e3 / d["value"]) < 1e-6 * d["ms_per_step"]
