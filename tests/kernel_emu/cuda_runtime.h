@@ -1,9 +1,9 @@
 // Test-only host stand-in for the CUDA qualifiers and builtins that the
 // kernel headers of topopt_in_petsc_transient_gb300/csrc name, so that their
 // kernels compile as host C++ and run on host threads (one std::thread per
-// CUDA thread, a std::barrier per CTA for __syncthreads).  Atomics and warp
-// shuffles are single-thread stand-ins: the emulated kernels run without
-// grid reductions.  Never part of the library.
+// CUDA thread, a std::barrier per CTA for __syncthreads, one CTA at a time).
+// Atomics are plain read-modify-writes: only thread 0 of a CTA issues them.
+// Never part of the library.
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -14,8 +14,13 @@
 #define __host__
 #define __forceinline__ inline
 #define __launch_bounds__(...)
-#define __shared__
+// CTAs run one after another, so a static local is the CTA's shared variable
+#define __shared__ static
 #define __align__(n) __attribute__((aligned(n)))
+namespace emu {
+extern unsigned char dyn_smem[];  // the dynamic shared memory of the running CTA
+}
+#define TOPO_DYNAMIC_SMEM(T, name) T *name = reinterpret_cast<T *>(emu::dyn_smem)
 struct emu_uint3 {
     unsigned x = 0, y = 0, z = 0;
 };
@@ -28,9 +33,16 @@ inline unsigned atomicAdd(unsigned *p, unsigned v) {
     *p += v;
     return o;
 }
+// every thread of the CTA calls the shuffles of a reduction the same number of
+// times: exchange through a CTA-shared buffer between two barriers
 template <class T>
-inline T __shfl_xor_sync(unsigned, T v, int) {
-    return v;
+inline T __shfl_xor_sync(unsigned, T v, int o) {
+    static T buf[1024];
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    const T r = buf[threadIdx.x ^ (unsigned)o];
+    __syncthreads();
+    return r;
 }
 using std::max;
 using std::min;

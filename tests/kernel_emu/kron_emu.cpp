@@ -12,8 +12,8 @@ thread_local emu_uint3 threadIdx, blockIdx;
 emu_uint3 blockDim, gridDim;
 static std::barrier<> *g_bar = nullptr;
 void __syncthreads() { g_bar->arrive_and_wait(); }
-namespace topo {
-unsigned char kron_smem[256 * 1024] __attribute__((aligned(16)));
+namespace emu {
+unsigned char dyn_smem[256 * 1024] __attribute__((aligned(16)));
 }
 
 template <class Body>

@@ -1,10 +1,11 @@
 """CPU execution of the device source of the alternative kernel forms: the
 z-marching slab operator kernel (slab.cuh) against the brick kernel
-(tile.cuh) for FP32, FP64 and double-float with one and two staged inputs,
-and the line-segment Kronecker passes against the staged ones (kron.cuh),
-compiled as host C++ (tests/kernel_emu/cuda_runtime.h) and run with one host
-thread per CUDA thread; outputs must agree bitwise and every node be written
-once."""
+(tile.cuh) for FP32, FP64 and double-float with one and two staged inputs
+and through the grid reduction of a policy with dot products, and the
+line-segment Kronecker passes against the staged ones (kron.cuh), compiled as
+host C++ (tests/kernel_emu/cuda_runtime.h) and run with one host thread per
+CUDA thread; outputs must agree bitwise, every node be written once, and the
+reduced sums match the host's."""
 import os
 import shutil
 import subprocess

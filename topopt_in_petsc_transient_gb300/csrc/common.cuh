@@ -14,6 +14,12 @@
 
 #include "../../include/topopt_gb300.h"
 
+// dynamic shared memory of a kernel: one declaration form for every kernel
+// (a host build of the kernel sources for tests may define it otherwise)
+#ifndef TOPO_DYNAMIC_SMEM
+#define TOPO_DYNAMIC_SMEM(T, name) extern __shared__ __align__(16) T name[]
+#endif
+
 namespace topo {
 
 // status codes TOPO_OK / TOPO_ERR_* come from the C ABI header

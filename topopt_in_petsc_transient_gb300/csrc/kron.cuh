@@ -171,7 +171,7 @@ template <class T, class R>
 static __global__ void __launch_bounds__(KRON_THREADS)
     k_kron_x(GridDesc g, int kx, R *r, const double *__restrict__ r64, const SolveScalars *S, const T *__restrict__ ms,
              KronBand<T> B, T *out) {
-    extern __shared__ __align__(16) unsigned char kron_smem[];
+    TOPO_DYNAMIC_SMEM(unsigned char, kron_smem);
     const int LP = kx_pitch(g.nx);
     T *tile = reinterpret_cast<T *>(kron_smem);  // [kx][3][LP]
     T *otile = tile + kx * 3 * LP;               // [kx][3][LP]
@@ -240,7 +240,7 @@ template <class T, class R, int AXIS, bool DOT>
 static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
     k_kron_yz(GridDesc g, const R *__restrict__ r, const T *__restrict__ ms, KronBand<T> B, const T *__restrict__ in,
               T *out, KronDot kd) {
-    extern __shared__ __align__(16) unsigned char kron_smem[];
+    TOPO_DYNAMIC_SMEM(unsigned char, kron_smem);
     const int len = AXIS == 1 ? g.ny : g.nz;
     T *tile = reinterpret_cast<T *>(kron_smem);  // [len][KW]
     T *tint = tile + (size_t)len * KW;           // [3][KRON_W]

@@ -166,7 +166,7 @@ __device__ __forceinline__ void slab_element(const ElemConst<T> &C, const Pol &p
 template <class T, class Pol>
 __global__ void __launch_bounds__(SLAB_THREADS, sizeof(T) == 4 ? 3 : 2)
     k_slab(const GridDesc g, const ElemConst<T> C, const Pol pol, const SlabShape sh) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TOPO_DYNAMIC_SMEM(unsigned char, smem_raw);
     T *sN = reinterpret_cast<T *>(smem_raw);       // [NIN][289][3] staged top node layer
     T *sEl = sN + Pol::NIN * SLAB_STAGED * 3;      // [2][256][EL_STRIDE] element layers
     if (pol_skip(pol, 0)) return;

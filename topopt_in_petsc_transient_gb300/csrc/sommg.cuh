@@ -174,7 +174,7 @@ __device__ void red_setup(const RedSys &R, double *sm, int *bad) {
 // forward sweep: CompleteInitialState (u0 = du0 = 0, M ddu0 = f(0),
 // LinearElasticity.cc:1049-1078) and every SolveStateBlock step (:1298-1397)
 static __global__ void k_red_forward(RedSys R) {
-    extern __shared__ __align__(16) double red_sm[];
+    TOPO_DYNAMIC_SMEM(double, red_sm);
     __shared__ int bad;
     const int kb = R.kb, k2 = kb * kb;
     if (threadIdx.x == 0) bad = 0;
@@ -286,7 +286,7 @@ __device__ __forceinline__ void red_outer(int kb, double *S, double c, const dou
 // accumulators S_K, S_M (lambda w' of ComputeSensitivitiesElementLoopn /
 // Loop0 :1911-2204) and S_oK, S_oM (the explicit dfx0 terms)
 static __global__ void k_red_adjoint(RedSys R) {
-    extern __shared__ __align__(16) double red_sm[];
+    TOPO_DYNAMIC_SMEM(double, red_sm);
     __shared__ int bad;
     __shared__ double hval;
     const int kb = R.kb, k2 = kb * kb;

@@ -225,7 +225,7 @@ __device__ __forceinline__ void tile_brick(const GridDesc &g, const ElemConst<T>
 
 template <class T, class Pol>
 __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(const GridDesc g, const ElemConst<T> C, const Pol pol) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TOPO_DYNAMIC_SMEM(unsigned char, smem_raw);
     T *sIn = reinterpret_cast<T *>(smem_raw);
     T *sEl = sIn + Pol::NIN * TILE_STAGED * 3;
     if (pol_skip(pol, 0)) return;
