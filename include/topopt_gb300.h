@@ -170,6 +170,17 @@ int topo_le_get_state(topo_le *le, int which, int j, double *out);
  * and GenerateCheckPoints' later files.  Checkpoints 1..ncp-1 are valid after
  * GenerateCheckPoints. */
 int topo_le_get_checkpoint(topo_le *le, int c, double *U, double *DU, double *DDU);
+/* initial displacement U0 (ndof values, DMDA order) for the next
+ * CompleteInitialState instead of rest: LinearElasticity::LoadSolutionAsU0
+ * with -onlyLoadDesign -solutionAsU0 (LinearElasticity.cc:2621-2677; U0 is the
+ * first record of the -restartFileVecSol file).  U0 = NULL restores u0 = 0.
+ * Full path only (the reduced path starts from rest). */
+int topo_le_set_initial_displacement(topo_le *le, const double *U0, int on_device);
+/* the vectors of LinearElasticity::WriteRestartFiles (RestartSol0x.dat,
+ * LinearElasticity.cc:2457-2496) into host arrays of ndof values: DDU0 the
+ * initial acceleration, LT the terminal adjoint of the last reverse sweep,
+ * DDL0 the adjoint acceleration at t = 0.  Full path only. */
+int topo_le_get_restart_state(topo_le *le, double *DDU0, double *LT, double *DDL0);
 /* weighted products K x and M x with the current densities (no masking) */
 int topo_le_apply_km(topo_le *le, const double *x, double *Kx, double *Mx);
 int topo_le_get_stats(topo_le *le, topo_le_stats *out);

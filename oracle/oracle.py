@@ -37,6 +37,7 @@ def lib():
         L.oracle_le_generate_checkpoints.argtypes = [C.c_void_p]
         L.oracle_le_compute_objective_sensitivities.argtypes = [C.c_void_p, dp, dp, dp]
         L.oracle_le_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.oracle_le_set_u0.argtypes = [C.c_void_p, dp]
         L.oracle_le_get_vectors.argtypes = [C.c_void_p, dp, dp, dp]
         L.oracle_le_get_newmark.argtypes = [C.c_void_p, dp, dp]
         L.oracle_le_get_initial_state.argtypes = [C.c_void_p, dp, dp, dp]
@@ -171,6 +172,10 @@ class LinearElasticity:
         U = np.zeros(self.ndof); DU = np.zeros(self.ndof); DDU = np.zeros(self.ndof)
         lib().oracle_le_get_initial_state(self._h, _p(U), _p(DU), _p(DDU))
         return U, DU, DDU
+
+    def set_u0(self, U0):
+        """LoadSolutionAsU0: initial displacement of the next CompleteInitialState (None: rest)."""
+        lib().oracle_le_set_u0(self._h, None if U0 is None else _p(_f64(U0)))
 
     def last_block_state(self, j):
         U = np.zeros(self.ndof); DU = np.zeros(self.ndof); DDU = np.zeros(self.ndof)

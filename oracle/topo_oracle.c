@@ -890,6 +890,16 @@ void oracle_le_volume_constraint(int nel, const double *xPhys, double volfrac, d
     for (int e = 0; e < nel; e++) dgdx[e] = 1.0 / nel;
 }
 
+/* LoadSolutionAsU0 (LinearElasticity.cc:2621-2677, called at :523 after
+ * VecSet(U0, 0)): the initial displacement of every CompleteInitialState;
+ * NULL restores rest */
+void oracle_le_set_u0(topo_oracle *o, const double *U0) {
+    if (U0)
+        memcpy(o->U0init, U0, sizeof(double) * o->ndof);
+    else
+        memset(o->U0init, 0, sizeof(double) * o->ndof);
+}
+
 int oracle_le_sizes(const topo_oracle *o, int *ndof, int *nel, int *Ts) {
     *ndof = o->ndof;
     *nel = o->nel;

@@ -61,6 +61,7 @@ int oracle_le_complete_initial_state(topo_oracle *o, const double *xPhys);
 int oracle_le_generate_checkpoints(topo_oracle *o);
 int oracle_le_compute_objective_sensitivities(topo_oracle *o, const double *xPhys, double *fx, double *dfdx);
 void oracle_le_volume_constraint(int nel, const double *xPhys, double volfrac, double *gx, double *dgdx);
+void oracle_le_set_u0(topo_oracle *o, const double *U0);
 /* introspection for tests */
 int oracle_le_sizes(const topo_oracle *o, int *ndof, int *nel, int *Ts);
 void oracle_le_get_vectors(const topo_oracle *o, double *N, double *P, double *RHS0);

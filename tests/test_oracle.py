@@ -190,6 +190,35 @@ def test_region_weighted_sensitivities_match_finite_differences(region, objectiv
         assert abs(fd - df[e]) <= 5e-7 * np.abs(df).max(), (region, e, fd, df[e])
 
 
+@pytest.mark.parametrize("objective", [0, 3, 5])
+def test_initial_displacement_sensitivities_match_finite_differences(objective):
+    # LoadSolutionAsU0 (-solutionAsU0, LinearElasticity.cc:2621-2677): the
+    # transient starts from a loaded displacement instead of rest; u0 enters
+    # the initial acceleration (K u0, LinearElasticity.cc:1049-1066) and the
+    # t = 0 sensitivities through dK u0
+    kw = dict(ncp=2, tsc=4, t1=0.8, objective=objective, loadsignal=1, dalpha=0.01, dbeta=0.01)
+    le = O.LinearElasticity(4, 2, 2, **kw)
+    rng = np.random.default_rng(30 + objective)
+    x = 0.3 + 0.4 * rng.random(le.nel)
+    N, _, _ = le.vectors()
+    u0 = N * 1e-2 * np.sin(np.arange(le.ndof) * 0.37)  # zero on clamped DOFs
+    rest = le.objective_sensitivities(x)[1]
+    le.set_u0(u0)
+    rc, fx, df = le.objective_sensitivities(x)
+    assert rc == 0 and np.isfinite(fx) and abs(fx - rest) > 1e-3 * abs(rest)
+    U0, DU0, DDU0 = le.initial_state()
+    assert np.array_equal(U0, u0) and not np.any(DU0)
+    h = 1e-5
+    for e in (0, 6, 13):
+        xp, xm = x.copy(), x.copy()
+        xp[e] += h
+        xm[e] -= h
+        fd = (le.objective_sensitivities(xp)[1] - le.objective_sensitivities(xm)[1]) / (2 * h)
+        assert abs(fd - df[e]) <= 5e-7 * np.abs(df).max(), (objective, e, fd, df[e])
+    le.set_u0(None)  # back to rest (the solves start warm: equal to their tolerance)
+    assert abs(le.objective_sensitivities(x)[1] - rest) <= 1e-10 * abs(rest)
+
+
 def test_reference_pulse_objective_fd():
     # reference load signal (Gaussian-modulated cosines, LinearElasticity.cc:597-606), t in [0, 16]
     kw = dict(ncp=4, tsc=10, t1=16.0, objective=0, loadsignal=0, Emax=1e3, Rmax=4.1667e-4, Rmin=4.1667e-7,

@@ -57,7 +57,7 @@ EXPORTS = [
     "topo_le_generate_checkpoints",
     "topo_le_compute_objective_sensitivities", "topo_le_compute_objective_sensitivities_dev",
     "topo_le_volume_constraint", "topo_le_volume_constraint_dev",
-    "topo_le_get_state", "topo_le_get_checkpoint", "topo_le_apply_km", "topo_le_get_stats", "topo_le_time_apply",
+    "topo_le_get_state", "topo_le_get_checkpoint", "topo_le_set_initial_displacement", "topo_le_get_restart_state", "topo_le_apply_km", "topo_le_get_stats", "topo_le_time_apply",
     "topo_le_kernel_timing", "topo_volume_constraint_noalloc_dev", "topo_le_reduced_system",
     "topo_box_element_matrices",
     "topo_pdefilt_create", "topo_pdefilt_destroy", "topo_pdefilt_filter_project", "topo_pdefilt_filter_project_dev",
@@ -103,6 +103,8 @@ def load(path=None):
         "topo_le_volume_constraint": (ip, [vp, dp, vp, vp, d]),
         "topo_le_volume_constraint_dev": (ip, [vp, dp, vp, vp, d]),
         "topo_le_get_checkpoint": (ip, [vp, ip, vp, vp, vp]),
+        "topo_le_set_initial_displacement": (ip, [vp, vp, ip]),
+        "topo_le_get_restart_state": (ip, [vp, vp, vp, vp]),
         "topo_le_get_state": (ip, [vp, ip, ip, vp]),
         "topo_le_apply_km": (ip, [vp, vp, vp, vp]),
         "topo_le_get_stats": (ip, [vp, C.POINTER(LEStats)]),

@@ -212,6 +212,16 @@ int topo_le_get_checkpoint(topo_le *le, int c, double *U, double *DU, double *DD
     return le_get_checkpoint(le->impl, c, U, DU, DDU);
 }
 
+int topo_le_set_initial_displacement(topo_le *le, const double *U0, int on_device) {
+    if (!le) return TOPO_ERR_ARG;
+    return le_set_initial_displacement(le->impl, U0, on_device);
+}
+
+int topo_le_get_restart_state(topo_le *le, double *DDU0, double *LT, double *DDL0) {
+    if (!le || !DDU0 || !LT || !DDL0) return TOPO_ERR_ARG;
+    return le_get_restart_state(le->impl, DDU0, LT, DDL0);
+}
+
 int topo_le_set_output(topo_le *le, topo_mpiio *io) {
     if (!le) return TOPO_ERR_ARG;
     return le_set_output(le->impl, io);

@@ -388,6 +388,10 @@ struct TopoLE {
     double *Lp1 = nullptr, *DLp1 = nullptr, *DDLp1 = nullptr, *DLc = nullptr, *DDLc = nullptr, *Lp2 = nullptr, *Lp3 = nullptr;
     double *KL = nullptr, *ML = nullptr, *hK = nullptr, *hM = nullptr;
     double *DDL0 = nullptr;
+    // restart vectors: LT the terminal adjoint of the last reverse sweep
+    // (RestartSol0x.dat), u0init a loaded initial displacement (-solutionAsU0;
+    // null: u0 = 0)
+    double *LT = nullptr, *u0init = nullptr;
     double *df = nullptr;
     // per-node sensitivity combinations: FP64 (2 x ndof) or FP32 (5 x ndof)
     double *sw64 = nullptr;
@@ -555,6 +559,7 @@ int le_alloc(TopoLE *le) {
     AG(le->hK, nd);
     AG(le->hM, nd);
     AG(le->DDL0, nd);
+    AG(le->LT, nd);
     AG(le->df, ne);
     if (p.mixed && p.sens_fp32)
         AG(le->sw32, 5 * nd);
@@ -782,6 +787,7 @@ void le_destroy(TopoLE *le) {
     if (!le) return;
     if (le->gx_fwd) cudaGraphExecDestroy(le->gx_fwd);
     if (le->gx_adj) cudaGraphExecDestroy(le->gx_adj);
+    if (le->u0init) cudaFree(le->u0init);
     le->arena.release();
     if (le->stream) cudaStreamDestroy(le->stream);
     delete le;
@@ -1791,6 +1797,10 @@ static int run_block(TopoLE *le, int c, int adjoint) {
             int rc = adjoint ? adj_step(le, false) : fwd_step(le, false);
             if (rc) return rc;
         }
+        if (adjoint && j == 0 && c == le->p.ncp - 1) {  // the terminal adjoint L(T) (LT, LinearElasticity.cc:882-888)
+            count_launch();
+            k_copy<<<ew_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, le->Lp1, le->LT);
+        }
     }
     CK(cudaGetLastError());
     return TOPO_OK;
@@ -2121,6 +2131,8 @@ int le_complete_initial_state(TopoLE *le, const double *xPhys_dev, double Emin, 
     // (LinearElasticity.cc:1046-1078); u0 = du0 = 0 (LinearElasticity.cc:521-587)
     long long nd = le->ndof;
     CK(cudaMemsetAsync(le->cp, 0, sizeof(double) * 3 * nd, s));
+    if (le->u0init)  // LoadSolutionAsU0 (LinearElasticity.cc:2621-2677)
+        CK(cudaMemcpyAsync(le->cp, le->u0init, sizeof(double) * nd, cudaMemcpyDeviceToDevice, s));
     product<true, false>(le, le->cp, le->KL, nullptr, 1.0, 0.0);
     product<true, true>(le, le->cp + nd, le->ML, nullptr, p.dbeta, p.dalpha);
     double s0 = 0.0;
@@ -2250,6 +2262,50 @@ int le_get_checkpoint(TopoLE *le, int c, double *U, double *DU, double *DDU) {
     CK(cudaMemcpyAsync(U, base, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
     CK(cudaMemcpyAsync(DU, base + nd, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
     CK(cudaMemcpyAsync(DDU, base + 2 * nd, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaStreamSynchronize(le->stream));
+    return TOPO_OK;
+}
+
+int le_set_initial_displacement(TopoLE *le, const double *U0, int on_device) {
+    if (le->kb) {
+        set_error("an initial displacement needs the full path: the reduced path starts from rest");
+        return TOPO_ERR_ARG;
+    }
+    const long long nd = le->ndof;
+    if (!U0) {
+        if (le->u0init) cudaFree(le->u0init);
+        le->u0init = nullptr;
+        le->design_ready = 0;
+        return TOPO_OK;
+    }
+    if (!le->u0init) {
+        cudaError_t e = cudaMalloc(&le->u0init, sizeof(double) * nd);
+        if (e != cudaSuccess) {
+            le->u0init = nullptr;
+            set_error(std::string("initial displacement: ") + cudaGetErrorString(e));
+            return TOPO_ERR_OOM;
+        }
+    }
+    CK(cudaMemcpyAsync(le->u0init, U0, sizeof(double) * nd, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       le->stream));
+    CK(cudaStreamSynchronize(le->stream));
+    le->design_ready = 0;  // CompleteInitialState must run again
+    return TOPO_OK;
+}
+
+int le_get_restart_state(TopoLE *le, double *DDU0, double *LT, double *DDL0) {
+    if (le->kb) {
+        set_error("RestartSol vectors are kept on the full path only");
+        return TOPO_ERR_ARG;
+    }
+    if (!le->design_ready) {
+        set_error("restart vectors requested before CompleteInitialState");
+        return TOPO_ERR_STATE;
+    }
+    const long long nd = le->ndof;
+    CK(cudaMemcpyAsync(DDU0, le->cp + 2 * nd, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaMemcpyAsync(LT, le->LT, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
+    CK(cudaMemcpyAsync(DDL0, le->DDL0, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
     CK(cudaStreamSynchronize(le->stream));
     return TOPO_OK;
 }

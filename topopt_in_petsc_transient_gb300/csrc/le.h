@@ -24,6 +24,8 @@ int le_compute_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_dev)
 int le_get_state(TopoLE *le, int which, int j, double *host_out);
 int le_get_checkpoint(TopoLE *le, int c, double *U, double *DU, double *DDU);
 int le_set_output(TopoLE *le, topo_mpiio *io);
+int le_set_initial_displacement(TopoLE *le, const double *U0, int on_device);
+int le_get_restart_state(TopoLE *le, double *DDU0, double *LT, double *DDL0);
 int le_apply_km(TopoLE *le, const double *x_dev, double *Kx_dev, double *Mx_dev);
 int le_stats(TopoLE *le, LEStats *out);
 long long le_nel(const TopoLE *le);

@@ -231,6 +231,52 @@ class LinearElasticity:
             write_petsc_vecs(os.path.join(directory, "cp%04d.dat" % c), list(self.checkpoint(c)))
         return 0
 
+    def restart_state(self):
+        """(DDU0, LT, DDL0): the initial acceleration, the terminal adjoint of
+        the last reverse sweep and the adjoint acceleration at t = 0."""
+        out = [np.zeros(self.ndof) for _ in range(3)]
+        check(_lib.load().topo_le_get_restart_state(self._h, *[a.ctypes.data for a in out]), "restart state")
+        return tuple(out)
+
+    def WriteRestartFiles(self, directory):
+        """LinearElasticity::WriteRestartFiles (LinearElasticity.cc:2457-2496):
+        DDU0, LT, DDL0 into RestartSol00.dat / RestartSol01.dat, the two sets
+        alternating (flip starts true, LinearElasticity.cc:2685); returns the
+        file written."""
+        import os
+        self._flip = not getattr(self, "_flip", True)
+        path = os.path.join(directory, "RestartSol%s.dat" % ("01" if self._flip else "00"))
+        write_petsc_vecs(path, list(self.restart_state()))
+        return path
+
+    def set_initial_displacement(self, U0):
+        """Initial displacement for the next CompleteInitialState (None: rest)."""
+        if U0 is None:
+            check(_lib.load().topo_le_set_initial_displacement(self._h, None, 0), "initial displacement")
+            return
+        dev, a = _addr(U0, self.ndof, "U0")
+        check(_lib.load().topo_le_set_initial_displacement(self._h, a, int(dev)), "initial displacement")
+
+    def LoadSolutionAsU0(self, path):
+        """LinearElasticity::LoadSolutionAsU0 with -onlyLoadDesign -solutionAsU0
+        (LinearElasticity.cc:2621-2677): the first record of the PETSc vector
+        file `path` (-restartFileVecSol) becomes the initial displacement."""
+        U0 = np.zeros(self.ndof)
+        read_petsc_vecs(path, [U0])
+        self.set_initial_displacement(U0)
+        return U0
+
+    def LoadRestartSol(self, path):
+        """The -restartFileVecSol read of SetUpSolver1/2
+        (LinearElasticity.cc:2716-2738): DDU0, LT, DDL0 from a RestartSol file,
+        checked against this mesh.  The reference uses them only as starting
+        guesses of three Krylov solves; the GPU solves start from their own
+        predictors, which gives the same solutions to the solve tolerance, so
+        the vectors are returned, not installed."""
+        out = [np.zeros(self.ndof) for _ in range(3)]
+        read_petsc_vecs(path, out)
+        return tuple(out)
+
     def apply_km(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
         K = np.zeros(self.ndof)
