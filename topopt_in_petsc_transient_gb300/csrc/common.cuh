@@ -230,20 +230,6 @@ __host__ __device__ __forceinline__ void mode_khat_mass(const ElemConst<T> &C, T
     }
 }
 
-// y_e = ck * KE u_e + cm * ME u_e for one element: in/out indexed [comp][L]
-template <class T>
-__host__ __device__ __forceinline__ void elem_apply(const ElemConst<T> &C, T ck, T cm, T u[3][8], T y[3][8]) {
-#pragma unroll
-    for (int c = 0; c < 3; c++) mode_fwd(u[c]);
-    mode_stiffness(C, u, y);
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-#pragma unroll
-        for (int m = 0; m < 8; m++) y[c][m] = ck * y[c][m] + (cm * C.W[m]) * u[c][m];
-        mode_bwd(y[c]);
-    }
-}
-
 // ---------------------------------------------------------------------------
 // deterministic grid-wide reductions: per-CTA partials, last CTA sums in a
 // fixed order (no floating-point atomics, bitwise reproducible)
