@@ -324,3 +324,31 @@ def test_density_and_sensitivity_filter_restatement():
     # anisotropic elements: ElemConn from the smallest size, per-axis upper limits
     Ha = np.stack([O.dens_filter_apply(*n, np.eye(nel)[k], 2.5, h=(1.0, 2.0, 1.0)) for k in range(nel)], 1)
     assert Ha[0, 0] == 2.5 and Ha[0, 6] == 0.5 and Ha[6, 0] == 0.5
+
+
+def test_increase_beta_host_logic_matches_oracle():
+    # Filter::IncreaseBeta (Filter.cc:273-300): the host mirror and the oracle
+    # on every branch (change by +1 below 7, by 20% above, capped at betaFinal
+    # with the change revoked, blocked by gx > 0 or by ch >= 0.01 off the
+    # every-10th iteration)
+    from topopt_in_petsc_transient_gb300.topopt import Filter
+    for beta in (0.1, 1.0, 6.5, 7.0, 20.0, 47.0, 48.0):
+        for gx in (-0.1, 0.0, 1e-9):
+            for itr in (9, 10, 11):
+                for ch in (0.005, 0.01, 0.2):
+                    got = Filter.IncreaseBeta(beta, 48.0, gx, itr, ch)
+                    ref = O.increase_beta(beta, 48.0, gx, itr, ch)
+                    assert got == ref, (beta, gx, itr, ch, got, ref)
+
+
+def test_volume_constraint_and_load_signals():
+    # VolumeConstraint (LinearElasticity.cc:1283-1296) and the two load
+    # signals: the reference pulse (LinearElasticity.cc:597-606) peaks at
+    # t = 8 with value 1, the workload's sin(2 pi t) stops at t = 0.5
+    x = np.linspace(0.0, 1.0, 11)
+    gx, dg = O.volume_constraint(x, 0.3)
+    assert abs(gx - (x.mean() - 0.3)) < 1e-15 and np.all(dg == 1.0 / x.size)
+    assert O.load_signal(0, 8.0) == 1.0
+    assert abs(O.load_signal(0, 8.0 + 1e-3)) < 1.0
+    assert abs(O.load_signal(1, 0.25) - 1.0) < 1e-15 and abs(O.load_signal(1, 0.125) - 0.5 ** 0.5) < 1e-15
+    assert O.load_signal(1, 0.0) == 0.0 and O.load_signal(1, 0.75) == 0.0
