@@ -1,5 +1,6 @@
 // Runs the real k_kron_yz (staged lines) and k_kron_seg (line segments)
-// sources on host threads and compares the y and z passes value by value.
+// sources on host threads and compares the y and z passes value by value, and
+// the two index forms of k_kron_x.
 #include <barrier>
 #include <cstdio>
 #include <random>
@@ -62,8 +63,47 @@ static bool compare(int nx, int ny, int nz) {
     return diff == 0 && unset == 0;
 }
 
+// x pass: divided and incremental index forms, with and without the
+// replacement rescale (which also rewrites r from the FP64 residual)
+static bool compare_x(int nx, int ny, int nz, int kx, bool rescale) {
+    using namespace topo;
+    GridDesc g{nx, ny, nz, nx - 1, ny - 1, nz - 1};
+    const long long nd = 3 * g.nn();
+    const int nmax = std::max(nx, std::max(ny, nz));
+    std::mt19937_64 rng(nx * 17 + ny * 5 + nz + kx);
+    std::uniform_real_distribution<float> U(-1.0f, 1.0f);
+    std::vector<float> tab((size_t)9 * nmax * KRON_W), ms(nd), ra(nd), rb(nd), a(nd, -7.0f), b(nd, -7.0f);
+    std::vector<double> r64(nd);
+    for (auto &v : tab) v = U(rng);
+    for (auto &v : ms) v = U(rng);
+    for (auto &v : ra) v = U(rng);
+    for (auto &v : r64) v = U(rng);
+    rb = ra;
+    SolveScalars S{};
+    S.rescale = rescale ? 1 : 0;
+    S.sigma = 1.75;
+    KronBand<float> B{tab.data(), nmax};
+    const unsigned grid = (unsigned)(((long long)ny * nz + kx - 1) / kx);
+    run_grid(grid, KRON_THREADS,
+             [&] { k_kron_x<float, float>(g, kx, ra.data(), r64.data(), &S, ms.data(), B, a.data()); });
+    run_grid(grid, KRON_THREADS,
+             [&] { k_kron_xi<float, float>(g, kx, rb.data(), r64.data(), &S, ms.data(), B, b.data()); });
+    long diff = 0, unset = 0;
+    for (long long i = 0; i < nd; i++) {
+        if (a[i] != b[i] || ra[i] != rb[i]) diff++;
+        if (b[i] == -7.0f) unset++;
+    }
+    std::printf("x pass grid %dx%dx%d, %d lines per CTA%s: differences %ld, unwritten %ld\n", nx, ny, nz, kx,
+                rescale ? ", rescale" : "", diff, unset);
+    return diff == 0 && unset == 0;
+}
+
 int main() {
     bool ok = true;
+    ok &= compare_x(5, 4, 3, 3, false);    // row 15 < block: many lines per trip
+    ok &= compare_x(97, 6, 5, 8, true);    // row 291 > block
+    ok &= compare_x(193, 3, 4, 2, false);  // row 579
+    ok &= compare_x(40, 7, 9, 5, true);
     ok &= compare<1>(5, 40, 3);
     ok &= compare<2>(5, 3, 40);
     ok &= compare<1>(11, 17, 9);

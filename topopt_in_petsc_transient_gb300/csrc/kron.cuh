@@ -167,10 +167,13 @@ __host__ inline int kx_lines_launch(const GridDesc &g, size_t elem, long long sl
     return (int)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
-template <class T, class R>
-static __global__ void __launch_bounds__(KRON_THREADS)
-    k_kron_x(GridDesc g, int kx, R *r, const double *__restrict__ r64, const SolveScalars *S, const T *__restrict__ ms,
-             KronBand<T> B, T *out) {
+// INCR: the thread's (line, position) and (row, group) indices advance with
+// carries as t steps by the block size (one integer division per thread
+// instead of one per value); the same mapping as the divided form
+template <class T, class R, bool INCR>
+__device__ __forceinline__ void kron_x_body(const GridDesc &g, int kx, R *r, const double *__restrict__ r64,
+                                            const SolveScalars *S, const T *__restrict__ ms, const KronBand<T> &B,
+                                            T *out) {
     TOPO_DYNAMIC_SMEM(unsigned char, kron_smem);
     const int LP = kx_pitch(g.nx);
     T *tile = reinterpret_cast<T *>(kron_smem);  // [kx][3][LP]
@@ -185,9 +188,16 @@ static __global__ void __launch_bounds__(KRON_THREADS)
     kron_stage_interior(B, 0, g.nx, tint);
     const long long q0 = line0 * row;
     const int nv = nl * row;
+    // line l and position w of value t = l row + w, and their step per trip
+    const int sl = KRON_THREADS / row, sw = KRON_THREADS - sl * row;
+    int l = (int)threadIdx.x / row, w = (int)threadIdx.x - l * row;
 #pragma unroll 4
     for (int t = threadIdx.x; t < nv; t += KRON_THREADS) {
-        const int l = t / row, w = t - l * row, i = w / 3, c = w - 3 * i;
+        if (!INCR) {
+            l = t / row;
+            w = t - l * row;
+        }
+        const int i = w / 3, c = w - 3 * i;
         const long long q = q0 + t;
         R rv;
         if (rs) {
@@ -198,25 +208,75 @@ static __global__ void __launch_bounds__(KRON_THREADS)
         }
         const T m = ms[q];
         tile[(l * 3 + c) * LP + i] = m < T(0) ? T(0) : (T)rv * m;
+        if (INCR) {
+            l += sl;
+            w += sw;
+            if (w >= row) {
+                w -= row;
+                l++;
+            }
+        }
     }
     __syncthreads();
     const int ngrp = (g.nx + KRON_MP - 1) / KRON_MP;
     const int nrows = nl * 3;
+    const int sgrp = KRON_THREADS / nrows, sr = KRON_THREADS - sgrp * nrows;
+    int rw = (int)threadIdx.x % nrows, grp = (int)threadIdx.x / nrows;
     for (int t = threadIdx.x; t < nrows * ngrp; t += KRON_THREADS) {
-        const int rw = t % nrows, grp = t / nrows, c = rw % 3;
+        if (!INCR) {
+            rw = t % nrows;
+            grp = t / nrows;
+        }
+        const int c = rw % 3;
         const int p0 = grp * KRON_MP;
         T o[KRON_MP];
         kron_line(tile + rw * LP, 1, g.nx, p0, tint, B, 0, c, o);
 #pragma unroll
         for (int k = 0; k < KRON_MP; k++)
             if (p0 + k < g.nx) otile[rw * LP + p0 + k] = o[k];
+        if (INCR) {
+            grp += sgrp;
+            rw += sr;
+            if (rw >= nrows) {
+                rw -= nrows;
+                grp++;
+            }
+        }
     }
     __syncthreads();
+    l = (int)threadIdx.x / row;
+    w = (int)threadIdx.x - l * row;
 #pragma unroll 4
     for (int t = threadIdx.x; t < nv; t += KRON_THREADS) {
-        const int l = t / row, w = t - l * row, i = w / 3, c = w - 3 * i;
+        if (!INCR) {
+            l = t / row;
+            w = t - l * row;
+        }
+        const int i = w / 3, c = w - 3 * i;
         out[q0 + t] = otile[(l * 3 + c) * LP + i];
+        if (INCR) {
+            l += sl;
+            w += sw;
+            if (w >= row) {
+                w -= row;
+                l++;
+            }
+        }
     }
+}
+
+template <class T, class R>
+static __global__ void __launch_bounds__(KRON_THREADS)
+    k_kron_x(GridDesc g, int kx, R *r, const double *__restrict__ r64, const SolveScalars *S, const T *__restrict__ ms,
+             KronBand<T> B, T *out) {
+    kron_x_body<T, R, false>(g, kx, r, r64, S, ms, B, out);
+}
+// the incremental-index form (kron_form = 1), held to 64 registers (4 CTAs per SM)
+template <class T, class R>
+static __global__ void __launch_bounds__(KRON_THREADS, 4)
+    k_kron_xi(GridDesc g, int kx, R *r, const double *__restrict__ r64, const SolveScalars *S,
+              const T *__restrict__ ms, KronBand<T> B, T *out) {
+    kron_x_body<T, R, true>(g, kx, r, r64, S, ms, B, out);
 }
 
 // y pass (AXIS 1) and z pass (AXIS 2): a CTA stages a chunk of KW values of

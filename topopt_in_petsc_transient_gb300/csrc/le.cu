@@ -1047,6 +1047,8 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     static bool attr = false;
     if (!attr) {  // staged lines: the selection keeps every pass within KRON_SMEM_MAX
         cudaFuncSetAttribute(k_kron_x<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
+        if constexpr (std::is_same<T, float>::value)
+            cudaFuncSetAttribute(k_kron_xi<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
         cudaFuncSetAttribute(k_kron_yz<T, T, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
         cudaFuncSetAttribute(k_kron_yz<T, T, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
         cudaFuncSetAttribute(k_kron_yz<T, T, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
@@ -1055,8 +1057,16 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     bool t;
     count_launch();
     t = timer_begin(TOPO_KT_KRON, g.nn(), s);
-    k_kron_x<T, T><<<(unsigned)((nlines + kx - 1) / kx), KRON_THREADS, smx, s>>>(
-        g, kx, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
+    bool incr = false;
+    if constexpr (std::is_same<T, float>::value) {
+        incr = le->p.kron_form == 1;
+        if (incr)  // incremental indices (same outputs)
+            k_kron_xi<T, T><<<(unsigned)((nlines + kx - 1) / kx), KRON_THREADS, smx, s>>>(
+                g, kx, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
+    }
+    if (!incr)
+        k_kron_x<T, T><<<(unsigned)((nlines + kx - 1) / kx), KRON_THREADS, smx, s>>>(
+            g, kx, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
     timer_end(t, s);
     if constexpr (std::is_same<T, float>::value) {
         if (le->p.kron_form == 1) {  // y and z passes as register line segments (same outputs)
