@@ -260,7 +260,9 @@ constexpr int tile_class() {
 template <class T, class Pol>
 static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, cudaStream_t s) {
     // z-marching slabs (slab.cuh) for the FP32 and double-float kernels; the
-    // FP64 ones keep the brick form (their carried corners would spill)
+    // FP64 ones keep the brick form (their carried corners would spill), and
+    // so does a grid whose slabs would fill less than half the resident slots
+    // (small meshes, coarse multigrid levels)
     if constexpr (!std::is_same<T, double>::value) if (g_tile_form == 1) {
         static long long slots = 0;
         const size_t sm = slab_smem_bytes<T, Pol>();
@@ -273,11 +275,13 @@ static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol
             slots = (long long)std::max(1, per_sm) * std::max(1, nsm);
         }
         const SlabShape sh = slab_shape(g, slots);
-        const bool timed = tile_class<T, Pol>() >= 0 && timer_begin(tile_class<T, Pol>(), g.nn(), s);
-        count_launch();
-        k_slab<T, Pol><<<(unsigned)(sh.ncx * sh.ncy * sh.nzr), SLAB_THREADS, sm, s>>>(g, C, pol, sh);
-        timer_end(timed, s);
-        return;
+        if (2LL * sh.ncx * sh.ncy * sh.nzr >= slots) {
+            const bool timed = tile_class<T, Pol>() >= 0 && timer_begin(tile_class<T, Pol>(), g.nn(), s);
+            count_launch();
+            k_slab<T, Pol><<<(unsigned)(sh.ncx * sh.ncy * sh.nzr), SLAB_THREADS, sm, s>>>(g, C, pol, sh);
+            timer_end(timed, s);
+            return;
+        }
     }
     static int resident = 0;
     const size_t sm = tile_smem_bytes<T, Pol>();
