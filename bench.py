@@ -1,17 +1,26 @@
 """Throughput of the transient forward + adjoint design iteration on GB300.
 
-Workload (the cantilever the headline metric is quoted on): 96x48x48 unit hex8
-elements (698,691 DOFs), E0 = 1, Emin = 1e-9, nu = 0.3, mass density 1, SIMP
-p = 3, Rayleigh alpha = 0, beta = 1e-3, clamped face x = 0, line load at the
-mid line of face x = nelx with f(t) = sin(2 pi t) for t < 0.5, 200 Newmark
-steps of dt = 0.005, uniform density 0.12, PDE filter radius 2, MMA, 5
-multigrid levels.  Objective: reference objective 3 (potential energy, the
-reference-expressible form of time-integrated compliance).  Synthetic inputs
-(no dataset is involved).
+Workload (the cantilever the headline metric is quoted on): 192x96x96 unit
+hex8 elements (5,447,811 DOFs), E0 = 1, Emin = 1e-9, nu = 0.3, mass density 1,
+SIMP p = 3, Rayleigh alpha = 0, beta = 1e-3, clamped face x = 0, line load at
+the mid line of face x = nelx with f(t) = sin(2 pi t) for t < 0.5 plus a second
+point load at a seeded node with a seeded phase, 400 Newmark steps of
+dt = 0.0025 in 20 checkpoint blocks of 20 steps, initial density 0.12 plus
+seeded U(-0.02, 0.02) noise, PDE filter radius 2, MMA, 6 multigrid levels.
+Objective: reference objective 3 (potential energy, the reference-expressible
+form of time-integrated compliance).  Synthetic inputs (no dataset is
+involved).
 
 A "step" is one design iteration of main.cc's loop: CompleteInitialState,
-ComputeObjectiveSensitivities (forward + adjoint + sensitivities),
-VolumeConstraint, Filter::Gradients, MMA::Update, Filter::FilterProject.
+GenerateCheckPoints, ComputeObjectiveSensitivities (forward + adjoint +
+sensitivities), VolumeConstraint, Filter::Gradients, MMA::Update,
+Filter::FilterProject.
+
+Besides the timed legs the line carries the accuracy of the mixed and plain
+paths against the FP64 oracle on one full design evaluation of the
+96x48x48 cantilever (200 steps, not extrapolated), and a central
+finite-difference check of the adjoint sensitivities on seeded elements of
+the headline workload.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
@@ -156,6 +165,61 @@ def replica_value(steps, ws, t_job):
     return ws * steps / t_job
 
 
+MAT6 = ("Emin", "Emax", "Rmin", "Rmax", "penalK", "penalM")
+
+
+def make_physics(o, **over):
+    """A LinearElasticity object for the TopOpt options `o` (the constructor
+    call of main.cc:33), with solver options overridden by `over`."""
+    from topopt_in_petsc_transient_gb300 import LinearElasticity
+    kw = dict(nlvls=o.nlvls, ncp=o.ncp, tsc=o.tsc, t1=o.t1, objective=o.objective, dalpha=o.dalpha,
+              dbeta=o.dbeta, loadsignal=o.loadsignal, mixed=o.mixed, rtol=o.rtol, smooth=o.smooth,
+              cheb_ratio=o.cheb_ratio, use_graphs=o.use_graphs, coarse_dense_max=o.coarse_dense_max,
+              coarse_smooth=o.coarse_smooth, sens_fp32=o.sens_fp32, inner_tol=o.inner_tol,
+              inner_maxit=o.inner_maxit, reduction=o.reduction, basis=o.basis, omega0=o.omega0,
+              load2_node=o.load2_node, load2_phase=o.load2_phase, out_dof=o.out_dof, tile_form=o.tile_form,
+              kron_form=o.kron_form)
+    kw.update(over)
+    return LinearElasticity(o.nelx, o.nely, o.nelz, **kw)
+
+
+def evaluate(ph, o, xPhys):
+    """CompleteInitialState + GenerateCheckPoints + ComputeObjectiveSensitivities
+    (main.cc:82-90) on device xPhys; returns (fx, dfdx tensor)."""
+    import torch
+    ph.CompleteInitialState(xPhys, *[getattr(o, k) for k in MAT6])
+    ph.GenerateCheckPoints()
+    df = torch.zeros_like(xPhys)
+    fx = ph.ComputeObjectiveSensitivities(df)
+    return fx, df
+
+
+def timed_iterations(opt, k, flush_l2, events=True):
+    """k design iterations, each bracketed by CUDA events after an L2 flush;
+    returns the per-iteration seconds and objectives."""
+    import torch
+
+    from topopt_in_petsc_transient_gb300 import design_iteration
+    times, fxs = [], []
+    for _ in range(k):
+        flush_l2()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("timed_design_iteration")  # lets a profiler select the timed region
+        e0.record()
+        fx = design_iteration(opt)[0]  # every library call returns synchronised
+        e1.record()
+        e1.synchronize()
+        torch.cuda.nvtx.range_pop()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        fxs.append(fx)
+    return times, fxs
+
+
+def spread(times):
+    return {"min_s": min(times), "median_s": statistics.median(times), "max_s": max(times)}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -183,27 +247,18 @@ def run_gb300(args):
     # ---- headline: mixed-precision path, design vectors resident in HBM ----
     wl = workload(args)
     opt = TopOpt(mixed=True, **wl).setup()
-    for _ in range(args.warmup):
+    xphys0 = opt.xPhys.clone()  # the filtered initial design (finite-difference check)
+    raw = {}
+    for w in range(args.warmup):
+        if w == 0:  # the unscaled, unfiltered sensitivities of iteration 1 (mixed vs plain)
+            raw["mixed"] = evaluate(opt.physics, opt, opt.xPhys)
         design_iteration(opt)
     le_stats0 = opt.physics.stats()
     launches0 = L.topo_kernel_launches()
     barrier()
     sampler = ClockSampler(local)
     sampler.start()
-    times = []
-    fxs = []
-    for _ in range(args.steps):
-        flush_l2()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.nvtx.range_push("timed_design_iteration")  # lets a profiler select the timed region
-        e0.record()
-        fx, fxs_, gx, ch, mnd = design_iteration(opt)  # every library call returns synchronised
-        e1.record()
-        e1.synchronize()
-        torch.cuda.nvtx.range_pop()
-        times.append(e0.elapsed_time(e1) / 1e3)
-        fxs.append(fx)
+    times, fxs = timed_iterations(opt, args.steps, flush_l2)
     barrier()
     clocks = sampler.stop()
     le_stats1 = opt.physics.stats()
@@ -214,37 +269,29 @@ def run_gb300(args):
     iters_per_solve = ((le_stats1["cg_iterations"] - le_stats0["cg_iterations"]) /
                        max(1, le_stats1["solves"] - le_stats0["solves"]))
 
-    # ---- plain FP64 path and objective agreement on the same initial design ----
+    # ---- plain FP64 path: the same design iterations (after the same
+    # number of warm-up iterations), and iteration 1's objective and
+    # sensitivities against the mixed path's on the same initial design ----
     plain = None
     if args.plain_steps > 0:
-        # both paths from the same uniform design: objective and sensitivity
-        # agreement on the first iteration; the plain path is then timed on
-        # the same iterations as the headline (after the warm-up iterations)
-        a = TopOpt(mixed=True, **wl).setup()
         b = TopOpt(mixed=False, **wl).setup()
-        fa = design_iteration(a)[0]
-        dfa = a.dfdx.clone()
-        fb = design_iteration(b)[0]
-        dfb = b.dfdx.clone()
-        del a
-        for _ in range(max(0, args.warmup - 1)):
+        for w in range(args.warmup):
+            if w == 0:
+                raw["plain"] = evaluate(b.physics, b, b.xPhys)
             design_iteration(b)
-        torch.cuda.synchronize()
-        tp = []
-        for k in range(args.plain_steps):
-            flush_l2()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            design_iteration(b)
-            e1.record()
-            e1.synchronize()
-            tp.append(e0.elapsed_time(e1) / 1e3)
+        tp, _ = timed_iterations(b, args.plain_steps, flush_l2)
+        (fa, dfa), (fb, dfb) = raw["mixed"], raw["plain"]
+        same = min(args.steps, args.plain_steps)
         plain = {"value": len(tp) / sum(tp), "unit": UNIT, "steps": len(tp), "warmup": args.warmup,
+                 "iterations": "design iterations %d..%d, as the headline" % (args.warmup + 1,
+                                                                             args.warmup + len(tp)),
+                 "seconds": spread(tp), "mixed_seconds": spread(times),
                  "objective_rel_diff_mixed_vs_plain": abs(fa - fb) / abs(fb),
                  "dfdx_maxrel_diff_mixed_vs_plain": float((dfa - dfb).abs().max() / dfb.abs().max()),
-                 "speedup_mixed_over_plain": value / ws / (len(tp) / sum(tp))}
+                 "speedup_mixed_over_plain": value / ws / (len(tp) / sum(tp)),
+                 "speedup_same_iterations": sum(tp[:same]) / sum(times[:same])}
         del b
+    raw.clear()
 
     # ---- end to end through the C ABI with host buffers ----
     e2e = None
@@ -252,12 +299,66 @@ def run_gb300(args):
         e2e = run_e2e(args, wl, flush_l2)
 
     # ---- roofline of the dominant kernels, timed in the solve ----
-    # One extra design iteration per kernel class (outside the timed region,
-    # the same kernels launched directly instead of from CUDA graphs)
-    # brackets each launch of that class with CUDA events on the library
-    # stream; achieved = algorithmic bytes per launch / mean launch time.
+    roof = roofline(args, wl, opt)
+
+    # ---- central finite differences of the adjoint sensitivities ----
+    fd = None
+    if args.fd_check > 0:
+        fd = fd_check(args, opt, xphys0)
+    del opt
+
+    # ---- CPU legs: the bounded baseline sample, then the accuracy of both
+    # GPU paths against one full (not extrapolated) oracle evaluation ----
+    cpu = acc = None
+    if rank == 0 and ws == 1:
+        if args.cpu_sample:
+            cpu = cpu_baseline(args, wl)
+        if args.oracle_check:
+            acc = oracle_accuracy(args)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded density noise and second load, analytic load pulse)" if args.noise > 0 else
+                "synthetic (uniform density, analytic load pulse)",
+        "config": {"workload": workload_name(args), "mode": "mixed: FP32 flexible-CG recurrence, Kronecker mass preconditioner (multigrid when the stiffness share is large), FP64-accurate residual replacements",
+                   "dofs": 3 * (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1), "elements": opt_nel(wl),
+                   "steps_per_design_iter": args.nsteps, "ncp": args.ncp,
+                   "rtol": args.rtol, "smooth": args.smooth, "nlvls": args.nlvls,
+                   "operator_kernels": "z-marching slabs" if args.tile_form == 1 else "bricks",
+                   "kronecker_passes": "register line segments" if args.kron_form == 1 else "staged lines",
+                   "l2": "state history %.1f GB > 129 MB L2; 256 MB L2 flush between timed iterations"
+                         % (3 * args.nsteps / args.ncp * 3 * (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1)
+                            * 8 / 1e9),
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "objective": fxs[-1] if fxs else None, "seconds": spread(times), "krylov_iters_per_solve": iters_per_solve,
+        "dof_updates_per_s": 2.0 * 3 * (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1) * args.nsteps
+                             * value / ws,
+        "plain_fp64": plain, "accuracy_vs_oracle": acc, "fd_check": fd, "e2e": e2e, "roofline": roof,
+        "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def opt_nel(wl):
+    return wl["nelx"] * wl["nely"] * wl["nelz"]
+
+
+def roofline(args, wl, opt):
+    """One extra design iteration per kernel class (outside the timed region,
+    the same kernels launched directly instead of from CUDA graphs) brackets
+    each launch of that class with CUDA events on the library stream;
+    achieved = algorithmic bytes per launch / mean launch time."""
     import ctypes as C
-    nel = opt.nel
+
+    from topopt_in_petsc_transient_gb300 import TopOpt, design_iteration, _lib
+    L = _lib.load()
+    nel = opt_nel(wl)
     nn = (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1)
     probe = TopOpt(mixed=True, **dict(wl, use_graphs=False)).setup()
     for _ in range(args.warmup):
@@ -301,33 +402,42 @@ def run_gb300(args):
                  "other_kernels": kern[1:],
                  "fp64_apply": {"kernel": "k_tile<double,PolResid>", "ms_per_launch": ms_fp64.value,
                                 "achieved_gbs": (3 * nn * 3 * 8 + 2 * nel * 8 + nn) / (ms_fp64.value * 1e-3) / 1e9}})
+    return roof
 
-    cpu = None
-    if rank == 0 and args.cpu_sample and ws == 1:
-        cpu = cpu_baseline(args, wl)
 
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
-        "data": "synthetic (seedless uniform density 0.12, analytic load pulse)",
-        "config": {"workload": workload_name(args), "mode": "mixed: FP32 flexible-CG recurrence, Kronecker mass preconditioner (multigrid when the stiffness share is large), FP64-accurate residual replacements",
-                   "dofs": 3 * nn, "elements": nel, "steps_per_design_iter": args.nsteps, "ncp": args.ncp,
-                   "rtol": args.rtol, "smooth": args.smooth, "nlvls": args.nlvls,
-                   "operator_kernels": "z-marching slabs" if args.tile_form == 1 else "bricks",
-                   "kronecker_passes": "register line segments" if args.kron_form == 1 else "staged lines",
-                   "l2": "state history %.1f GB > 129 MB L2; 256 MB L2 flush between timed iterations"
-                         % (3 * args.nsteps / args.ncp * 3 * nn * 8 / 1e9),
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "objective": fxs[-1] if fxs else None, "krylov_iters_per_solve": iters_per_solve,
-        "plain_fp64": plain, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-        "gpu_launches": int(launches),
-    }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+def fd_check(args, opt, xphys0):
+    """Central differences (h = args.fd_h) of the objective on args.fd_check
+    seeded elements of the filtered initial design against the adjoint
+    sensitivities of the mixed path, solved to args.fd_rtol; one object,
+    the same checkpointing as the headline."""
+    import numpy as np
+    t0 = time.perf_counter()
+    ph = make_physics(opt, mixed=True, rtol=args.fd_rtol)
+    x = xphys0.clone()
+    fx, df = evaluate(ph, opt, x)
+    dfh = df.cpu().numpy()
+    rng = np.random.default_rng(0x7A11 + 32)
+    els = sorted(int(e) for e in rng.choice(x.numel(), args.fd_check, replace=False))
+    h = args.fd_h
+    fd = []
+    for e in els:
+        x0 = float(x[e])
+        x[e] = x0 + h
+        fp = evaluate(ph, opt, x)[0]
+        x[e] = x0 - h
+        fm = evaluate(ph, opt, x)[0]
+        x[e] = x0
+        fd.append((fp - fm) / (2.0 * h))
+    fd = np.array(fd)
+    ad = dfh[els]
+    dev = np.abs(fd - ad)
+    scale = np.abs(ad).max()
+    del ph
+    return {"elements": len(els), "h": h, "rtol": args.fd_rtol, "seed": "0x7A11+32", "objective": fx,
+            "max_abs_dev_over_max_abs_dfdx": float(dev.max() / scale),
+            "max_rel_dev": float((dev / np.abs(ad)).max()), "median_rel_dev": float(np.median(dev / np.abs(ad))),
+            "dfdx_range_sampled": [float(np.abs(ad).min()), float(scale)], "seconds": time.perf_counter() - t0,
+            "path": "mixed (FP32 sensitivity element math)"}
 
 
 def run_e2e(args, wl, flush_l2):
@@ -336,15 +446,10 @@ def run_e2e(args, wl, flush_l2):
     inputs host->device and results device->host inside the timed region."""
     import numpy as np
 
-    from topopt_in_petsc_transient_gb300 import MMA, Filter, LinearElasticity, TopOpt
+    from topopt_in_petsc_transient_gb300 import MMA, Filter, TopOpt
     o = TopOpt(mixed=True, **wl)
     n = o.nel
-    ph = LinearElasticity(o.nelx, o.nely, o.nelz, nlvls=o.nlvls, ncp=o.ncp, tsc=o.tsc, t1=o.t1, objective=o.objective,
-                          dalpha=o.dalpha, dbeta=o.dbeta, loadsignal=o.loadsignal, mixed=True, rtol=o.rtol,
-                          smooth=o.smooth, cheb_ratio=o.cheb_ratio, use_graphs=o.use_graphs,
-                          coarse_dense_max=o.coarse_dense_max, coarse_smooth=o.coarse_smooth, sens_fp32=o.sens_fp32,
-                          inner_tol=o.inner_tol, inner_maxit=o.inner_maxit, reduction=o.reduction, basis=o.basis,
-                          omega0=o.omega0, load2_node=o.load2_node, load2_phase=o.load2_phase, out_dof=o.out_dof)
+    ph = make_physics(o)
     filt = Filter(o.nelx, o.nely, o.nelz, 2, o.rmin)
     mma = MMA(n, 1)
     mma.SetAsymptotes(0.1, 0.6, 1.05)
@@ -360,7 +465,6 @@ def run_e2e(args, wl, flush_l2):
     hi = np.zeros(n)
     filt.FilterProject(x, xT, xP, False, o.beta, o.eta)
     fscale = None
-    h2d = d2h = 0
     times = []
     nwarm = max(1, args.warmup)  # the first pass also captures the CUDA graphs
     for k in range(nwarm + args.e2e_steps):
@@ -375,7 +479,7 @@ def run_e2e(args, wl, flush_l2):
         filt.GetMND(xP)
         if fscale is None:
             fscale = 1.0 / fx
-        df *= fscale
+        df *= fscale  # VecScale on the host vector (main.cc:121)
         mma.SetOuterMovelimit(o.Xmin, o.Xmax, o.movlim, x, lo, hi)
         mma.Update(x, df, [gx], dg, lo, hi)
         mma.DesignChange(x, xold)
@@ -387,7 +491,8 @@ def run_e2e(args, wl, flush_l2):
     h2d = b * (1 + 0 + 1 + 3 + 1 + 1 + 5 + 2 + 1)
     d2h = b * (0 + 1 + 1 + 2 + 0 + 2 + 1 + 1 + 2)
     return {"value": len(times) / sum(times), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "steps": len(times), "timer": "host wall clock around the synchronous C-ABI calls"}
+            "steps": len(times), "seconds": spread(times),
+            "timer": "host wall clock around the synchronous C-ABI calls"}
 
 
 def load_peaks():
@@ -405,47 +510,124 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s"}
 
 
-def cpu_baseline(args, wl, steps_small=(2, 4)):
-    """The oracle (CPU FP64 restatement of the reference path: assembled
-    27-point block operators, Jacobi-PCG, the reference's dense 24x24 element
-    loops) on the host cores, on a bounded sample of the same workload: the
-    design iteration at horizons of 2 and 4 steps, extrapolated linearly to the
-    full horizon (the per-step cost is the same for every step)."""
+def oracle_le(wl, steps, dt, rtol):
+    """The oracle's LinearElasticity for the workload's physics over `steps`
+    Newmark steps in one block."""
+    from oracle import oracle as O
+    return O.LinearElasticity(wl["nelx"], wl["nely"], wl["nelz"], ncp=1, tsc=steps, t1=dt * steps,
+                              objective=wl["objective"], loadsignal=wl["loadsignal"], dalpha=wl["dalpha"],
+                              dbeta=wl["dbeta"], rtol=rtol, Emin=wl["Ef"] * wl["Emax"], Emax=wl["Emax"],
+                              Rmin=wl["Rf"] * wl["Rmax"], Rmax=wl["Rmax"], load2_node=wl.get("load2_node", -1),
+                              load2_phase=wl.get("load2_phase", 0.0))
+
+
+def oracle_design_x(wl, noise, seed=0x7A11):
+    import numpy as np
+    n = opt_nel(wl)
+    x = np.full(n, wl["V0"])
+    if noise > 0.0:
+        x += np.random.default_rng(seed).uniform(-noise, noise, n)
+    return x
+
+
+def oracle_physics_seconds(wl, steps, dt, rtol, x):
+    le = oracle_le(wl, steps, dt, rtol)
+    t0 = time.perf_counter()
+    rc, fx, df = le.objective_sensitivities(x)
+    return time.perf_counter() - t0, rc, fx, df
+
+
+def oracle_design_seconds(wl, x):
+    """Filter, filter chain rule and MMA of one design iteration in the oracle."""
     import numpy as np
 
     from oracle import oracle as O
-    ncores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
-    t = []
-    for s in steps_small:
-        le = O.LinearElasticity(wl["nelx"], wl["nely"], wl["nelz"], ncp=1, tsc=s, t1=args.dt * s,
-                                objective=wl["objective"], loadsignal=1, dalpha=0.0, dbeta=1e-3, rtol=1e-10,
-                                Emin=1e-9, Emax=1.0, Rmin=1e-3, Rmax=1.0)
-        x = np.full(le.nel, 0.12)
-        t0 = time.perf_counter()
-        le.objective_sensitivities(x)
-        t.append(time.perf_counter() - t0)
-        del le
-    per_step = (t[1] - t[0]) / (steps_small[1] - steps_small[0])
-    fixed = t[0] - steps_small[0] * per_step
-    # filter + gradients + MMA of one design iteration
-    n = wl["nelx"] * wl["nely"] * wl["nelz"]
-    x = np.full(n, 0.12)
+    nx, ny, nz = wl["nelx"], wl["nely"], wl["nelz"]
+    n = nx * ny * nz
     t0 = time.perf_counter()
-    xt, xp = O.filter_project(wl["nelx"], wl["nely"], wl["nelz"], x, wl["rmin"], False, 0.1, 0.15, rtol=1e-8)
-    O.filter_gradients(wl["nelx"], wl["nely"], wl["nelz"], xt, np.ones(n), np.full(n, 1.0 / n), wl["rmin"], False,
-                       0.1, 0.15, rtol=1e-8)
+    xt, xp = O.filter_project(nx, ny, nz, x, wl["rmin"], False, 0.1, 0.15, rtol=1e-8)
+    O.filter_gradients(nx, ny, nz, xt, np.ones(n), np.full(n, 1.0 / n), wl["rmin"], False, 0.1, 0.15, rtol=1e-8)
     mma = O.MMA(n, 1, x)
     lo, hi = O.MMA.SetOuterMovelimit(0.0, 1.0, 0.2, x)
-    mma.Update(x, np.ones(n) * 1e-3, np.array([0.0]), np.full(n, 1.0 / n), lo, hi)
-    t_design = time.perf_counter() - t0
-    t_iter = fixed + args.nsteps * per_step + t_design
+    mma.Update(x.copy(), np.ones(n) * 1e-3, np.array([0.0]), np.full(n, 1.0 / n), lo, hi)
+    return time.perf_counter() - t0
+
+
+def extrapolated_seconds(wl, nsteps, dt, rtol, x, horizons=(2, 4)):
+    """The oracle design evaluation at two short horizons on the full mesh,
+    extrapolated linearly to nsteps (every step costs the same)."""
+    t = [oracle_physics_seconds(wl, s, dt, rtol, x)[0] for s in horizons]
+    per_step = (t[1] - t[0]) / (horizons[1] - horizons[0])
+    fixed = t[0] - horizons[0] * per_step
+    return fixed + nsteps * per_step, sum(t)
+
+
+def cpu_baseline(args, wl, horizons=(2, 4)):
+    """The oracle (CPU FP64 restatement of the reference path: assembled
+    27-point block operators, Jacobi-PCG, the reference's dense 24x24 element
+    loops) on the host cores, on a bounded sample of the same workload: the
+    design evaluation at horizons of 2 and 4 steps on the full mesh,
+    extrapolated linearly to the full horizon, plus filter and MMA at full
+    size.  The extrapolation is checked against one full oracle evaluation
+    in oracle_accuracy."""
+    ncores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
+    x = oracle_design_x(wl, args.noise)
+    t_phys, t_sample = extrapolated_seconds(wl, args.nsteps, args.dt, 1e-10, x, horizons)
+    t_design = oracle_design_seconds(wl, x)
+    t_iter = t_phys + t_design
     return {"value": 1.0 / t_iter, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", ncores)),
             "kind": "port",
-            "sample": "oracle (C, OpenMP) design iteration at horizons %s steps on the full %s mesh, per-step cost "
-                      "extrapolated to %d steps, + filter/MMA at full size (%.1f s total)"
-                      % (list(steps_small), args.mesh, args.nsteps, sum(t) + t_design),
+            "sample": "oracle (C, OpenMP, Jacobi-PCG at rtol 1e-10) design evaluation at horizons %s steps on the "
+                      "full %s mesh, per-step cost extrapolated to %d steps, + filter/MMA at full size (%.1f s total)"
+                      % (list(horizons), args.mesh, args.nsteps, t_sample + t_design),
             "seconds_per_design_iter": t_iter}
+
+
+def oracle_accuracy(args):
+    """Objective and sensitivity error of the mixed and the plain GPU path
+    against the FP64 oracle on one full design evaluation (all steps, not
+    extrapolated) of the accuracy workload (default: the 96x48x48 cantilever,
+    200 steps of dt = 0.005, 5 levels, uniform density 0.12, the same pulse
+    and objective), both GPU paths at the headline rtol, the oracle at
+    args.oracle_rtol.  The same run times the full oracle design iteration
+    and checks the linear extrapolation the CPU baseline uses."""
+    import numpy as np
+    import torch
+
+    from topopt_in_petsc_transient_gb300 import TopOpt
+    ncores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
+    a = argparse.Namespace(**vars(args))
+    a.mesh, a.nsteps, a.dt, a.nlvls, a.ncp = args.oracle_mesh, args.oracle_nsteps, args.oracle_dt, \
+        args.oracle_nlvls, 1
+    a.noise, a.load2 = 0.0, False
+    wl = workload(a)
+    o = TopOpt(**wl)
+    x = oracle_design_x(wl, 0.0)
+    xd = torch.tensor(x, dtype=torch.float64, device="cuda")
+    res = {}
+    for name, mixed in (("mixed", True), ("plain", False)):
+        ph = make_physics(o, mixed=mixed)
+        t0 = time.perf_counter()
+        fx, df = evaluate(ph, o, xd)
+        torch.cuda.synchronize()
+        res[name] = (fx, df.cpu().numpy(), time.perf_counter() - t0)
+        del ph
+    t_full, rc, fx_o, df_o = oracle_physics_seconds(wl, a.nsteps, a.dt, args.oracle_rtol, x)
+    t_ext, _ = extrapolated_seconds(wl, a.nsteps, a.dt, args.oracle_rtol, x)
+    t_design = oracle_design_seconds(wl, x)
+    out = {"workload": workload_name(a), "oracle_rtol": args.oracle_rtol, "gpu_rtol": args.rtol,
+           "oracle_status": rc, "objective_oracle": fx_o,
+           "oracle_seconds_full_design_iteration": t_full + t_design,
+           "oracle_seconds_extrapolated_from_2_and_4_steps": t_ext + t_design,
+           "cores": int(os.environ.get("OMP_NUM_THREADS", ncores))}
+    scale = np.abs(df_o).max()
+    for name, (fx, df, tg) in res.items():
+        out[name] = {"objective": fx, "objective_rel_err_vs_oracle": abs(fx - fx_o) / abs(fx_o),
+                     "dfdx_maxrel_err_vs_oracle": float(np.abs(df - df_o).max() / scale),
+                     "gpu_seconds_first_evaluation": tg}
+    return out
 
 
 def run_reference(args):
@@ -458,19 +640,19 @@ def run_reference(args):
         return
     wl = workload(args)
     for _ in range(args.warmup):
-        cpu_baseline(args, wl, steps_small=(1, 2))
+        cpu_baseline(args, wl, horizons=(1, 2))
     vals = []
     t0 = time.perf_counter()
     last = None
     for _ in range(args.steps):
-        last = cpu_baseline(args, wl, steps_small=(1, 2))
+        last = cpu_baseline(args, wl, horizons=(1, 2))
         vals.append(last["value"])
     wall = time.perf_counter() - t0
     value = statistics.mean(vals)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "impl": "reference",
-            "data": "synthetic (uniform density 0.12, analytic load pulse)",
+            "data": "synthetic (seeded density noise and second load, analytic load pulse)",
             "config": {"workload": workload_name(args), "mode": "CPU FP64 restatement of the reference",
                        "parallelism": "OpenMP host threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["cores"], "kind": "port",
@@ -486,11 +668,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mesh", default="96x48x48")
-    ap.add_argument("--nsteps", type=int, default=200)
-    ap.add_argument("--dt", type=float, default=0.005)
-    ap.add_argument("--ncp", type=int, default=1)
-    ap.add_argument("--nlvls", type=int, default=5)
+    ap.add_argument("--mesh", default="192x96x96")
+    ap.add_argument("--nsteps", type=int, default=400)
+    ap.add_argument("--dt", type=float, default=0.0025)
+    ap.add_argument("--ncp", type=int, default=20)
+    ap.add_argument("--nlvls", type=int, default=6)
     ap.add_argument("--smooth", type=int, default=3)
     ap.add_argument("--cheb-ratio", dest="cheb_ratio", type=float, default=30.0)
     ap.add_argument("--rtol", type=float, default=1e-10)
@@ -501,22 +683,37 @@ def main():
     ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-5)
     ap.add_argument("--inner-maxit", dest="inner_maxit", type=int, default=40)
     ap.add_argument("--objective", type=int, default=3, help="0..6 reference objectives, 7 output-DOF displacement")
-    ap.add_argument("--noise", type=float, default=0.0, help="seeded U(-a, a) noise on the initial design")
-    ap.add_argument("--load2", action="store_true", help="seeded second point load with a seeded phase")
+    ap.add_argument("--noise", type=float, default=0.02, help="seeded U(-a, a) noise on the initial design")
+    ap.add_argument("--no-load2", dest="load2", action="store_false",
+                    help="without the seeded second point load")
     ap.add_argument("--reduction", action="store_true", help="SOMMG reduced-order path")
     ap.add_argument("--basis", type=int, default=8, help="SOMMG basis vectors (with --reduction)")
     ap.add_argument("--omega0", type=float, default=1e-4,
                     help="SOMMG expansion frequency; below the first eigenfrequency for an SPD P0")
     ap.add_argument("--no-graphs", dest="no_graphs", action="store_true",
                     help="launch every kernel directly (profilers see each launch); same kernels")
-    ap.add_argument("--plain-steps", dest="plain_steps", type=int, default=1)
+    ap.add_argument("--plain-steps", dest="plain_steps", type=int, default=None,
+                    help="timed plain FP64 iterations (default: --steps)")
     ap.add_argument("--e2e-steps", dest="e2e_steps", type=int, default=2)
     ap.add_argument("--no-cpu", dest="cpu_sample", action="store_false")
+    ap.add_argument("--no-oracle-check", dest="oracle_check", action="store_false",
+                    help="skip the full oracle evaluation of the accuracy workload")
+    ap.add_argument("--oracle-mesh", dest="oracle_mesh", default="96x48x48")
+    ap.add_argument("--oracle-nsteps", dest="oracle_nsteps", type=int, default=200)
+    ap.add_argument("--oracle-dt", dest="oracle_dt", type=float, default=0.005)
+    ap.add_argument("--oracle-nlvls", dest="oracle_nlvls", type=int, default=5)
+    ap.add_argument("--oracle-rtol", dest="oracle_rtol", type=float, default=1e-12)
+    ap.add_argument("--fd-check", dest="fd_check", type=int, default=32,
+                    help="seeded elements of the central finite-difference check (0: skip)")
+    ap.add_argument("--fd-h", dest="fd_h", type=float, default=1e-4)
+    ap.add_argument("--fd-rtol", dest="fd_rtol", type=float, default=1e-12)
     ap.add_argument("--tile-form", dest="tile_form", type=int, default=0,
                     help="operator kernels: 0 bricks of 7x7x7 output nodes, 1 z-marching slabs")
     ap.add_argument("--kron-form", dest="kron_form", type=int, default=0,
                     help="Kronecker y/z passes: 0 lines staged in shared memory, 1 register line segments")
     args = ap.parse_args()
+    if args.plain_steps is None:
+        args.plain_steps = args.steps
     if args.impl == "reference":
         run_reference(args)
     else:

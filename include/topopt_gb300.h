@@ -120,6 +120,10 @@ typedef struct topo_le_stats {
     double device_bytes;      /* HBM held by the object                 */
     double last_fx;           /* last objective                         */
     long long graph_body_launches; /* kernels run inside device-side Krylov loops */
+    long long mg_solves;      /* solves preconditioned by the multigrid V-cycle */
+    int step_precond;         /* preconditioner of the current design's Newmark
+                                 step solves: 0 multigrid V-cycle, 1 Kronecker
+                                 mass preconditioner, -1 before the first design */
 } topo_le_stats;
 
 /* fills p with the reference defaults for a cantilever of nelx x nely x nelz
@@ -160,6 +164,12 @@ int topo_le_volume_constraint_dev(topo_le *le, double *gx, double *dgdx_dev, con
  * the legacy default stream and returns after gx has been copied to the host. */
 int topo_volume_constraint_noalloc_dev(long long nel, double *gx, double *dgdx_dev, const double *xPhys_dev,
                                        double volfrac);
+
+/* VecScale(dfdx, alpha) of the design loop (main.cc:121, :127: the objective
+ * scaling fscale and the sign flip of -minmax 1) on a device vector of n
+ * values, x <- alpha x; runs on the legacy default stream and returns after
+ * the kernel has finished. */
+int topo_vec_scale_dev(double *x_dev, long long n, double alpha);
 
 /* inspection (tests / output): which = 0 U, 1 DU, 2 DDU of step j of the
  * resident block (j = -1: block start state); copies 3*nn values to host */

@@ -43,6 +43,7 @@ def lib():
         L.oracle_le_get_initial_state.argtypes = [C.c_void_p, dp, dp, dp]
         L.oracle_le_get_last_block.argtypes = [C.c_void_p, C.c_int, dp, dp, dp]
         L.oracle_le_get_adjoint0.argtypes = [C.c_void_p, dp, dp]
+        L.oracle_le_get_restart_state.argtypes = [C.c_void_p, dp, dp, dp]
         L.oracle_le_total_cg_iterations.argtypes = [C.c_void_p]
         L.oracle_le_total_cg_iterations.restype = C.c_long
         L.oracle_le_apply_KM.argtypes = [C.c_void_p, dp, dp, dp]
@@ -186,6 +187,12 @@ class LinearElasticity:
         L1 = np.zeros(self.ndof); DDL0 = np.zeros(self.ndof)
         lib().oracle_le_get_adjoint0(self._h, _p(L1), _p(DDL0))
         return L1, DDL0
+
+    def restart_state(self):
+        """(DDU0, LT, DDL0) of WriteRestartFiles (LinearElasticity.cc:2457-2496)."""
+        out = [np.zeros(self.ndof) for _ in range(3)]
+        lib().oracle_le_get_restart_state(self._h, *[_p(v) for v in out])
+        return tuple(out)
 
     def apply_KM(self, x):
         x = _f64(x)

@@ -201,6 +201,44 @@ static void st_mult(const stencil_t *s, const double *x, double *y) {
             }
 }
 
+/* Two MatMults with matrices of the same pattern in one sweep: kx = K x and
+ * mx = M x, each summed in the order st_mult uses (bitwise the same values). */
+static void st_mult2(const stencil_t *K, const stencil_t *M, const double *x, double *kx, double *mx) {
+    int nx = K->nx, ny = K->ny, nz = K->nz;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                int n = i + nx * (j + ny * k);
+                double ak[3] = {0, 0, 0}, am[3] = {0, 0, 0};
+                for (int dk = -1; dk <= 1; dk++) {
+                    int kk = k + dk;
+                    if (kk < 0 || kk >= nz) continue;
+                    for (int dj = -1; dj <= 1; dj++) {
+                        int jj = j + dj;
+                        if (jj < 0 || jj >= ny) continue;
+                        for (int di = -1; di <= 1; di++) {
+                            int ii = i + di;
+                            if (ii < 0 || ii >= nx) continue;
+                            int m = ii + nx * (jj + ny * kk);
+                            int o = (di + 1) + 3 * (dj + 1) + 9 * (dk + 1);
+                            const double *bk = K->v + ((size_t)n * 27 + o) * 9;
+                            const double *bm = M->v + ((size_t)n * 27 + o) * 9;
+                            for (int c = 0; c < 3; c++)
+                                for (int d = 0; d < 3; d++) {
+                                    ak[c] += bk[c * 3 + d] * x[3 * m + d];
+                                    am[c] += bm[c * 3 + d] * x[3 * m + d];
+                                }
+                        }
+                    }
+                }
+                for (int c = 0; c < 3; c++) {
+                    kx[3 * n + c] = ak[c];
+                    mx[3 * n + c] = am[c];
+                }
+            }
+}
+
 static void st_diag(const stencil_t *s, double *dg) {
     int bs = s->bs;
     for (int n = 0; n < s->nn; n++)
@@ -231,6 +269,7 @@ static int pcg(op_fn op, void *ctx, const double *dinv, int n, const double *b, 
     double bn = sqrt(vdot(n, b, b));
     int it = 0, ok = 1;
     if (bn > 0.0) {
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < n; i++) z[i] = dinv[i] * r[i];
         memcpy(p, z, sizeof(double) * n);
         double rz = vdot(n, r, z);
@@ -273,6 +312,7 @@ struct topo_oracle {
     double *N, *P, *RHS0, *RHS;
     double *kfac, *dkfac, *mfac, *dmfac;
     stencil_t K, M;
+    stencil_t A; /* N Keff N + (I - N), the masked step operator of solve_eff */
     double *dinv_eff, *dinv_m;
     double *U0, *DU0, *DDU0, *U0init, *DU0init;
     double *cp; /* (ncp+1) x {U,DU,DDU}: cp%04d.dat held in memory */
@@ -420,6 +460,7 @@ topo_oracle *oracle_le_create(const topo_oracle_params *p) {
     o->dmfac = vnew(o->nel);
     st_alloc(&o->K, o->nx, o->ny, o->nz, 3);
     st_alloc(&o->M, o->nx, o->ny, o->nz, 3);
+    st_alloc(&o->A, o->nx, o->ny, o->nz, 3);
     o->dinv_eff = vnew(nd);
     o->dinv_m = vnew(nd);
     o->U0 = vnew(nd);
@@ -460,12 +501,14 @@ void oracle_le_destroy(topo_oracle *o) {
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
     st_free(&o->K);
     st_free(&o->M);
+    st_free(&o->A);
     free(o);
 }
 
 /* Load(t): RHS = RHS0 * signal / (ny-1), LinearElasticity.cc:593-615 */
 static void load(topo_oracle *o, double t) {
     double s = oracle_load_signal(o->p.loadsignal, t) / (o->ny - 1);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < o->ndof; i++) o->RHS[i] = o->RHS0[i] * s;
     /* second point load (workload extension, not in the reference) */
     if (o->p.load2_node >= 0 && o->N[3 * o->p.load2_node + 2] != 0.0)
@@ -488,17 +531,58 @@ static void op_masked(void *vctx, const double *x, double *y) {
     topo_oracle *o = c->o;
     int nd = o->ndof;
     double *xm = o->t3, *kx = o->t4;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nd; i++) xm[i] = o->N[i] * x[i];
     if (c->mass_only) {
         st_mult(&o->M, xm, y);
     } else {
         double cK = 1.0 + o->a[2] * o->p.dbeta, cM = o->a[5] + o->a[2] * o->p.dalpha;
-        st_mult(&o->K, xm, kx);
-        st_mult(&o->M, xm, y);
+        st_mult2(&o->K, &o->M, xm, kx, y);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < nd; i++) y[i] = cK * kx[i] + cM * y[i];
     }
     /* dRdS = N A N + (I - N): MatDiagonalScale + MatDiagonalSet, LinearElasticity.cc:1118-1122 */
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nd; i++) y[i] = o->N[i] * y[i] + (1.0 - o->N[i]) * x[i];
+}
+
+/* The same masked step operator N (cK K + cM M) N + (I - N), assembled once
+ * per design into one stencil (MatAXPY + MatDiagonalScale + MatDiagonalSet,
+ * LinearElasticity.cc:1022-1026, :1118-1122): one sweep per Krylov iteration.
+ * The mask entries are exactly 0 or 1, so masking the stored blocks equals
+ * masking the vectors; only the combination cK k + cM m rounds differently
+ * from cK (K x) + cM (M x). */
+static void assemble_masked_eff(topo_oracle *o) {
+    double cK = 1.0 + o->a[2] * o->p.dbeta, cM = o->a[5] + o->a[2] * o->p.dalpha;
+    int nx = o->nx, ny = o->ny, nz = o->nz;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                int n = i + nx * (j + ny * k);
+                for (int oo = 0; oo < 27; oo++) {
+                    int di = oo % 3 - 1, dj = (oo / 3) % 3 - 1, dk = oo / 9 - 1;
+                    int ii = i + di, jj = j + dj, kk = k + dk;
+                    double *ba = o->A.v + ((size_t)n * 27 + oo) * 9;
+                    if (ii < 0 || ii >= nx || jj < 0 || jj >= ny || kk < 0 || kk >= nz) {
+                        memset(ba, 0, 9 * sizeof(double));
+                        continue;
+                    }
+                    int m = ii + nx * (jj + ny * kk);
+                    const double *bk = o->K.v + ((size_t)n * 27 + oo) * 9;
+                    const double *bm = o->M.v + ((size_t)n * 27 + oo) * 9;
+                    for (int c = 0; c < 3; c++)
+                        for (int d = 0; d < 3; d++) {
+                            double v = o->N[3 * n + c] * (cK * bk[3 * c + d] + cM * bm[3 * c + d]) * o->N[3 * m + d];
+                            if (oo == 13 && c == d) v += 1.0 - o->N[3 * n + c];
+                            ba[3 * c + d] = v;
+                        }
+                }
+            }
+}
+static void op_eff(void *vctx, const double *x, double *y) {
+    opctx *c = (opctx *)vctx;
+    st_mult(&c->o->A, x, y);
 }
 
 /* KSPSolve with operator N A N + (I-N), A = -Keff (LinearElasticity.cc:1118-1126):
@@ -506,8 +590,9 @@ static void op_masked(void *vctx, const double *x, double *y) {
 static int solve_eff(topo_oracle *o, const double *R, double *x) {
     opctx c = {o, 0};
     double *rhs = o->t1;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < o->ndof; i++) rhs[i] = (o->N[i] != 0.0) ? -R[i] : R[i];
-    return pcg(op_masked, &c, o->dinv_eff, o->ndof, rhs, x, o->p.rtol, o->p.maxit, &o->cg_iters);
+    return pcg(op_eff, &c, o->dinv_eff, o->ndof, rhs, x, o->p.rtol, o->p.maxit, &o->cg_iters);
 }
 /* KSPSolve with operator N M N + (I-N) (LinearElasticity.cc:1063-1078, :763-776) */
 static int solve_mass(topo_oracle *o, const double *R, double *x) {
@@ -519,9 +604,10 @@ static int solve_mass(topo_oracle *o, const double *R, double *x) {
 static void bmult(topo_oracle *o, double cM, double cK, const double *x, double *y) {
     int nd = o->ndof;
     double *xm = o->t3, *kx = o->t4;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nd; i++) xm[i] = o->N[i] * x[i];
-    st_mult(&o->K, xm, kx);
-    st_mult(&o->M, xm, y);
+    st_mult2(&o->K, &o->M, xm, kx, y);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nd; i++) y[i] = o->N[i] * (cM * y[i] + cK * kx[i]);
 }
 
@@ -541,6 +627,7 @@ int oracle_le_complete_initial_state(topo_oracle *o, const double *xPhys) {
     /* AssembleMassMatrix / AssembleStiffnessMatrix, LinearElasticity.cc:2502-2603 */
     st_assemble(&o->M, o->ME, o->mfac);
     st_assemble(&o->K, o->KE, o->kfac);
+    assemble_masked_eff(o);
     double *dk = o->t1, *dm = o->t2;
     st_diag(&o->K, dk);
     st_diag(&o->M, dm);
@@ -588,8 +675,10 @@ static int solve_state_block(topo_oracle *o, int c) {
         bmult(o, a[5] + a[2] * p->dalpha, a[2] * p->dbeta, UM1, b1);
         bmult(o, a[3] - a[0] * p->dalpha, -a[0] * p->dbeta, DUM1, b2);
         bmult(o, a[4] - a[1] * p->dalpha, -a[1] * p->dbeta, DDUM1, b3);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < nd; i++) rr[i] = o->N[i] * (-(o->RHS[i] + b1[i] + b2[i] + b3[i]));
         rc |= solve_eff(o, rr, Uj);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < nd; i++) {
             double du = Uj[i] - UM1[i];
             DUj[i] = a[0] * DUM1[i] + a[1] * DDUM1[i] + a[2] * du;
@@ -744,6 +833,7 @@ static int solve_lagrangen(topo_oracle *o, int c) {
         double *Lj = o->L + (size_t)j * nd, *DLj = o->DL + (size_t)j * nd, *DDLj = o->DDL + (size_t)j * nd;
         gradient_objective_loop(o, o->U + (size_t)j * nd, o->DU + (size_t)j * nd, o->DDU + (size_t)j * nd);
         if (t == o->Ts - 1) {
+#pragma omp parallel for schedule(static)
             for (int i = 0; i < nd; i++) {
                 DLj[i] = -o->HDDU[i];
                 DDLj[i] = -o->HDDDU[i];
@@ -755,6 +845,7 @@ static int solve_lagrangen(topo_oracle *o, int c) {
             bmult(o, a[5] + a[2] * p->dalpha, a[2] * p->dbeta, o->Lp1, b1);
             bmult(o, a[3] - a[0] * p->dalpha, -a[0] * p->dbeta, o->Lp1, b2);
             bmult(o, a[4] - a[1] * p->dalpha, -a[1] * p->dbeta, o->Lp1, b3);
+#pragma omp parallel for schedule(static)
             for (int i = 0; i < nd; i++) {
                 DLj[i] = -(o->HDDU[i] + b2[i] - a[0] * o->DLp1[i] + a[3] * o->DDLp1[i]);
                 DDLj[i] = -(o->HDDDU[i] + b3[i] + a[4] * o->DDLp1[i]);
@@ -929,6 +1020,14 @@ void oracle_le_get_last_block(const topo_oracle *o, int j, double *U, double *DU
 }
 void oracle_le_get_adjoint0(const topo_oracle *o, double *L1, double *DDL0) {
     memcpy(L1, o->Lp1, sizeof(double) * o->ndof);
+    memcpy(DDL0, o->DDL0, sizeof(double) * o->ndof);
+}
+/* the three vectors of WriteRestartFiles (LinearElasticity.cc:2457-2496):
+ * the initial acceleration (checkpoint 0), the terminal adjoint of the last
+ * reverse sweep and the adjoint acceleration at t = 0 */
+void oracle_le_get_restart_state(const topo_oracle *o, double *DDU0, double *LT, double *DDL0) {
+    memcpy(DDU0, o->cp + 2 * (size_t)o->ndof, sizeof(double) * o->ndof);
+    memcpy(LT, o->LT, sizeof(double) * o->ndof);
     memcpy(DDL0, o->DDL0, sizeof(double) * o->ndof);
 }
 long oracle_le_total_cg_iterations(const topo_oracle *o) { return o->cg_iters; }

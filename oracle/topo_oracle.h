@@ -69,6 +69,7 @@ void oracle_le_get_newmark(const topo_oracle *o, double *a6, double *dt);
 void oracle_le_get_initial_state(const topo_oracle *o, double *U0, double *DU0, double *DDU0);
 void oracle_le_get_last_block(const topo_oracle *o, int j, double *U, double *DU, double *DDU);
 void oracle_le_get_adjoint0(const topo_oracle *o, double *L1, double *DDL0);
+void oracle_le_get_restart_state(const topo_oracle *o, double *DDU0, double *LT, double *DDL0);
 long oracle_le_total_cg_iterations(const topo_oracle *o);
 /* SOMMG reduced-order path (SOMMG.cc:40-265 and the reduction branches of
  * LinearElasticity.cc): basis of k vectors at expansion frequency omega0,

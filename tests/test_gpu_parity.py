@@ -122,13 +122,20 @@ def test_states_and_checkpointing(gpu, ncp, tsc, graphs):
 def test_mixed_default_fp32_sensitivities(gpu, nlvls, coarse_smooth):
     # the mixed-path default: FP32 element math in the sensitivity kernel
     # (state combinations formed in FP64); stated tolerance 1e-6 on the
-    # objective and 1e-5 of max|dfdx| on the sensitivities
+    # objective and 1e-5 of max|dfdx| on the sensitivities.  The multigrid
+    # preconditioner is forced (mass_precond 0: this mass-dominated operator
+    # would otherwise take the Kronecker one) at full depth (adaptive_kappa 0)
+    # with an iterative coarsest level, so the FP32 V-cycle of nlvls levels
+    # and its coarse Chebyshev solve of degree coarse_smooth run
     n = (16, 8, 8)
     kw = dict(ncp=2, tsc=6, t1=0.06, objective=3, loadsignal=1, dalpha=0.0, dbeta=1e-3)
     rng = np.random.default_rng(21)
     x = 0.12 + 0.02 * (2 * rng.random(np.prod(n)) - 1)
-    le = _le(n, nlvls=nlvls, coarse_smooth=coarse_smooth, mixed=True, rtol=1e-10, **kw)
+    le = _le(n, nlvls=nlvls, coarse_smooth=coarse_smooth, mixed=True, rtol=1e-10, mass_precond=0,
+             coarse_dense_max=0, adaptive_kappa=0.0, **kw)
     fx, df = _run_gpu(le, x)
+    st = le.stats()
+    assert st["step_precond"] == 0 and st["mg_solves"] == st["solves"]
     ref = O.LinearElasticity(*n, **kw)
     rc, fx_r, df_r = ref.objective_sensitivities(x)
     assert abs(fx - fx_r) <= 1e-6 * abs(fx_r)

@@ -48,7 +48,8 @@ class LEParams(C.Structure):
 
 class LEStats(C.Structure):
     _fields_ = [("cg_iterations", C.c_longlong), ("solves", C.c_longlong), ("device_bytes", C.c_double),
-                ("last_fx", C.c_double), ("graph_body_launches", C.c_longlong)]
+                ("last_fx", C.c_double), ("graph_body_launches", C.c_longlong), ("mg_solves", C.c_longlong),
+                ("step_precond", C.c_int)]
 
 
 EXPORTS = [
@@ -58,7 +59,7 @@ EXPORTS = [
     "topo_le_compute_objective_sensitivities", "topo_le_compute_objective_sensitivities_dev",
     "topo_le_volume_constraint", "topo_le_volume_constraint_dev",
     "topo_le_get_state", "topo_le_get_checkpoint", "topo_le_set_initial_displacement", "topo_le_get_restart_state", "topo_le_apply_km", "topo_le_get_stats", "topo_le_time_apply",
-    "topo_le_kernel_timing", "topo_volume_constraint_noalloc_dev", "topo_le_reduced_system",
+    "topo_le_kernel_timing", "topo_volume_constraint_noalloc_dev", "topo_le_reduced_system", "topo_vec_scale_dev",
     "topo_box_element_matrices",
     "topo_pdefilt_create", "topo_pdefilt_destroy", "topo_pdefilt_filter_project", "topo_pdefilt_filter_project_dev",
     "topo_filter_project", "topo_filter_project_dev", "topo_filter_gradients", "topo_filter_gradients_dev",
@@ -112,6 +113,7 @@ def load(path=None):
         "topo_le_kernel_timing": (ip, [vp, ip, ip, dp, C.POINTER(C.c_longlong)]),
         "topo_le_reduced_system": (ip, [vp, vp, vp, vp, vp]),
         "topo_volume_constraint_noalloc_dev": (ip, [C.c_longlong, dp, vp, vp, d]),
+        "topo_vec_scale_dev": (ip, [vp, C.c_longlong, d]),
         "topo_box_element_matrices": (None, [d, d, d, d, vp, vp]),
         "topo_pdefilt_create": (ip, [pp, ip, ip, ip, d, d, d, d, d, ip]),
         "topo_pdefilt_destroy": (None, [vp]),

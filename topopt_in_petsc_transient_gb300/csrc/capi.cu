@@ -64,6 +64,11 @@ __global__ void k_volume(long long n, const double *__restrict__ x, double volfr
     if (grid_reduce<EW, 1>(v, part, tot)) *gx = tot[0] / (double)n - volfrac;
 }
 
+__global__ void k_scale(long long n, double *__restrict__ x, double alpha) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] *= alpha;
+}
+
 }  // namespace
 
 extern "C" {
@@ -199,6 +204,18 @@ int topo_le_volume_constraint(topo_le *le, double *gx, double *dgdx, const doubl
     int rc = topo_le_volume_constraint_dev(le, gx, le->d_df, le->d_x, volfrac);
     if (rc) return rc;
     ACK(cudaMemcpy(dgdx, le->d_df, sizeof(double) * le->nel, cudaMemcpyDeviceToHost));
+    return TOPO_OK;
+}
+
+int topo_vec_scale_dev(double *x_dev, long long n, double alpha) {
+    if (n < 0 || (n > 0 && !x_dev)) return TOPO_ERR_ARG;
+    if (n == 0) return TOPO_OK;
+    int rc = device_ok();
+    if (rc) return rc;
+    count_launch();
+    k_scale<<<ew_blocks(n), EW>>>(n, x_dev, alpha);
+    ACK(cudaGetLastError());
+    ACK(cudaStreamSynchronize(0));
     return TOPO_OK;
 }
 

@@ -420,6 +420,7 @@ struct TopoLE {
     double mu_KM = 0.0;  // largest generalized eigenvalue of (KE, ME), fine box
     int *err = nullptr;
     long long nsolves = 0;
+    long long mg_solves = 0;  // solves whose preconditioner is the V-cycle
     long long step_kernels[2] = {0, 0}, body_kernels = 0, direct_iters = 0;
     // graphs
     cudaGraphExec_t gx_fwd = nullptr, gx_adj = nullptr;
@@ -1286,6 +1287,7 @@ static int solve_direct(TopoLE *le, int o, const double *b) {
     count_launch();
     k_solve_check<<<1, 1, 0, le->stream>>>(le->S, le->err);
     le->nsolves++;
+    if (!le->ops[o].kron) le->mg_solves++;
     CK(cudaGetLastError());
     return TOPO_OK;
 }
@@ -1806,6 +1808,7 @@ static int run_block(TopoLE *le, int c, int adjoint) {
         if (gx) {
             CK(cudaGraphLaunch(gx, le->stream));
             le->nsolves++;
+            if (!le->ops[0].kron) le->mg_solves++;
             count_launch(le->step_kernels[adjoint]);
         } else {
             int rc = adjoint ? adj_step(le, false) : fwd_step(le, false);
@@ -2363,6 +2366,8 @@ int le_stats(TopoLE *le, LEStats *out) {
     CK(cudaStreamSynchronize(le->stream));
     le->stats.cg_iterations = h.total_it;
     le->stats.solves = le->nsolves;
+    le->stats.mg_solves = le->mg_solves;
+    le->stats.step_precond = le->design_ready ? (le->ops[0].kron ? 1 : 0) : -1;
     le->stats.graph_body_launches = (h.total_it - le->direct_iters) * le->body_kernels;
     *out = le->stats;
     return TOPO_OK;

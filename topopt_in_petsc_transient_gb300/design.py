@@ -157,6 +157,7 @@ class TopOpt:
 def design_iteration(opt: TopOpt):
     """One iteration of the main.cc optimisation loop (main.cc:76-160);
     returns (fx_true, fx_scaled, gx0, ch, mnd)."""
+    from .topopt import VecScale
     opt.itr += 1
     ph = opt.physics
     w, out2 = getattr(opt, "firstIterWrite", False), getattr(opt, "output2", None)
@@ -174,10 +175,10 @@ def design_iteration(opt: TopOpt):
     if opt.itr == 1:
         opt.fscale = 1.0 / fx
     fxs = fx * opt.fscale
-    opt.dfdx.mul_(opt.fscale)
+    VecScale(opt.dfdx, opt.fscale)
     opt.mma.SetOuterMovelimit(opt.Xmin, opt.Xmax, opt.movlim, opt.x, opt.xmin, opt.xmax)
     if opt.minmax == 1:
-        opt.dfdx.mul_(-1.0)
+        VecScale(opt.dfdx, -1.0)
     opt.mma.Update(opt.x, opt.dfdx, [gx0], opt.dgdx, opt.xmin, opt.xmax)
     ch = opt.mma.DesignChange(opt.x, opt.xold)
     if opt.projectionFilter and (opt.itr >= 200 or ch < 0.01):

@@ -58,6 +58,18 @@ def read_petsc_vecs(path, outs, first=0):
         check(lib.topo_petsc_vec_read(os.fsencode(path), first + k, a, n, int(dev)), "PETSc vector read")
 
 
+def VecScale(v, alpha):
+    """PETSc's VecScale as main.cc uses it on dfdx (main.cc:121, :127):
+    v <- alpha v in place, for a CUDA float64 tensor (one library kernel) or a
+    host float64 array."""
+    if _is_dev(v):
+        _, a = _addr(v, None, "vector")
+        check(_lib.load().topo_vec_scale_dev(a, v.numel(), float(alpha)), "VecScale")
+    else:
+        np.multiply(v, alpha, out=v)
+    return 0
+
+
 class LinearElasticity:
     """LinearElasticity (LinearElasticity.h:23-240) on the GPU.
 
@@ -288,7 +300,8 @@ class LinearElasticity:
         s = LEStats()
         check(_lib.load().topo_le_get_stats(self._h, C.byref(s)), "get_stats")
         return {"cg_iterations": s.cg_iterations, "solves": s.solves, "device_bytes": s.device_bytes,
-                "last_fx": s.last_fx, "graph_body_launches": s.graph_body_launches}
+                "last_fx": s.last_fx, "graph_body_launches": s.graph_body_launches, "mg_solves": s.mg_solves,
+                "step_precond": s.step_precond}
 
 
 class MPIIO:
