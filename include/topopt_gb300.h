@@ -215,6 +215,25 @@ int topo_le_kernel_timing(topo_le *le, int kclass, int enable, double *ms_total,
  * Kr, Mr (basis x basis, row-major), Pr (basis); any pointer may be NULL.
  * Requires reduction = 1 and CompleteInitialState. */
 int topo_le_reduced_system(topo_le *le, double *Q, double *Kr, double *Mr, double *Pr);
+/* SOMMG (SOMMG.h:14-34): the second-order moment-matching reduction model a
+ * LinearElasticity object built with reduction = 1 owns (the reference's
+ * private member reductionmodel).  topo_sommg_create replaces
+ * SOMMG(Vec x, PetscInt order) (SOMMG.cc:11-24): the handle refers to `le`,
+ * whose basis must equal order; it does not own `le`. */
+typedef struct topo_sommg topo_sommg;
+int topo_sommg_create(topo_sommg **out, topo_le *le, int order);
+void topo_sommg_destroy(topo_sommg *s);
+/* SOMMG::ConstructBasis(K, M, C, P, N, om, ksp) (SOMMG.h:25, SOMMG.cc:40-265):
+ * K, M, C, the load P and the Dirichlet mask N are those of le's current
+ * design (after CompleteInitialState), the solves use le's solver.  The
+ * reduced forward sweep follows, so a later ComputeObjectiveSensitivities
+ * integrates in the new basis. */
+int topo_sommg_construct_basis(topo_sommg *s, double om);
+/* the public members QQ (order x 3*nn, row b = basis vector b), Kr, Mr, Cr
+ * (order x order, row-major) and Pr (order) (SOMMG.h:21-22) into host
+ * arrays; any pointer may be NULL */
+int topo_sommg_get(topo_sommg *s, double *QQ, double *Kr, double *Mr, double *Cr, double *Pr);
+
 /* 24x24 box element matrices (E = 1, unit density) as applied by the
  * matrix-free kernels, in the local node order of DMDAGetElements_3D
  * (LinearElasticity.cc:3067-3074), row-major: the Hex8IsoparametricKE/ME

@@ -4,6 +4,7 @@
 // device pointers directly.
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "filter.h"
 #include "kernels.cuh"
@@ -24,6 +25,10 @@ struct topo_pdefilt {
     double *d_a, *d_b, *d_c, *d_g;
     long long nel;
     int gcap;  // constraint columns held by d_g
+};
+struct topo_sommg {
+    topo_le *le;  // the LinearElasticity object whose reduction model this is
+    int order;
 };
 struct topo_mma {
     TopoMMA *impl;
@@ -278,6 +283,43 @@ int topo_le_reduced_system(topo_le *le, double *Q, double *Kr, double *Mr, doubl
 int topo_le_kernel_timing(topo_le *le, int kclass, int enable, double *ms_total, long long *launches) {
     if (!le) return TOPO_ERR_ARG;
     return le_kernel_timing(le->impl, kclass, enable, ms_total, launches);
+}
+
+int topo_sommg_create(topo_sommg **out, topo_le *le, int order) {
+    if (!out || !le) return TOPO_ERR_ARG;
+    *out = nullptr;
+    const int kb = le_basis(le->impl);
+    if (kb == 0 || order != kb) {
+        set_error("SOMMG(x, order): the LinearElasticity object must be created with reduction = 1 and basis = order");
+        return TOPO_ERR_ARG;
+    }
+    *out = new topo_sommg{le, order};
+    return TOPO_OK;
+}
+
+void topo_sommg_destroy(topo_sommg *s) { delete s; }
+
+int topo_sommg_construct_basis(topo_sommg *s, double om) {
+    if (!s) return TOPO_ERR_ARG;
+    return le_sommg_construct_basis(s->le->impl, om);
+}
+
+int topo_sommg_get(topo_sommg *s, double *QQ, double *Kr, double *Mr, double *Cr, double *Pr) {
+    if (!s) return TOPO_ERR_ARG;
+    const int kb = s->order;
+    std::vector<double> k, m;
+    if (Cr) {
+        k.resize((size_t)kb * kb);
+        m.resize((size_t)kb * kb);
+    }
+    int rc = le_reduced_system(s->le->impl, QQ, Cr ? k.data() : Kr, Cr ? m.data() : Mr, Pr);
+    if (rc || !Cr) return rc;
+    double alpha, beta;
+    le_damping(s->le->impl, &alpha, &beta);
+    for (size_t i = 0; i < k.size(); i++) Cr[i] = alpha * m[i] + beta * k[i];  // Q'(alpha M + beta K)Q, SOMMG.cc:246-249
+    if (Kr) memcpy(Kr, k.data(), sizeof(double) * k.size());
+    if (Mr) memcpy(Mr, m.data(), sizeof(double) * m.size());
+    return TOPO_OK;
 }
 
 void topo_box_element_matrices(double hx, double hy, double hz, double nu, double *KE, double *ME) {

@@ -2057,6 +2057,23 @@ static int sommg_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_de
     return TOPO_OK;
 }
 
+// SOMMG::ConstructBasis (SOMMG.cc:40-265) with expansion frequency om on the
+// operators of the current design, then the reduced forward sweep, so that a
+// following ComputeObjectiveSensitivities integrates in the new basis
+int le_sommg_construct_basis(TopoLE *le, double om) {
+    if (!le->kb || !le->design_ready) {
+        set_error("ConstructBasis needs reduction = 1 and CompleteInitialState");
+        return TOPO_ERR_STATE;
+    }
+    if (!(om > 0.0)) {
+        set_error("ConstructBasis: om must be > 0 (the basis recursion scales by om)");
+        return TOPO_ERR_ARG;
+    }
+    le->p.omega0 = om;
+    le->ops[2].sM = -om * om;
+    return sommg_initial_state(le);
+}
+
 int le_reduced_system(TopoLE *le, double *Q, double *Kr, double *Mr, double *Pr) {
     if (!le->kb || !le->design_ready) {
         set_error("reduced_system needs reduction = 1 and CompleteInitialState");
@@ -2374,6 +2391,11 @@ int le_stats(TopoLE *le, LEStats *out) {
 }
 
 long long le_nel(const TopoLE *le) { return le->nel; }
+int le_basis(const TopoLE *le) { return le->kb; }
+void le_damping(const TopoLE *le, double *alpha, double *beta) {
+    *alpha = le->p.dalpha;
+    *beta = le->p.dbeta;
+}
 long long le_ndof(const TopoLE *le) { return le->ndof; }
 void *le_stream(TopoLE *le) { return (void *)le->stream; }
 

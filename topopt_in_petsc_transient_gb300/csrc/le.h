@@ -34,6 +34,9 @@ void *le_stream(TopoLE *le);
 int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms);
 int le_kernel_timing(TopoLE *le, int kclass, int enable, double *ms_total, long long *launches);
 int le_reduced_system(TopoLE *le, double *Q, double *Kr, double *Mr, double *Pr);
+int le_sommg_construct_basis(TopoLE *le, double om);
+int le_basis(const TopoLE *le);
+void le_damping(const TopoLE *le, double *alpha, double *beta);
 void box_element_matrices(double hx, double hy, double hz, double nu, double *KE, double *ME);
 
 }  // namespace topo

@@ -304,6 +304,61 @@ class LinearElasticity:
                 "step_precond": s.step_precond}
 
 
+class SOMMG:
+    """SOMMG (SOMMG.h:14-34): the second-order moment-matching reduction of a
+    LinearElasticity object created with reduction=True.  SOMMG(physics,
+    order) stands for SOMMG(Vec x, order) (SOMMG.cc:11-24); order must equal
+    the object's basis.  ConstructBasis(om) is SOMMG::ConstructBasis on the
+    object's operators of its current design (SOMMG.cc:40-265); QQ (order x
+    3 nn), Kr, Mr, Cr (order x order) and Pr (order) are its public members
+    (SOMMG.h:21-22), read back as numpy arrays."""
+
+    def __init__(self, physics, order):
+        h_ = C.c_void_p()
+        check(_lib.load().topo_sommg_create(C.byref(h_), physics._h, int(order)), "SOMMG")
+        self._h = h_
+        self.physics = physics
+        self.order = int(order)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.load().topo_sommg_destroy(h)
+            self._h = None
+
+    def ConstructBasis(self, om):
+        check(_lib.load().topo_sommg_construct_basis(self._h, float(om)), "ConstructBasis")
+        return 0
+
+    def _members(self):
+        k = self.order
+        Q = np.zeros((k, self.physics.ndof))
+        Kr, Mr, Cr, Pr = np.zeros((k, k)), np.zeros((k, k)), np.zeros((k, k)), np.zeros(k)
+        check(_lib.load().topo_sommg_get(self._h, Q.ctypes.data, Kr.ctypes.data, Mr.ctypes.data, Cr.ctypes.data,
+                                         Pr.ctypes.data), "SOMMG members")
+        return Q, Kr, Mr, Cr, Pr
+
+    @property
+    def QQ(self):
+        return self._members()[0]
+
+    @property
+    def Kr(self):
+        return self._members()[1]
+
+    @property
+    def Mr(self):
+        return self._members()[2]
+
+    @property
+    def Cr(self):
+        return self._members()[3]
+
+    @property
+    def Pr(self):
+        return self._members()[4]
+
+
 class MPIIO:
     """MPIIO (MPIIO.h:27-100): result files for bin2vtu.py.
 
