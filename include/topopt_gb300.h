@@ -234,6 +234,16 @@ int topo_sommg_construct_basis(topo_sommg *s, double om);
  * arrays; any pointer may be NULL */
 int topo_sommg_get(topo_sommg *s, double *QQ, double *Kr, double *Mr, double *Cr, double *Pr);
 
+/* The Gram product of the reduced matrices (the VecDot(MatMult(A, QQ[j]),
+ * QQ[i]) loops of SOMMG.cc:234-251) on the tensor cores, as the reduction of
+ * the mixed path computes it: out[a * kb + b] = sum_i Q[a][i] W[b][i] (host
+ * array, row-major) for kb <= 32 device rows Q (FP32, row stride ldq) and W
+ * (FP64, row stride ldw) of n values.  Operands are split into TF32 pieces
+ * that multiply exactly; sums run in FP32 over 64 values in tensor memory,
+ * then in double-float and FP64.  Allocates its padded operands. */
+int topo_sommg_gram_dev(const float *Q_dev, long long ldq, const double *W_dev, long long ldw, long long n, int kb,
+                        double *out);
+
 /* 24x24 box element matrices (E = 1, unit density) as applied by the
  * matrix-free kernels, in the local node order of DMDAGetElements_3D
  * (LinearElasticity.cc:3067-3074), row-major: the Hex8IsoparametricKE/ME

@@ -102,7 +102,11 @@ def test_mixed_multigrid_in_the_reference_regime(gpu):
     # the reference's default material (Emax 1e3, Rmax 4.1667e-4) and pulse
     # with dt = 0.4: the Newmark operator is stiffness-dominated, the solver
     # picks the multigrid V-cycle, and the mixed path runs its FP32 V-cycle
-    # (Chebyshev-Jacobi smoothing, dense coarsest inverse) inside FCG
+    # (Chebyshev-Jacobi smoothing, dense coarsest inverse) inside FCG.  Its
+    # FP64-accurate residuals are double-float products, good to about 2^-48
+    # of the summed element terms; with this operator's cancellation that
+    # floors the reachable tolerance between 1e-11 and 1e-12 (the plain path
+    # reaches 1e-12), so the tight case runs at rtol 1e-11
     from topopt_in_petsc_transient_gb300 import LinearElasticity
     n = (16, 8, 8)
     kw = dict(ncp=4, tsc=10, t1=16.0, objective=3, loadsignal=0, dalpha=1e-4, dbeta=1e-4)
@@ -112,7 +116,7 @@ def test_mixed_multigrid_in_the_reference_regime(gpu):
     ref = O.LinearElasticity(*n, Emin=mat[0], Emax=mat[1], Rmin=mat[2], Rmax=mat[3], **kw)
     rc, fx_r, df_r = ref.objective_sensitivities(x)
     assert rc == 0
-    for rtol, sens32, tf, td in ((1e-12, False, 1e-10, 1e-9), (1e-10, True, 1e-6, 1e-5)):
+    for rtol, sens32, tf, td in ((1e-11, False, 1e-10, 1e-9), (1e-10, True, 1e-6, 1e-5)):
         le = LinearElasticity(*n, nlvls=3, mixed=True, rtol=rtol, sens_fp32=sens32, **kw)
         xd = torch.tensor(x, dtype=torch.float64, device="cuda")
         df = torch.zeros_like(xd)

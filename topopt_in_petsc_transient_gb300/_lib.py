@@ -61,7 +61,7 @@ EXPORTS = [
     "topo_le_get_state", "topo_le_get_checkpoint", "topo_le_set_initial_displacement", "topo_le_get_restart_state", "topo_le_apply_km", "topo_le_get_stats", "topo_le_time_apply",
     "topo_le_kernel_timing", "topo_volume_constraint_noalloc_dev", "topo_le_reduced_system", "topo_vec_scale_dev",
     "topo_box_element_matrices", "topo_sommg_create", "topo_sommg_destroy", "topo_sommg_construct_basis",
-    "topo_sommg_get",
+    "topo_sommg_get", "topo_sommg_gram_dev",
     "topo_pdefilt_create", "topo_pdefilt_destroy", "topo_pdefilt_filter_project", "topo_pdefilt_filter_project_dev",
     "topo_filter_project", "topo_filter_project_dev", "topo_filter_gradients", "topo_filter_gradients_dev",
     "topo_filter_mnd", "topo_filter_mnd_dev",
@@ -120,6 +120,7 @@ def load(path=None):
         "topo_sommg_destroy": (None, [vp]),
         "topo_sommg_construct_basis": (ip, [vp, d]),
         "topo_sommg_get": (ip, [vp, vp, vp, vp, vp, vp]),
+        "topo_sommg_gram_dev": (ip, [vp, C.c_longlong, vp, C.c_longlong, C.c_longlong, ip, vp]),
         "topo_pdefilt_create": (ip, [pp, ip, ip, ip, d, d, d, d, d, ip]),
         "topo_pdefilt_destroy": (None, [vp]),
         "topo_pdefilt_filter_project": (ip, [vp, vp, vp]),

@@ -299,6 +299,13 @@ int topo_sommg_create(topo_sommg **out, topo_le *le, int order) {
 
 void topo_sommg_destroy(topo_sommg *s) { delete s; }
 
+int topo_sommg_gram_dev(const float *Q_dev, long long ldq, const double *W_dev, long long ldw, long long n, int kb,
+                        double *out) {
+    int rc = device_ok();
+    if (rc) return rc;
+    return le_gram_tc_dev(Q_dev, ldq, W_dev, ldw, n, kb, out);
+}
+
 int topo_sommg_construct_basis(topo_sommg *s, double om) {
     if (!s) return TOPO_ERR_ARG;
     return le_sommg_construct_basis(s->le->impl, om);

@@ -26,6 +26,7 @@
 #include "mpiio.h"
 #include "slab.cuh"
 #include "sommg.cuh"
+#include "gram.cuh"
 
 namespace topo {
 
@@ -43,6 +44,16 @@ static thread_local std::string g_last_error;
 // 0 bricks (tile.cuh), 1 z-marching slabs (slab.cuh); set by le_create,
 // applies process-wide
 static int g_tile_form = 0;
+
+// Function attributes, occupancy and SM counts are properties of a device:
+// the one-time caches of the launch helpers are indexed by the ordinal of the
+// current device (a second device gets its own attribute calls and grid sizes)
+constexpr int MAX_DEVICES = 64;
+static int device_slot() {
+    int d = 0;
+    cudaGetDevice(&d);
+    return (d >= 0 && d < MAX_DEVICES) ? d : 0;
+}
 void set_error(const std::string &s) { g_last_error = s; }
 const char *last_error() { return g_last_error.c_str(); }
 
@@ -264,7 +275,8 @@ static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol
     // so does a grid whose slabs would fill less than half the resident slots
     // (small meshes, coarse multigrid levels)
     if constexpr (!std::is_same<T, double>::value) if (g_tile_form == 1) {
-        static long long slots = 0;
+        static long long slots_dev[MAX_DEVICES] = {};
+        long long &slots = slots_dev[device_slot()];
         const size_t sm = slab_smem_bytes<T, Pol>();
         if (!slots) {
             cudaFuncSetAttribute(k_slab<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -283,7 +295,8 @@ static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol
             return;
         }
     }
-    static int resident = 0;
+    static int resident_dev[MAX_DEVICES] = {};
+    int &resident = resident_dev[device_slot()];
     const size_t sm = tile_smem_bytes<T, Pol>();
     if (!resident) {
         cudaFuncSetAttribute(k_tile<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -373,9 +386,18 @@ struct TopoLE {
     double *AUt = nullptr, *AVt = nullptr, *AAt = nullptr, *AApt = nullptr, *KSt = nullptr;
     bool fwd_init_pending = false;
     int kb = 0;
-    bool fp64_solves = false;  // the SOMMG basis solves run the FP64 FCG in either mode
+    bool fp64_solves = false;  // the SOMMG basis solves of the plain path run the FP64 FCG
     double *Q = nullptr, *red = nullptr, *rhist = nullptr, *Sacc = nullptr, *Phi = nullptr, *mdpart = nullptr;
     int *rstatus = nullptr;
+    // mixed path: the basis in FP32 (rows of qld >= ndof values, a multiple of
+    // GR_KC, zero padded), Phi in FP32, the products W = A Q_j as FP32 pairs
+    // (Wh, Wl) for the tensor-core Gram (gram.cuh), its per-CTA partials and
+    // an FP64 scratch row qd
+    bool basis32 = false;
+    long long qld = 0;
+    float *Q32 = nullptr, *Phi32 = nullptr, *Wh = nullptr, *Wl = nullptr;
+    double *gpart = nullptr, *qd = nullptr;
+    int gram_blocks = 0;
     Arena arena;
     cudaStream_t stream = nullptr;
     topo_mpiio *out = nullptr;  // attached physics output (topo_le_set_output), not owned
@@ -759,11 +781,26 @@ int le_alloc(TopoLE *le) {
     if (p.reduction) {
         le->kb = p.basis;
         const int kb = le->kb;
-        AG(le->Q, (size_t)kb * nd);
+        le->basis32 = p.mixed != 0;
+        if (le->basis32) {
+            le->qld = (nd + GR_KC - 1) / GR_KC * GR_KC;
+            AG(le->Q32, (size_t)kb * le->qld);
+            AG(le->Wh, (size_t)kb * le->qld);
+            AG(le->Wl, (size_t)kb * le->qld);
+            AG(le->Phi32, (size_t)4 * kb * nd);
+            AG(le->qd, nd);
+            int dev = 0, nsm = 0;
+            CK(cudaGetDevice(&dev));
+            CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            le->gram_blocks = 2 * std::max(1, nsm);
+            AG(le->gpart, (size_t)le->gram_blocks * 1024);
+        } else {
+            AG(le->Q, (size_t)kb * nd);
+            AG(le->Phi, (size_t)4 * kb * nd);
+        }
         AG(le->red, (size_t)6 * kb * kb + kb + 1);
         AG(le->rhist, (size_t)le->Ts * 3 * kb);
         AG(le->Sacc, (size_t)4 * kb * kb);
-        AG(le->Phi, (size_t)4 * kb * nd);
         AG(le->mdpart, (size_t)kb * MD_CHUNKS);
         AG(le->rstatus, 1);
     }
@@ -1040,7 +1077,8 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     const T *sc = kron_scale<T>(le->ops[o]);
     const bool mixed = fz && std::is_same<T, float>::value;
     const long long nlines = (long long)g.ny * g.nz;
-    static int nsm = 0;
+    static int nsm_dev[MAX_DEVICES] = {};
+    int &nsm = nsm_dev[device_slot()];
     if (!nsm) {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -1049,7 +1087,8 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     }
     const int kx = kx_lines_launch(g, sizeof(T), 4LL * nsm);  // 4 resident CTAs of the x pass per SM
     const size_t smx = kron_x_smem(g, sizeof(T), kx), smy = kron_yz_smem(g, 1, sizeof(T));
-    static bool attr = false;
+    static bool attr_dev[MAX_DEVICES] = {};
+    bool &attr = attr_dev[device_slot()];
     if (!attr) {  // staged lines: the selection keeps every pass within KRON_SMEM_MAX
         cudaFuncSetAttribute(k_kron_x<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
         if constexpr (std::is_same<T, float>::value)
@@ -1854,11 +1893,12 @@ __global__ void k_init_accel_rhs(long long nn, const uint8_t *fixed, const doubl
 // SOMMG reduced path (SOMMG.cc:40-265, reduction branches of
 // LinearElasticity.cc): basis, reduced system, reduced sweeps
 // ---------------------------------------------------------------------------
-// out[b * ostride] = Q_b . y for b < kb (Q_b = Qbase + b ndof)
-static void multidot(TopoLE *le, const double *Qbase, int kb, const double *y, double *out, int ostride) {
+// out[b * ostride] = Q_b . y for b < kb (Q_b = Qbase + b qs)
+template <class QT>
+static void multidot(TopoLE *le, const QT *Qbase, long long qs, int kb, const double *y, double *out, int ostride) {
     cudaStream_t s = le->stream;
     count_launch();
-    k_md_partial<<<dim3(MD_CHUNKS, kb), 256, 0, s>>>(le->ndof, Qbase, kb, y, le->mdpart);
+    k_md_partial<QT><<<dim3(MD_CHUNKS, kb), 256, 0, s>>>(le->ndof, Qbase, qs, kb, y, le->mdpart);
     count_launch();
     k_md_final<<<1, 32, 0, s>>>(kb, MD_CHUNKS, le->mdpart, out, ostride);
 }
@@ -1871,81 +1911,171 @@ static double *red_fx(TopoLE *le) { return red_pr(le) + le->kb; }
 // ConstructBasis (SOMMG.cc:40-210): Qb_0 = P0^-1 N P; Qb_j = P0^-1 N 2 om M Q_{j-1}
 // (the moment-matching correction of :113-176 is scaled by the comma
 // expression (-1,0) == 0 at :176 and so contributes nothing); modified
-// Gram-Schmidt against the accepted vectors and normalisation
+// Gram-Schmidt against the accepted vectors and normalisation.  The plain
+// path keeps the basis in FP64 and solves with the FP64 FCG; the mixed path
+// solves with its mixed FCG (FP32 preconditioner, FP64-accurate residual
+// replacements), orthonormalises each row in FP64 against the stored rows
+// and stores it rounded to FP32, so every later product sees the same basis
 static int sommg_basis(TopoLE *le) {
     cudaStream_t s = le->stream;
     const long long nd = le->ndof, nn = le->nn;
     const int kb = le->kb;
+    const bool b32 = le->basis32;
     const uint8_t *fixed = le->L[0].fixed;
     double *Ut = red_mat(le, RED_UT), *Pv = le->hM;
-    struct Fp64Solves {  // FP64 FCG for the basis solves, restored on every exit
+    struct Fp64Solves {  // FP64 FCG for the plain path's basis solves, restored on every exit
         TopoLE *le;
-        explicit Fp64Solves(TopoLE *l) : le(l) { le->fp64_solves = true; }
-        ~Fp64Solves() { le->fp64_solves = false; }
-    } fp64(le);
+        bool old;
+        Fp64Solves(TopoLE *l, bool on) : le(l), old(l->fp64_solves) { le->fp64_solves = on || old; }
+        ~Fp64Solves() { le->fp64_solves = old; }
+    } fp64(le, !b32);
     count_launch();
     k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->rhs0, 1.0, Pv);  // VecPointwiseMult(P, P, N), :75
     for (int j = 0; j < kb; j++) {
-        double *Qj = le->Q + (size_t)j * nd;
+        double *q = b32 ? le->qd : le->Q + (size_t)j * nd;  // the FP64 working row
         if (j == 0) {
             CK(cudaMemcpyAsync(le->sb, Pv, sizeof(double) * nd, cudaMemcpyDeviceToDevice, s));
         } else {
-            product<false, true>(le, le->Q + (size_t)(j - 1) * nd, le->ML, nullptr, 0.0, 1.0);
+            const double *prev = le->Q + (size_t)(j - 1) * nd;
+            if (b32) {
+                count_launch();
+                k_f2d_row<<<ew_blocks(nd), EW, 0, s>>>(nd, le->Q32 + (size_t)(j - 1) * le->qld, le->KL);
+                prev = le->KL;
+            }
+            product<false, true>(le, prev, le->ML, nullptr, 0.0, 1.0);
             count_launch();
             k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->ML, 2.0 * le->p.omega0, le->sb);  // :109-111, :181
         }
         CK(cudaMemsetAsync(le->sx, 0, sizeof(double) * nd, s));
         int rc = solve(le, 2, le->sb, false);  // :78-80, :185
         if (rc) return rc;
-        CK(cudaMemcpyAsync(Qj, le->sx, sizeof(double) * nd, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(q, le->sx, sizeof(double) * nd, cudaMemcpyDeviceToDevice, s));
         for (int i = 0; i < j; i++) {  // :195-202
-            const double *Qi = le->Q + (size_t)i * nd;
-            multidot(le, Qi, 1, Qj, Ut + (size_t)i * kb + j, 1);
+            double *coef = Ut + (size_t)i * kb + j;
             count_launch();
-            k_axpy_dev<<<ew_blocks(nd), EW, 0, s>>>(nd, Qj, Qi, Ut + (size_t)i * kb + j);
+            if (b32) {
+                const float *Qi = le->Q32 + (size_t)i * le->qld;
+                multidot<float>(le, Qi, le->qld, 1, q, coef, 1);
+                k_axpy_dev<float><<<ew_blocks(nd), EW, 0, s>>>(nd, q, Qi, coef);
+            } else {
+                const double *Qi = le->Q + (size_t)i * nd;
+                multidot<double>(le, Qi, nd, 1, q, coef, 1);
+                k_axpy_dev<double><<<ew_blocks(nd), EW, 0, s>>>(nd, q, Qi, coef);
+            }
         }
-        multidot(le, Qj, 1, Qj, Ut + (size_t)j * kb + j, 1);  // :92, :206
+        multidot<double>(le, q, nd, 1, q, Ut + (size_t)j * kb + j, 1);  // :92, :206
         count_launch();
-        k_normalise<<<ew_blocks(nd), EW, 0, s>>>(nd, Qj, Ut + (size_t)j * kb + j);
+        k_normalise<<<ew_blocks(nd), EW, 0, s>>>(nd, q, Ut + (size_t)j * kb + j);
         count_launch();
         k_sqrt1<<<1, 1, 0, s>>>(Ut + (size_t)j * kb + j);
+        if (b32) {
+            count_launch();
+            k_d2f_row<<<ew_blocks(nd), EW, 0, s>>>(nd, q, le->Q32 + (size_t)j * le->qld);
+        }
     }
+    CK(cudaGetLastError());
+    return TOPO_OK;
+}
+
+// one tensor-core Gram product (gram.cuh): out[a kb + b] = Q_a . W_b with
+// W_b = Wh_b + Wl_b, deterministic
+static int gram_tc(TopoLE *le, double *out) {
+    cudaStream_t s = le->stream;
+    static bool attr_dev[MAX_DEVICES] = {};
+    bool &attr = attr_dev[device_slot()];
+    if (!attr) {
+        CK(cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, GR_SMEM));
+        attr = true;
+    }
+    const GramArgs g{le->Q32, le->Wh, le->Wl, le->qld, le->kb, le->gpart, le->err, TOPO_ERR_SYNC_TIMEOUT};
+    count_launch();
+    k_gram_tc<<<le->gram_blocks, GR_THREADS, GR_SMEM, s>>>(g);
+    count_launch();
+    k_gram_final<<<(le->kb * le->kb + 255) / 256, 256, 0, s>>>(le->gram_blocks, le->gpart, le->kb, out);
     CK(cudaGetLastError());
     return TOPO_OK;
 }
 
 // reduced matrices (SOMMG.cc:228-252) and the objective projections of the
 // reduced state gradients (LinearElasticity.cc:2318-2336): column j of each is
-// Q' (A Q_j); Q vanishes on clamped DOFs, so masked and unmasked products agree
+// Q' (A Q_j); Q vanishes on clamped DOFs, so masked and unmasked products agree.
+// Plain path: FP64 dot products per column.  Mixed path: the products of all
+// columns first (FP64 products of the FP32 rows, stored as FP32 pairs), then
+// one tensor-core Gram per matrix.
 static int sommg_reduce(TopoLE *le) {
     cudaStream_t s = le->stream;
     const long long nd = le->ndof, nn = le->nn;
     const int kb = le->kb, ob = le->p.objective;
     const uint8_t *fixed = le->L[0].fixed;
     double *tmp = le->sp;
-    for (int j = 0; j < kb; j++) {
-        const double *Qj = le->Q + (size_t)j * nd;
-        product<true, false>(le, Qj, le->KL, nullptr, 1.0, 0.0);
-        multidot(le, le->Q, kb, le->KL, red_mat(le, RED_KR) + j, kb);
-        product<false, true>(le, Qj, le->ML, nullptr, 0.0, 1.0);
-        count_launch();
-        k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->ML, 1.0, tmp);
-        multidot(le, le->Q, kb, tmp, red_mat(le, RED_MR) + j, kb);
-        if (ob == 3 || ob == 5 || ob == 6) {
-            product<true, false>(le, Qj, le->KL, le->P, 1.0, 0.0);
-            multidot(le, le->Q, kb, le->KL, red_mat(le, RED_KP) + j, kb);
-        }
-        if (ob == 4 || ob == 5 || ob == 6) {
-            product<false, true>(le, Qj, le->ML, le->P, 0.0, 1.0);
-            multidot(le, le->Q, kb, le->ML, red_mat(le, RED_MP) + j, kb);
-        }
-        if (ob <= 2) {
+    const bool useK = ob == 3 || ob == 5 || ob == 6, useM = ob == 4 || ob == 5 || ob == 6, useG = ob <= 2;
+    if (!le->basis32) {
+        for (int j = 0; j < kb; j++) {
+            const double *Qj = le->Q + (size_t)j * nd;
+            product<true, false>(le, Qj, le->KL, nullptr, 1.0, 0.0);
+            multidot<double>(le, le->Q, nd, kb, le->KL, red_mat(le, RED_KR) + j, kb);
+            product<false, true>(le, Qj, le->ML, nullptr, 0.0, 1.0);
             count_launch();
-            k_cnt_mul<<<ew_blocks(nn), EW, 0, s>>>(nn, le->cntP, Qj, tmp);
-            multidot(le, le->Q, kb, tmp, red_mat(le, RED_GC) + j, kb);
+            k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->ML, 1.0, tmp);
+            multidot<double>(le, le->Q, nd, kb, tmp, red_mat(le, RED_MR) + j, kb);
+            if (useK) {
+                product<true, false>(le, Qj, le->KL, le->P, 1.0, 0.0);
+                multidot<double>(le, le->Q, nd, kb, le->KL, red_mat(le, RED_KP) + j, kb);
+            }
+            if (useM) {
+                product<false, true>(le, Qj, le->ML, le->P, 0.0, 1.0);
+                multidot<double>(le, le->Q, nd, kb, le->ML, red_mat(le, RED_MP) + j, kb);
+            }
+            if (useG) {
+                count_launch();
+                k_cnt_mul<<<ew_blocks(nn), EW, 0, s>>>(nn, le->cntP, Qj, tmp);
+                multidot<double>(le, le->Q, nd, kb, tmp, red_mat(le, RED_GC) + j, kb);
+            }
         }
+        multidot<double>(le, le->Q, nd, kb, le->hM, red_pr(le), 1);  // Pr = Q' N P
+        CK(cudaGetLastError());
+        return TOPO_OK;
     }
-    multidot(le, le->Q, kb, le->hM, red_pr(le), 1);  // Pr = Q' N P
+    enum { OP_K, OP_M, OP_KP, OP_MP, OP_GC };
+    auto project = [&](int op, int which) -> int {
+        for (int j = 0; j < kb; j++) {
+            count_launch();
+            k_f2d_row<<<ew_blocks(nd), EW, 0, s>>>(nd, le->Q32 + (size_t)j * le->qld, le->qd);
+            const double *w = tmp;
+            switch (op) {
+            case OP_K:
+                product<true, false>(le, le->qd, le->KL, nullptr, 1.0, 0.0);
+                w = le->KL;
+                break;
+            case OP_M:
+                product<false, true>(le, le->qd, le->ML, nullptr, 0.0, 1.0);
+                count_launch();
+                k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->ML, 1.0, tmp);
+                break;
+            case OP_KP:
+                product<true, false>(le, le->qd, le->KL, le->P, 1.0, 0.0);
+                w = le->KL;
+                break;
+            case OP_MP:
+                product<false, true>(le, le->qd, le->ML, le->P, 0.0, 1.0);
+                w = le->ML;
+                break;
+            default:
+                count_launch();
+                k_cnt_mul<<<ew_blocks(nn), EW, 0, s>>>(nn, le->cntP, le->qd, tmp);
+            }
+            count_launch();
+            k_split_f32<<<ew_blocks(nd), EW, 0, s>>>(nd, w, le->Wh + (size_t)j * le->qld, le->Wl + (size_t)j * le->qld);
+        }
+        return gram_tc(le, red_mat(le, which));
+    };
+    int rc = project(OP_K, RED_KR);
+    if (!rc) rc = project(OP_M, RED_MR);
+    if (!rc && useK) rc = project(OP_KP, RED_KP);
+    if (!rc && useM) rc = project(OP_MP, RED_MP);
+    if (!rc && useG) rc = project(OP_GC, RED_GC);
+    if (rc) return rc;
+    multidot<float>(le, le->Q32, le->qld, kb, le->hM, red_pr(le), 1);  // Pr = Q' N P
     CK(cudaGetLastError());
     return TOPO_OK;
 }
@@ -1989,7 +2119,8 @@ static int red_status(TopoLE *le) {
 }
 
 static void red_attributes() {
-    static bool attr = false;
+    static bool attr_dev[MAX_DEVICES] = {};
+    bool &attr = attr_dev[device_slot()];
     if (!attr) {
         cudaFuncSetAttribute(k_red_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)red_smem_bytes(KB_MAX));
         cudaFuncSetAttribute(k_red_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)red_smem_bytes(KB_MAX));
@@ -2030,22 +2161,30 @@ static int sommg_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_de
     // Phi_s = Q S_s' for S_K, S_M and the objective terms in use
     const bool useoK = ob == 3 || ob == 5 || ob == 6, useoM = ob >= 4;
     const int ns = (useoK || useoM) ? 4 : 2;
-    count_launch();
-    k_red_phi<<<ew_blocks(nd), 256, 0, s>>>(nd, kb, le->Q, le->Sacc, ns, le->Phi);
-    RedSens A;
-    A.g = le->g;
-    A.kb = kb;
-    A.Q = le->Q;
-    A.phiK = le->Phi;
-    A.phiM = le->Phi + (size_t)kb * nd;
-    A.phioK = useoK ? le->Phi + (size_t)2 * kb * nd : nullptr;
-    A.phioM = useoM ? le->Phi + (size_t)3 * kb * nd : nullptr;
-    A.dkf = le->dkf;
-    A.dmf = le->dmf;
-    A.P = le->P;
-    A.df = le->df;
-    count_launch();
-    k_red_sens<<<red_blocks(le->nel), EW, 0, s>>>(A, le->L[0].Cd);
+    auto sens = [&](auto *Q, long long qs, auto *Phi) {
+        using QT = std::remove_const_t<std::remove_pointer_t<decltype(Q)>>;
+        count_launch();
+        k_red_phi<QT><<<ew_blocks(nd), 256, 0, s>>>(nd, kb, Q, qs, le->Sacc, ns, Phi);
+        RedSens<QT> A;
+        A.g = le->g;
+        A.kb = kb;
+        A.qs = qs;
+        A.Q = Q;
+        A.phiK = Phi;
+        A.phiM = Phi + (size_t)kb * nd;
+        A.phioK = useoK ? Phi + (size_t)2 * kb * nd : nullptr;
+        A.phioM = useoM ? Phi + (size_t)3 * kb * nd : nullptr;
+        A.dkf = le->dkf;
+        A.dmf = le->dmf;
+        A.P = le->P;
+        A.df = le->df;
+        count_launch();
+        k_red_sens<QT><<<red_blocks(le->nel), EW, 0, s>>>(A, le->L[0].Cd);
+    };
+    if (le->basis32)
+        sens(static_cast<const float *>(le->Q32), le->qld, le->Phi32);
+    else
+        sens(static_cast<const double *>(le->Q), nd, le->Phi);
     CK(cudaGetLastError());
     if (dfdx_dev) CK(cudaMemcpyAsync(dfdx_dev, le->df, sizeof(double) * le->nel, cudaMemcpyDeviceToDevice, s));
     double h = 0.0;
@@ -2054,6 +2193,56 @@ static int sommg_objective_sensitivities(TopoLE *le, double *fx, double *dfdx_de
     if (rc) return rc;
     *fx = h;
     le->stats.last_fx = h;
+    return TOPO_OK;
+}
+
+// out[a kb + b] = sum_i Q[a][i] W[b][i] on the tensor cores for device rows Q
+// (FP32, stride ldq) and W (FP64, stride ldw), n values each: the Gram
+// product of the reduced matrices as a stand-alone routine (it allocates its
+// padded operands and per-CTA partials)
+int le_gram_tc_dev(const float *Q, long long ldq, const double *W, long long ldw, long long n, int kb, double *out) {
+    if (!Q || !W || !out || n < 1 || kb < 1 || kb > 32 || ldq < n || ldw < n) {
+        set_error("gram: need 1 <= kb <= 32, n >= 1 and row strides >= n");
+        return TOPO_ERR_ARG;
+    }
+    const long long ld = (n + GR_KC - 1) / GR_KC * GR_KC;
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int nblk = 2 * std::max(1, nsm);
+    Arena arena;
+    float *q = nullptr, *wh = nullptr, *wl = nullptr;
+    double *part = nullptr, *o = nullptr;
+    int *err = nullptr;
+    struct Release {
+        Arena &a;
+        ~Release() { a.release(); }
+    } rel{arena};
+    AG(q, (size_t)kb * ld);
+    AG(wh, (size_t)kb * ld);
+    AG(wl, (size_t)kb * ld);
+    AG(part, (size_t)nblk * 1024);
+    AG(o, (size_t)kb * kb);
+    AG(err, 1);
+    CK(cudaMemcpy2D(q, sizeof(float) * ld, Q, sizeof(float) * ldq, sizeof(float) * n, kb, cudaMemcpyDeviceToDevice));
+    for (int b = 0; b < kb; b++) {
+        count_launch();
+        k_split_f32<<<ew_blocks(n), EW>>>(n, W + (size_t)b * ldw, wh + (size_t)b * ld, wl + (size_t)b * ld);
+    }
+    CK(cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, GR_SMEM));
+    const GramArgs g{q, wh, wl, ld, kb, part, err, TOPO_ERR_SYNC_TIMEOUT};
+    count_launch();
+    k_gram_tc<<<nblk, GR_THREADS, GR_SMEM>>>(g);
+    count_launch();
+    k_gram_final<<<(kb * kb + 255) / 256, 256>>>(nblk, part, kb, o);
+    CK(cudaGetLastError());
+    int h = 0;
+    CK(cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        set_error("gram: an mbarrier wait of the tensor-core kernel gave up");
+        return h;
+    }
+    CK(cudaMemcpy(out, o, sizeof(double) * kb * kb, cudaMemcpyDeviceToHost));
     return TOPO_OK;
 }
 
@@ -2081,7 +2270,15 @@ int le_reduced_system(TopoLE *le, double *Q, double *Kr, double *Mr, double *Pr)
     }
     cudaStream_t s = le->stream;
     const size_t k2 = (size_t)le->kb * le->kb;
-    if (Q) CK(cudaMemcpyAsync(Q, le->Q, sizeof(double) * le->kb * le->ndof, cudaMemcpyDeviceToHost, s));
+    if (Q && le->basis32) {  // the FP32 rows, widened
+        std::vector<float> h((size_t)le->kb * le->ndof);
+        CK(cudaMemcpy2DAsync(h.data(), sizeof(float) * le->ndof, le->Q32, sizeof(float) * le->qld,
+                             sizeof(float) * le->ndof, le->kb, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        for (size_t i = 0; i < h.size(); i++) Q[i] = h[i];
+    } else if (Q) {
+        CK(cudaMemcpyAsync(Q, le->Q, sizeof(double) * le->kb * le->ndof, cudaMemcpyDeviceToHost, s));
+    }
     if (Kr) CK(cudaMemcpyAsync(Kr, red_mat(le, RED_KR), sizeof(double) * k2, cudaMemcpyDeviceToHost, s));
     if (Mr) CK(cudaMemcpyAsync(Mr, red_mat(le, RED_MR), sizeof(double) * k2, cudaMemcpyDeviceToHost, s));
     if (Pr) CK(cudaMemcpyAsync(Pr, red_pr(le), sizeof(double) * le->kb, cudaMemcpyDeviceToHost, s));
@@ -2110,13 +2307,21 @@ static int out_block(TopoLE *le, int c) {
     return TOPO_OK;
 }
 
+// full = sum_k r_k Q_k (the lifts of LinearElasticity.cc:1087-1108, :1225-1243)
+static void lift(TopoLE *le, const double *r, double *full) {
+    const long long nd = le->ndof;
+    count_launch();
+    if (le->basis32)
+        k_lift<float><<<ew_blocks(nd), EW, 0, le->stream>>>(nd, le->kb, le->Q32, le->qld, r, full);
+    else
+        k_lift<double><<<ew_blocks(nd), EW, 0, le->stream>>>(nd, le->kb, le->Q, nd, r, full);
+}
+
 // reduced path: steps t0..t1 of the reduced history lifted to the full space,
 // U = sum_k u_k Q_k (LinearElasticity.cc:1087-1108, :1225-1243)
 static int out_reduced(TopoLE *le, int t0, int t1) {
-    const long long nd = le->ndof;
     for (int t = t0; t <= t1; t++) {
-        count_launch();
-        k_lift<<<ew_blocks(nd), EW, 0, le->stream>>>(nd, le->kb, le->Q, le->rhist + (size_t)t * 3 * le->kb, le->sp);
+        lift(le, le->rhist + (size_t)t * 3 * le->kb, le->sp);
         int rc = out_state(le, (unsigned long long)t, le->sp);
         if (rc) return rc;
     }
@@ -2349,9 +2554,7 @@ int le_get_state(TopoLE *le, int which, int j, double *out) {
     long long nd = le->ndof;
     if (le->kb) {  // lift the reduced state (LinearElasticity.cc:1225-1243)
         const int t = le->p.tsc * (le->p.ncp - 1) + j + 1;
-        count_launch();
-        k_lift<<<ew_blocks(nd), EW, 0, le->stream>>>(nd, le->kb, le->Q,
-                                                       le->rhist + ((size_t)t * 3 + which) * le->kb, le->sp);
+        lift(le, le->rhist + ((size_t)t * 3 + which) * le->kb, le->sp);
         CK(cudaMemcpyAsync(out, le->sp, sizeof(double) * nd, cudaMemcpyDeviceToHost, le->stream));
         CK(cudaStreamSynchronize(le->stream));
         return TOPO_OK;

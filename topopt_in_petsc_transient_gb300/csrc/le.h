@@ -35,6 +35,7 @@ int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms);
 int le_kernel_timing(TopoLE *le, int kclass, int enable, double *ms_total, long long *launches);
 int le_reduced_system(TopoLE *le, double *Q, double *Kr, double *Mr, double *Pr);
 int le_sommg_construct_basis(TopoLE *le, double om);
+int le_gram_tc_dev(const float *Q, long long ldq, const double *W, long long ldw, long long n, int kb, double *out);
 int le_basis(const TopoLE *le);
 void le_damping(const TopoLE *le, double *alpha, double *beta);
 void box_element_matrices(double hx, double hy, double hz, double nu, double *KE, double *ME);

@@ -24,14 +24,16 @@ constexpr int KB_MAX = 32;  // basis vectors supported by the reduced kernels
 
 // ---- reductions against the basis: out[b * ostride] = Q_b . y, b < kb ----
 // deterministic: per-chunk partials, then a fixed-order sum
+// (Q_b = Q + b qs: FP64 rows of the plain path, FP32 rows of the mixed path)
 constexpr int MD_CHUNKS = 152;
-static __global__ void __launch_bounds__(256) k_md_partial(long long nd, const double *__restrict__ Q, int kb,
+template <class QT>
+static __global__ void __launch_bounds__(256) k_md_partial(long long nd, const QT *__restrict__ Q, long long qs, int kb,
                                                            const double *__restrict__ y, double *part) {
     const int b = blockIdx.y;
-    const double *q = Q + (size_t)b * nd;
+    const QT *q = Q + (size_t)b * qs;
     double s = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x)
-        s += q[i] * y[i];
+        s += (double)q[i] * y[i];
     __shared__ double sm[8];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
@@ -51,10 +53,20 @@ static __global__ void k_md_final(int kb, int nchunk, const double *__restrict__
 }
 
 // modified Gram-Schmidt step (SOMMG.cc:195-202): v -= coef * q
-static __global__ void k_axpy_dev(long long nd, double *v, const double *__restrict__ q, const double *coef) {
+template <class QT>
+static __global__ void k_axpy_dev(long long nd, double *v, const QT *__restrict__ q, const double *coef) {
     const double c = *coef;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x)
-        v[i] -= c * q[i];
+        v[i] -= c * (double)q[i];
+}
+// basis row j of the FP32 basis from its FP64 solve, and back
+static __global__ void k_d2f_row(long long nd, const double *__restrict__ x, float *q) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x)
+        q[i] = (float)x[i];
+}
+static __global__ void k_f2d_row(long long nd, const float *__restrict__ q, double *x) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x)
+        x[i] = (double)q[i];
 }
 // normalisation (SOMMG.cc:92-95, :206-208): v /= sqrt(nrm2)
 static __global__ void k_normalise(long long nd, double *v, const double *nrm2) {
@@ -79,11 +91,12 @@ static __global__ void k_cnt_mul(long long nn, const float *__restrict__ cnt, co
     }
 }
 // full = sum_b r[b] Q_b (the lift of LinearElasticity.cc:1089-1107), for output
-static __global__ void k_lift(long long nd, int kb, const double *__restrict__ Q, const double *__restrict__ r,
-                              double *full) {
+template <class QT>
+static __global__ void k_lift(long long nd, int kb, const QT *__restrict__ Q, long long qs,
+                              const double *__restrict__ r, double *full) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x) {
         double s = 0.0;
-        for (int b = 0; b < kb; b++) s += r[b] * Q[(size_t)b * nd + i];
+        for (int b = 0; b < kb; b++) s += r[b] * (double)Q[(size_t)b * qs + i];
         full[i] = s;
     }
 }
@@ -382,22 +395,24 @@ static __global__ void k_red_adjoint(RedSys R) {
 }
 
 // Phi_s = Q S_s' for the accumulators in use: Phi_s[a] = sum_b S_s[a][b] Q_b
-static __global__ void __launch_bounds__(256) k_red_phi(long long nd, int kb, const double *__restrict__ Q,
-                                                        const double *__restrict__ S, int ns, double *Phi) {
+// (FP64 sums; Phi stored in the basis type, rows of nd values)
+template <class QT>
+static __global__ void __launch_bounds__(256) k_red_phi(long long nd, int kb, const QT *__restrict__ Q, long long qs,
+                                                        const double *__restrict__ S, int ns, QT *Phi) {
     __shared__ double sS[4 * KB_MAX * KB_MAX];
     for (int i = threadIdx.x; i < ns * kb * kb; i += blockDim.x) sS[i] = S[i];
     __syncthreads();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x) {
         double q[KB_MAX];
 #pragma unroll
-        for (int b = 0; b < KB_MAX; b++) q[b] = b < kb ? Q[(size_t)b * nd + i] : 0.0;
+        for (int b = 0; b < KB_MAX; b++) q[b] = b < kb ? (double)Q[(size_t)b * qs + i] : 0.0;
         for (int s = 0; s < ns; s++)
             for (int a = 0; a < kb; a++) {
                 double acc = 0.0;
 #pragma unroll
                 for (int b = 0; b < KB_MAX; b++)
                     if (b < kb) acc += sS[(s * kb + a) * kb + b] * q[b];
-                Phi[((size_t)s * kb + a) * nd + i] = acc;
+                Phi[((size_t)s * kb + a) * nd + i] = (QT)acc;
             }
     }
 }
@@ -405,14 +420,17 @@ static __global__ void __launch_bounds__(256) k_red_phi(long long nd, int kb, co
 // element sensitivities of the reduced path (the sum over every step of
 // ComputeSensitivitiesElementLoopn / Loop0, in mode space):
 //   df_e = dkf_e sum_a x_a' KE (phiK_a + P_e phioK_a) + dmf_e sum_a x_a' ME (phiM_a + P_e phioM_a)
+template <class QT>
 struct RedSens {
     GridDesc g;
     int kb;
-    const double *Q, *phiK, *phiM, *phioK, *phioM;  // phio* may be null
+    long long qs;                                // row stride of Q
+    const QT *Q, *phiK, *phiM, *phioK, *phioM;  // phio* may be null; Phi rows of nd values
     const double *dkf, *dmf, *P;
     double *df;
 };
-static __global__ void __launch_bounds__(EW) k_red_sens(const RedSens A, const ElemConst<double> C) {
+template <class QT>
+static __global__ void __launch_bounds__(EW) k_red_sens(const RedSens<QT> A, const ElemConst<double> C) {
     const GridDesc g = A.g;
     const long long nel = g.nel(), nd = 3 * g.nn();
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
@@ -426,7 +444,7 @@ static __global__ void __launch_bounds__(EW) k_red_sens(const RedSens A, const E
         for (int a = 0; a < A.kb; a++) {
             const size_t off = (size_t)a * nd;
             double X[3][8], Y[3][8], KX[3][8];
-            gather8<double>(A.Q + off, nodes, X);
+            gather8<double>(A.Q + (size_t)a * A.qs, nodes, X);
 #pragma unroll
             for (int c = 0; c < 3; c++) mode_fwd(X[c]);
             mode_khat(C, X, KX);
@@ -435,7 +453,7 @@ static __global__ void __launch_bounds__(EW) k_red_sens(const RedSens A, const E
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     const long long q = 3 * nodes[L] + c;
-                    Y[c][L] = A.phiK[off + q] + (A.phioK ? Pe * A.phioK[off + q] : 0.0);
+                    Y[c][L] = (double)A.phiK[off + q] + (A.phioK ? Pe * (double)A.phioK[off + q] : 0.0);
                 }
 #pragma unroll
             for (int c = 0; c < 3; c++) {
@@ -448,7 +466,7 @@ static __global__ void __launch_bounds__(EW) k_red_sens(const RedSens A, const E
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     const long long q = 3 * nodes[L] + c;
-                    Y[c][L] = A.phiM[off + q] + (A.phioM ? Pe * A.phioM[off + q] : 0.0);
+                    Y[c][L] = (double)A.phiM[off + q] + (A.phioM ? Pe * (double)A.phioM[off + q] : 0.0);
                 }
 #pragma unroll
             for (int c = 0; c < 3; c++) {
