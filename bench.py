@@ -61,7 +61,7 @@ def workload(args):
                 coarse_dense_max=args.coarse_dense_max, coarse_smooth=args.coarse_smooth, sens_fp32=args.sens_fp32,
                 inner_tol=args.inner_tol, inner_maxit=args.inner_maxit, use_graphs=not args.no_graphs,
                 reduction=args.reduction, basis=args.basis, omega0=args.omega0,
-                noise=args.noise, tile_form=args.tile_form, kron_form=args.kron_form, **load2(args))
+                noise=args.noise, **load2(args))
 
 
 def load2(args):
@@ -177,8 +177,7 @@ def make_physics(o, **over):
               cheb_ratio=o.cheb_ratio, use_graphs=o.use_graphs, coarse_dense_max=o.coarse_dense_max,
               coarse_smooth=o.coarse_smooth, sens_fp32=o.sens_fp32, inner_tol=o.inner_tol,
               inner_maxit=o.inner_maxit, reduction=o.reduction, basis=o.basis, omega0=o.omega0,
-              load2_node=o.load2_node, load2_phase=o.load2_phase, out_dof=o.out_dof, tile_form=o.tile_form,
-              kron_form=o.kron_form)
+              load2_node=o.load2_node, load2_phase=o.load2_phase, out_dof=o.out_dof)
     kw.update(over)
     return LinearElasticity(o.nelx, o.nely, o.nelz, **kw)
 
@@ -299,7 +298,7 @@ def run_gb300(args):
         e2e = run_e2e(args, wl, flush_l2)
 
     # ---- roofline of the dominant kernels, timed in the solve ----
-    roof = roofline(args, wl, opt)
+    roof = roofline(args, wl, opt) if args.roofline else None
 
     # ---- central finite differences of the adjoint sensitivities ----
     fd = None
@@ -326,8 +325,6 @@ def run_gb300(args):
                    "dofs": 3 * (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1), "elements": opt_nel(wl),
                    "steps_per_design_iter": args.nsteps, "ncp": args.ncp,
                    "rtol": args.rtol, "smooth": args.smooth, "nlvls": args.nlvls,
-                   "operator_kernels": "z-marching slabs" if args.tile_form == 1 else "bricks",
-                   "kronecker_passes": "register line segments" if args.kron_form == 1 else "staged lines",
                    "l2": "state history %.1f GB > 129 MB L2; 256 MB L2 flush between timed iterations"
                          % (3 * args.nsteps / args.ncp * 3 * (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1)
                             * 8 / 1e9),
@@ -702,6 +699,8 @@ def main():
                     help="timed plain FP64 iterations (default: --steps)")
     ap.add_argument("--e2e-steps", dest="e2e_steps", type=int, default=2)
     ap.add_argument("--no-cpu", dest="cpu_sample", action="store_false")
+    ap.add_argument("--no-roofline", dest="roofline", action="store_false",
+                    help="skip the per-kernel-class timing iterations")
     ap.add_argument("--no-oracle-check", dest="oracle_check", action="store_false",
                     help="skip the full oracle evaluation of the accuracy workload")
     ap.add_argument("--oracle-mesh", dest="oracle_mesh", default="96x48x48")
@@ -715,10 +714,6 @@ def main():
     ap.add_argument("--fd-rtol", dest="fd_rtol", type=float, default=1e-12)
     ap.add_argument("--fd-floor", dest="fd_floor", type=float, default=0.01,
                     help="finite differences on elements with |dfdx| >= this fraction of max|dfdx|")
-    ap.add_argument("--tile-form", dest="tile_form", type=int, default=0,
-                    help="operator kernels: 0 bricks of 7x7x7 output nodes, 1 z-marching slabs")
-    ap.add_argument("--kron-form", dest="kron_form", type=int, default=0,
-                    help="Kronecker y/z passes: 0 lines staged in shared memory, 1 register line segments")
     args = ap.parse_args()
     if args.plain_steps is None:
         args.plain_steps = args.steps

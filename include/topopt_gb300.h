@@ -102,16 +102,6 @@ typedef struct topo_le_params {
     int load2_node;
     double load2_phase;
     int out_dof;
-    /* form of the FP32 and double-float operator kernels: 0 = bricks of
-     * 7x7x7 output nodes (default), 1 = z-marching slabs of 15x15 output
-     * nodes (fewer recomputed elements and staged nodes per output); FP64
-     * kernels always use bricks.  The form of the most recently created
-     * object applies process-wide */
-    int tile_form;
-    /* form of the y and z passes of the FP32 Kronecker preconditioner:
-     * 0 = lines staged in shared memory (default), 1 = one thread per line
-     * segment of 16 positions with its window in registers (same outputs) */
-    int kron_form;
 } topo_le_params;
 
 typedef struct topo_le_stats {
@@ -161,7 +151,10 @@ int topo_le_volume_constraint_dev(topo_le *le, double *gx, double *dgdx_dev, con
  * 1..16,777,216 (TOPO_ERR_ARG otherwise).  The first call on a device looks up
  * the scratch address and should come before any stream capture.  Calls that
  * overlap in time on one device share the scratch and race; each call runs on
- * the legacy default stream and returns after gx has been copied to the host. */
+ * the legacy default stream and returns after gx has been copied to the host.
+ * The legacy stream does not wait for work on non-blocking streams: xPhys_dev
+ * must be complete (its producing stream synchronised) before the call, as for
+ * topo_le_volume_constraint_dev. */
 int topo_volume_constraint_noalloc_dev(long long nel, double *gx, double *dgdx_dev, const double *xPhys_dev,
                                        double volfrac);
 

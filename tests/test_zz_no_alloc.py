@@ -56,3 +56,23 @@ def test_noalloc_volume_constraint_rejects_sizes_beyond_its_scratch(gpu):
         assert b"outside 1..16777216" in L.topo_last_error()
     rc, gx = _call(L, 16, dg, x, 0.5)
     assert rc == 0 and gx == -0.5 and torch.all(dg == 1.0 / 16)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [MAX_NEL, MAX_NEL - 1, 16_777_216 - 8 * 256 * 8 + 1])
+def test_noalloc_volume_constraint_at_the_scratch_limit(gpu, n):
+    # the last partial slot in use (a full last CTA, and a last CTA with one
+    # element or one thread's share missing), two calls in a row: gx against
+    # torch's FP64 mean, dgdx exactly 1/n
+    import torch
+    L = _lib.load()
+    g = torch.Generator(device=gpu).manual_seed(n)
+    x = torch.rand(n, dtype=torch.float64, device=gpu, generator=g)
+    ref = x.mean().item() - 0.12
+    for _ in range(2):
+        dg = torch.full_like(x, -1.0)
+        torch.cuda.synchronize()
+        rc, gx = _call(L, n, dg, x, 0.12)
+        assert rc == 0, L.topo_last_error()
+        assert abs(gx - ref) <= 1e-14 * max(1.0, abs(ref))
+        assert bool(torch.all(dg == 1.0 / n))

@@ -41,8 +41,7 @@ class LEParams(C.Structure):
         ("inner_tol", C.c_double), ("inner_maxit", C.c_int), ("adaptive_kappa", C.c_double),
         ("extrapolate", C.c_int), ("mass_precond", C.c_int), ("mass_precond_share", C.c_double),
         ("mass_precond_smooth", C.c_int), ("reduction", C.c_int), ("basis", C.c_int), ("omega0", C.c_double),
-        ("load2_node", C.c_int), ("load2_phase", C.c_double), ("out_dof", C.c_int), ("tile_form", C.c_int),
-        ("kron_form", C.c_int),
+        ("load2_node", C.c_int), ("load2_phase", C.c_double), ("out_dof", C.c_int),
     ]
 
 

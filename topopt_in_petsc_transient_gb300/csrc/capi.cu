@@ -121,8 +121,6 @@ void topo_le_default_params(topo_le_params *p, int nelx, int nely, int nelz) {
     p->load2_node = -1;
     p->load2_phase = 0.0;
     p->out_dof = -1;
-    p->tile_form = 0;
-    p->kron_form = 0;
 }
 
 int topo_le_create(topo_le **out, const topo_le_params *p) {

@@ -167,10 +167,7 @@ __host__ inline int kx_lines_launch(const GridDesc &g, size_t elem, long long sl
     return (int)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
-// INCR: the thread's (line, position) and (row, group) indices advance with
-// carries as t steps by the block size (one integer division per thread
-// instead of one per value); the same mapping as the divided form
-template <class T, class R, bool INCR>
+template <class T, class R>
 __device__ __forceinline__ void kron_x_body(const GridDesc &g, int kx, R *r, const double *__restrict__ r64,
                                             const SolveScalars *S, const T *__restrict__ ms, const KronBand<T> &B,
                                             T *out) {
@@ -188,15 +185,9 @@ __device__ __forceinline__ void kron_x_body(const GridDesc &g, int kx, R *r, con
     kron_stage_interior(B, 0, g.nx, tint);
     const long long q0 = line0 * row;
     const int nv = nl * row;
-    // line l and position w of value t = l row + w, and their step per trip
-    const int sl = KRON_THREADS / row, sw = KRON_THREADS - sl * row;
-    int l = (int)threadIdx.x / row, w = (int)threadIdx.x - l * row;
 #pragma unroll 4
     for (int t = threadIdx.x; t < nv; t += KRON_THREADS) {
-        if (!INCR) {
-            l = t / row;
-            w = t - l * row;
-        }
+        const int l = t / row, w = t - l * row;  // line and position of value t
         const int i = w / 3, c = w - 3 * i;
         const long long q = q0 + t;
         R rv;
@@ -208,25 +199,12 @@ __device__ __forceinline__ void kron_x_body(const GridDesc &g, int kx, R *r, con
         }
         const T m = ms[q];
         tile[(l * 3 + c) * LP + i] = m < T(0) ? T(0) : (T)rv * m;
-        if (INCR) {
-            l += sl;
-            w += sw;
-            if (w >= row) {
-                w -= row;
-                l++;
-            }
-        }
     }
     __syncthreads();
     const int ngrp = (g.nx + KRON_MP - 1) / KRON_MP;
     const int nrows = nl * 3;
-    const int sgrp = KRON_THREADS / nrows, sr = KRON_THREADS - sgrp * nrows;
-    int rw = (int)threadIdx.x % nrows, grp = (int)threadIdx.x / nrows;
     for (int t = threadIdx.x; t < nrows * ngrp; t += KRON_THREADS) {
-        if (!INCR) {
-            rw = t % nrows;
-            grp = t / nrows;
-        }
+        const int rw = t % nrows, grp = t / nrows;
         const int c = rw % 3;
         const int p0 = grp * KRON_MP;
         T o[KRON_MP];
@@ -234,34 +212,13 @@ __device__ __forceinline__ void kron_x_body(const GridDesc &g, int kx, R *r, con
 #pragma unroll
         for (int k = 0; k < KRON_MP; k++)
             if (p0 + k < g.nx) otile[rw * LP + p0 + k] = o[k];
-        if (INCR) {
-            grp += sgrp;
-            rw += sr;
-            if (rw >= nrows) {
-                rw -= nrows;
-                grp++;
-            }
-        }
     }
     __syncthreads();
-    l = (int)threadIdx.x / row;
-    w = (int)threadIdx.x - l * row;
 #pragma unroll 4
     for (int t = threadIdx.x; t < nv; t += KRON_THREADS) {
-        if (!INCR) {
-            l = t / row;
-            w = t - l * row;
-        }
+        const int l = t / row, w = t - l * row;
         const int i = w / 3, c = w - 3 * i;
         out[q0 + t] = otile[(l * 3 + c) * LP + i];
-        if (INCR) {
-            l += sl;
-            w += sw;
-            if (w >= row) {
-                w -= row;
-                l++;
-            }
-        }
     }
 }
 
@@ -269,16 +226,8 @@ template <class T, class R>
 static __global__ void __launch_bounds__(KRON_THREADS)
     k_kron_x(GridDesc g, int kx, R *r, const double *__restrict__ r64, const SolveScalars *S, const T *__restrict__ ms,
              KronBand<T> B, T *out) {
-    kron_x_body<T, R, false>(g, kx, r, r64, S, ms, B, out);
+    kron_x_body<T, R>(g, kx, r, r64, S, ms, B, out);
 }
-// the incremental-index form (kron_form = 1), held to 64 registers (4 CTAs per SM)
-template <class T, class R>
-static __global__ void __launch_bounds__(KRON_THREADS, 4)
-    k_kron_xi(GridDesc g, int kx, R *r, const double *__restrict__ r64, const SolveScalars *S,
-              const T *__restrict__ ms, KronBand<T> B, T *out) {
-    kron_x_body<T, R, true>(g, kx, r, r64, S, ms, B, out);
-}
-
 // y pass (AXIS 1) and z pass (AXIS 2): a CTA stages a chunk of KW values of
 // one x-row (consecutive in memory) at every position along the line.  The
 // z pass finishes P^-1: out = S x on free DOFs, r on clamped ones; with DOT it
@@ -365,101 +314,6 @@ static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
             S->beta = S->restart ? 0.0 : -tot[1] / S->pq;
             if (!isfinite(S->beta)) S->beta = 0.0;
             S->rescale = 0;
-        }
-    }
-}
-
-// Line-segment form of the y and z passes (kron_form = 1, FP32): one thread
-// per (x-row value w, line, segment of KSEG positions) loads the KSEG +
-// 2 KRON_B window values of its segment at once -- independent loads,
-// coalesced across consecutive w -- and applies the same tap rows in the same
-// order as kron_line, so its outputs equal the staged passes'.  No shared
-// memory and no barriers; neighbouring segments re-read their 2 KRON_B halo
-// values from L1/L2.
-constexpr int KSEG = 16;
-constexpr int KSEG_THREADS = 256;
-
-__host__ inline long long kron_seg_items(const GridDesc &g, int axis) {
-    const int len = axis == 1 ? g.ny : g.nz;
-    return 3LL * g.nx * (axis == 1 ? g.nz : g.ny) * ((len + KSEG - 1) / KSEG);
-}
-
-template <class T, class R, int AXIS, bool DOT>
-static __global__ void __launch_bounds__(KSEG_THREADS, 2)
-    k_kron_seg(GridDesc g, const R *__restrict__ r, const T *__restrict__ ms, KronBand<T> B,
-               const T *__restrict__ in, T *out, KronDot kd) {
-    const int row = 3 * g.nx;
-    const int len = AXIS == 1 ? g.ny : g.nz;
-    const int nother = AXIS == 1 ? g.nz : g.ny;
-    const int nseg = (len + KSEG - 1) / KSEG;
-    const long long S = AXIS == 1 ? (long long)row : (long long)row * g.ny;
-    const long long items = (long long)row * nother * nseg;
-    double red[2] = {0.0, 0.0};
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < items;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int w = (int)(t % row);
-        const long long rest = t / row;
-        const int other = (int)(rest % nother), seg = (int)(rest / nother);
-        const long long base = AXIS == 1 ? (long long)other * row * g.ny + w : (long long)other * row + w;
-        const int c = w % 3;
-        const int p0 = seg * KSEG;
-        T win[KSEG + 2 * KRON_B];
-#pragma unroll
-        for (int k = 0; k < KSEG + 2 * KRON_B; k++) {
-            int p = p0 - KRON_B + k;
-            p = p < 0 ? 0 : (p > len - 1 ? len - 1 : p);
-            win[k] = in[base + p * S];
-        }
-        const T *mid = B.row(AXIS, c, len / 2);  // interior taps (the staged passes' tint)
-        // output k of the segment: the z pass finishes P^-1 and its dots
-        auto emit = [&](int k, T o) {
-            const int p = p0 + k;
-            if (p >= len) return;
-            const long long q = base + p * S;
-            if (AXIS == 2) {
-                const T m = ms[q], rv = (T)r[q];
-                const T z = m < T(0) ? rv : m * o;
-                out[q] = z;
-                if (DOT) {
-                    red[0] += (double)((float)z * (float)rv);
-                    red[1] += (double)((float)z * kd.q32[q]);
-                }
-            } else {
-                out[q] = o;
-            }
-        };
-        if (p0 >= KRON_B && p0 + KSEG <= len - KRON_B) {
-            T tap[KRON_W];
-#pragma unroll
-            for (int d = 0; d < KRON_W; d++) tap[d] = mid[d];
-#pragma unroll
-            for (int k = 0; k < KSEG; k++) {
-                T acc = T(0);
-#pragma unroll
-                for (int d = 0; d < KRON_W; d++) acc += tap[d] * win[k + d];
-                emit(k, acc);
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < KSEG; k++) {
-                const int pos = p0 + k;
-                const T *tp = (pos >= KRON_B && pos < len - KRON_B) ? mid : B.row(AXIS, c, pos < len ? pos : len - 1);
-                T acc = T(0);
-#pragma unroll
-                for (int d = 0; d < KRON_W; d++) acc += tp[d] * win[k + d];
-                emit(k, acc);
-            }
-        }
-    }
-    if constexpr (DOT) {
-        double tot[2];
-        if (grid_reduce<KSEG_THREADS, 2>(red, kd.part, tot)) {
-            SolveScalars *S2 = kd.S;
-            S2->rho = tot[0];
-            S2->gam = tot[1];
-            S2->beta = S2->restart ? 0.0 : -tot[1] / S2->pq;
-            if (!isfinite(S2->beta)) S2->beta = 0.0;
-            S2->rescale = 0;
         }
     }
 }

@@ -24,7 +24,6 @@
 #include "le.h"
 #include "kron.cuh"
 #include "mpiio.h"
-#include "slab.cuh"
 #include "sommg.cuh"
 #include "gram.cuh"
 
@@ -40,10 +39,6 @@ namespace topo {
     } while (0)
 
 static thread_local std::string g_last_error;
-// form of the FP32 and double-float operator kernels (topo_le_params.tile_form):
-// 0 bricks (tile.cuh), 1 z-marching slabs (slab.cuh); set by le_create,
-// applies process-wide
-static int g_tile_form = 0;
 
 // Function attributes, occupancy and SM counts are properties of a device:
 // the one-time caches of the launch helpers are indexed by the ordinal of the
@@ -270,31 +265,6 @@ constexpr int tile_class() {
 // count; the others launch one CTA per brick
 template <class T, class Pol>
 static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, cudaStream_t s) {
-    // z-marching slabs (slab.cuh) for the FP32 and double-float kernels; the
-    // FP64 ones keep the brick form (their carried corners would spill), and
-    // so does a grid whose slabs would fill less than half the resident slots
-    // (small meshes, coarse multigrid levels)
-    if constexpr (!std::is_same<T, double>::value) if (g_tile_form == 1) {
-        static long long slots_dev[MAX_DEVICES] = {};
-        long long &slots = slots_dev[device_slot()];
-        const size_t sm = slab_smem_bytes<T, Pol>();
-        if (!slots) {
-            cudaFuncSetAttribute(k_slab<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            int dev = 0, nsm = 0, per_sm = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_slab<T, Pol>, SLAB_THREADS, sm);
-            slots = (long long)std::max(1, per_sm) * std::max(1, nsm);
-        }
-        const SlabShape sh = slab_shape(g, slots);
-        if (2LL * sh.ncx * sh.ncy * sh.nzr >= slots) {
-            const bool timed = tile_class<T, Pol>() >= 0 && timer_begin(tile_class<T, Pol>(), g.nn(), s);
-            count_launch();
-            k_slab<T, Pol><<<(unsigned)(sh.ncx * sh.ncy * sh.nzr), SLAB_THREADS, sm, s>>>(g, C, pol, sh);
-            timer_end(timed, s);
-            return;
-        }
-    }
     static int resident_dev[MAX_DEVICES] = {};
     int &resident = resident_dev[device_slot()];
     const size_t sm = tile_smem_bytes<T, Pol>();
@@ -386,7 +356,7 @@ struct TopoLE {
     double *AUt = nullptr, *AVt = nullptr, *AAt = nullptr, *AApt = nullptr, *KSt = nullptr;
     bool fwd_init_pending = false;
     int kb = 0;
-    bool fp64_solves = false;  // the SOMMG basis solves of the plain path run the FP64 FCG
+    bool fp64_solves = false;  // the SOMMG basis solves run the FP64 FCG in either mode
     double *Q = nullptr, *red = nullptr, *rhist = nullptr, *Sacc = nullptr, *Phi = nullptr, *mdpart = nullptr;
     int *rstatus = nullptr;
     // mixed path: the basis in FP32 (rows of qld >= ndof values, a multiple of
@@ -489,8 +459,7 @@ int le_create(TopoLE **out, const LEParams *pp) {
     const LEParams &p = *pp;
     if (p.nx < 2 || p.ny < 2 || p.nz < 2 || p.ncp < 1 || p.tsc < 1 || p.nlvls < 1 || p.hx <= 0 || p.hy <= 0 ||
         p.hz <= 0 || p.t1 <= 0 || p.objective < 0 || p.objective > 7 ||
-        p.load2_node >= (long long)p.nx * p.ny * p.nz || p.out_dof >= 3LL * p.nx * p.ny * p.nz ||
-        p.tile_form < 0 || p.tile_form > 1 || p.kron_form < 0 || p.kron_form > 1) {
+        p.load2_node >= (long long)p.nx * p.ny * p.nz || p.out_dof >= 3LL * p.nx * p.ny * p.nz) {
         set_error("invalid LinearElasticity parameters");
         return TOPO_ERR_ARG;
     }
@@ -509,7 +478,6 @@ int le_create(TopoLE **out, const LEParams *pp) {
         set_error("mesh dimension not compatible with the number of multigrid levels");
         return TOPO_ERR_ARG;
     }
-    g_tile_form = p.tile_form;
     TopoLE *le = new TopoLE();
     le->p = p;
     le->g = GridDesc{p.nx, p.ny, p.nz, p.nx - 1, p.ny - 1, p.nz - 1};
@@ -1091,8 +1059,6 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     bool &attr = attr_dev[device_slot()];
     if (!attr) {  // staged lines: the selection keeps every pass within KRON_SMEM_MAX
         cudaFuncSetAttribute(k_kron_x<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
-        if constexpr (std::is_same<T, float>::value)
-            cudaFuncSetAttribute(k_kron_xi<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
         cudaFuncSetAttribute(k_kron_yz<T, T, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
         cudaFuncSetAttribute(k_kron_yz<T, T, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
         cudaFuncSetAttribute(k_kron_yz<T, T, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KRON_SMEM_MAX);
@@ -1101,39 +1067,9 @@ static T *kron_apply(TopoLE *le, int o, T *r, VFuse *fz = nullptr) {
     bool t;
     count_launch();
     t = timer_begin(TOPO_KT_KRON, g.nn(), s);
-    bool incr = false;
-    if constexpr (std::is_same<T, float>::value) {
-        incr = le->p.kron_form == 1;
-        if (incr)  // incremental indices (same outputs)
-            k_kron_xi<T, T><<<(unsigned)((nlines + kx - 1) / kx), KRON_THREADS, smx, s>>>(
-                g, kx, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
-    }
-    if (!incr)
-        k_kron_x<T, T><<<(unsigned)((nlines + kx - 1) / kx), KRON_THREADS, smx, s>>>(
-            g, kx, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
+    k_kron_x<T, T><<<(unsigned)((nlines + kx - 1) / kx), KRON_THREADS, smx, s>>>(
+        g, kx, r, mixed ? fz->r64 : nullptr, mixed ? fz->S : nullptr, sc, B, w.xa);
     timer_end(t, s);
-    if constexpr (std::is_same<T, float>::value) {
-        if (le->p.kron_form == 1) {  // y and z passes as register line segments (same outputs)
-            const unsigned gy = (unsigned)((kron_seg_items(g, 1) + KSEG_THREADS - 1) / KSEG_THREADS);
-            const unsigned gz = (unsigned)((kron_seg_items(g, 2) + KSEG_THREADS - 1) / KSEG_THREADS);
-            count_launch();
-            t = timer_begin(TOPO_KT_KRON, g.nn(), s);
-            k_kron_seg<T, T, 1, false><<<gy, KSEG_THREADS, 0, s>>>(g, r, sc, B, w.xa, w.xb, KronDot{});
-            timer_end(t, s);
-            count_launch();
-            t = timer_begin(TOPO_KT_KRON, g.nn(), s);
-            if (mixed && le->p.mass_precond_smooth <= 0) {
-                k_kron_seg<T, T, 2, true><<<gz, KSEG_THREADS, 0, s>>>(g, r, sc, B, w.xb, w.xa,
-                                                                       KronDot{fz->q32, fz->S, fz->part});
-                fz->dotted = true;
-            } else {
-                k_kron_seg<T, T, 2, false><<<gz, KSEG_THREADS, 0, s>>>(g, r, sc, B, w.xb, w.xa, KronDot{});
-            }
-            timer_end(t, s);
-            if (mixed) fz->scaled = true;
-            return w.xa;
-        }
-    }
     count_launch();
     t = timer_begin(TOPO_KT_KRON, g.nn(), s);
     k_kron_yz<T, T, 1, false><<<kron_yz_blocks(g, 1), KRON_THREADS, smy, s>>>(g, r, sc, B, w.xa, w.xb, KronDot{});
@@ -1911,11 +1847,13 @@ static double *red_fx(TopoLE *le) { return red_pr(le) + le->kb; }
 // ConstructBasis (SOMMG.cc:40-210): Qb_0 = P0^-1 N P; Qb_j = P0^-1 N 2 om M Q_{j-1}
 // (the moment-matching correction of :113-176 is scaled by the comma
 // expression (-1,0) == 0 at :176 and so contributes nothing); modified
-// Gram-Schmidt against the accepted vectors and normalisation.  The plain
-// path keeps the basis in FP64 and solves with the FP64 FCG; the mixed path
-// solves with its mixed FCG (FP32 preconditioner, FP64-accurate residual
-// replacements), orthonormalises each row in FP64 against the stored rows
-// and stores it rounded to FP32, so every later product sees the same basis
+// Gram-Schmidt against the accepted vectors and normalisation.  The basis
+// solves run the FP64 FCG on both paths: P0 = K - om^2 M with a small om is a
+// nearly singular static operator whose FP32 curvature p'P0 p loses its sign
+// to rounding (the mixed recurrence breaks down).  The plain path keeps the
+// basis in FP64; the mixed path orthonormalises each row in FP64 against the
+// stored rows and stores it rounded to FP32, so every later product sees the
+// same basis
 static int sommg_basis(TopoLE *le) {
     cudaStream_t s = le->stream;
     const long long nd = le->ndof, nn = le->nn;
@@ -1923,12 +1861,11 @@ static int sommg_basis(TopoLE *le) {
     const bool b32 = le->basis32;
     const uint8_t *fixed = le->L[0].fixed;
     double *Ut = red_mat(le, RED_UT), *Pv = le->hM;
-    struct Fp64Solves {  // FP64 FCG for the plain path's basis solves, restored on every exit
+    struct Fp64Solves {  // FP64 FCG for the basis solves, restored on every exit
         TopoLE *le;
-        bool old;
-        Fp64Solves(TopoLE *l, bool on) : le(l), old(l->fp64_solves) { le->fp64_solves = on || old; }
-        ~Fp64Solves() { le->fp64_solves = old; }
-    } fp64(le, !b32);
+        explicit Fp64Solves(TopoLE *l) : le(l) { le->fp64_solves = true; }
+        ~Fp64Solves() { le->fp64_solves = false; }
+    } fp64(le);
     count_launch();
     k_mask_scale<<<ew_blocks(nn), EW, 0, s>>>(nn, fixed, le->rhs0, 1.0, Pv);  // VecPointwiseMult(P, P, N), :75
     for (int j = 0; j < kb; j++) {

@@ -77,8 +77,6 @@ class TopOpt:
     noise: float = 0.0  # initial design V0 + U(-noise, noise) from a generator seeded with seed
     seed: int = 0x7A11
     mass_precond_smooth: int = 0
-    tile_form: int = 0  # operator kernels: 0 bricks, 1 z-marching slabs
-    kron_form: int = 0  # Kronecker y/z passes: 0 staged lines, 1 register line segments
     # result files (TopOpt.cc:474-482 -outputDesign/-outputPhysics0/-outputPhysics1,
     # on by default in the reference, opt-in here) under ./workdir (-workdir)
     outputDesign: bool = False
@@ -134,8 +132,7 @@ class TopOpt:
             inner_tol=self.inner_tol, inner_maxit=self.inner_maxit, adaptive_kappa=self.adaptive_kappa,
             extrapolate=self.extrapolate, mass_precond=self.mass_precond,
             mass_precond_smooth=self.mass_precond_smooth, reduction=self.reduction, basis=self.basis,
-            omega0=self.omega0, load2_node=self.load2_node, load2_phase=self.load2_phase, out_dof=self.out_dof,
-            tile_form=self.tile_form, kron_form=self.kron_form)
+            omega0=self.omega0, load2_node=self.load2_node, load2_phase=self.load2_phase, out_dof=self.out_dof)
         self.filt = Filter(self.nelx, self.nely, self.nelz, self.filter, self.rmin, h=self.h, rtol=self.filter_rtol)
         # result files (main.cc:38-49): design fields per iteration, the physics
         # of the first iteration and of the final design

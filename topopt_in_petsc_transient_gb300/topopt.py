@@ -85,8 +85,7 @@ class LinearElasticity:
                  loadsignal=0, mixed=True, rtol=1e-10, maxit=500, smooth=3, cheb_ratio=30.0, use_graphs=True,
                  coarse_dense_max=None, coarse_smooth=None, sens_fp32=None, inner_tol=None, inner_maxit=None,
                  adaptive_kappa=None, extrapolate=None, mass_precond=None, mass_precond_share=None,
-                 mass_precond_smooth=None, load2_node=-1, load2_phase=0.0, out_dof=-1, tile_form=0,
-                 kron_form=0):
+                 mass_precond_smooth=None, load2_node=-1, load2_phase=0.0, out_dof=-1):
         L = _lib.load()
         p = LEParams()
         L.topo_le_default_params(C.byref(p), nelx, nely, nelz)
@@ -98,7 +97,6 @@ class LinearElasticity:
         p.dalpha, p.dbeta = dalpha, dbeta
         p.reduction, p.basis, p.omega0 = int(bool(reduction)), int(basis), float(omega0)
         p.load2_node, p.load2_phase, p.out_dof = int(load2_node), float(load2_phase), int(out_dof)
-        p.tile_form, p.kron_form = int(tile_form), int(kron_form)
         p.mixed, p.rtol, p.maxit, p.smooth = int(bool(mixed)), rtol, maxit, smooth
         p.cheb_ratio, p.use_graphs = cheb_ratio, int(bool(use_graphs))
         if coarse_dense_max is not None:
