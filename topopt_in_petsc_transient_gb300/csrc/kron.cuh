@@ -277,7 +277,9 @@ static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
         }
     }
     __syncthreads();
-    double red[2] = {0.0, 0.0};
+    // the FCG dot products: FP32 per thread (at most a few dozen terms), FP64
+    // across threads (GB300 runs FP64 at 1/64 of the FP32 rate)
+    float sr = 0.0f, sq = 0.0f;
     const int ngrp = (len + KRON_MP - 1) / KRON_MP;
     for (int t = threadIdx.x; t < ngrp * KW; t += KRON_THREADS) {
         const int grp = t / KW, w = t - grp * KW;
@@ -297,8 +299,8 @@ static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
                 const T z = m < T(0) ? rv : m * o[k];
                 out[q] = z;
                 if (DOT) {
-                    red[0] += (double)((float)z * (float)rv);
-                    red[1] += (double)((float)z * qt[sidx]);
+                    sr += (float)z * (float)rv;
+                    sq += (float)z * qt[sidx];
                 }
             } else {
                 out[q] = o[k];
@@ -306,7 +308,7 @@ static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
         }
     }
     if constexpr (DOT) {
-        double tot[2];
+        double red[2] = {(double)sr, (double)sq}, tot[2];
         if (grid_reduce<KRON_THREADS, 2>(red, kd.part, tot)) {
             SolveScalars *S = kd.S;
             S->rho = tot[0];

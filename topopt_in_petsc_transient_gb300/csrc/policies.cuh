@@ -195,7 +195,8 @@ struct PolPQ32 {
         r.f = fixed[n];
         return r;
     }
-    __device__ void epilogue(long long n, int, int, int, const float y[3], double red[1], const Pre &r) const {
+    using Red = float;  // p.q summed per thread in FP32 (about a dozen nodes), widened once
+    __device__ void epilogue(long long n, int, int, int, const float y[3], float red[1], const Pre &r) const {
         float *pout = (S->it & 1) ? pb[0] : pb[1];
         float s = 0.0f;
         for (int c = 0; c < 3; c++) {
@@ -205,7 +206,7 @@ struct PolPQ32 {
             q[3 * n + c] = qv;
             s += pv * qv;
         }
-        red[0] += (double)s;
+        red[0] += s;
     }
     __device__ void finish(const double t[1]) const {
         S->pq = t[0];
@@ -379,7 +380,8 @@ struct PolChebDot {
         r.f = fixed[n];
         return r;
     }
-    __device__ void epilogue(long long n, int, int, int, const float y[3], double red[2], const Pre &q) const {
+    using Red = float;  // the dot products summed per thread in FP32, widened once
+    __device__ void epilogue(long long n, int, int, int, const float y[3], float red[2], const Pre &q) const {
         const float c1 = (float)ctab[2 * k], c2 = (float)ctab[2 * k + 1];
         float s0 = 0.0f, s1 = 0.0f;
         for (int c = 0; c < 3; c++) {
@@ -391,8 +393,8 @@ struct PolChebDot {
             s0 += zv * q.b[c];
             s1 += zv * q.q[c];
         }
-        red[0] += (double)s0;
-        red[1] += (double)s1;
+        red[0] += s0;
+        red[1] += s1;
     }
     __device__ void finish(const double t[2]) const {
         S->rho = t[0];

@@ -14,6 +14,7 @@
 // assembled value (masking, fused vector updates, dot products) is supplied by
 // a policy type; see le.cu for the policies used by the solver.
 #pragma once
+#include <type_traits>
 #include "common.cuh"
 
 namespace topo {
@@ -70,16 +71,31 @@ template <class P>
 __device__ __forceinline__ NoPre pol_pre(const P &, long long, long) {
     return NoPre{};
 }
-template <class P, class T, class R>
-__device__ __forceinline__ auto pol_epi(const P &p, long long n, int i, int j, int k, const T y[3], double *red,
+template <class P, class T, class A, class R>
+__device__ __forceinline__ auto pol_epi(const P &p, long long n, int i, int j, int k, const T y[3], A *red,
                                         const R &pre, int) -> decltype(p.epilogue(n, i, j, k, y, red, pre)) {
     return p.epilogue(n, i, j, k, y, red, pre);
 }
-template <class P, class T, class R>
-__device__ __forceinline__ void pol_epi(const P &p, long long n, int i, int j, int k, const T y[3], double *red,
+template <class P, class T, class A, class R>
+__device__ __forceinline__ void pol_epi(const P &p, long long n, int i, int j, int k, const T y[3], A *red,
                                         const R &, long) {
     p.epilogue(n, i, j, k, y, red);
 }
+
+// per-thread accumulator type of a policy's reductions: `using Red = float;`
+// in an FP32 policy keeps the per-node sums on the FP32 pipe (GB300 runs FP64
+// at 1/64 of the FP32 rate); the thread's partials widen to FP64 once, for the
+// grid reduction
+template <class P, class = void>
+struct pol_red {
+    using type = double;
+};
+template <class P>
+struct pol_red<P, std::void_t<typename P::Red>> {
+    using type = typename P::Red;
+};
+template <class P>
+using pol_red_t = typename pol_red<P>::type;
 
 // staged input nodes of brick `tile` held by this thread (at most two)
 template <class T, class Pol>
@@ -119,7 +135,7 @@ constexpr bool tile_persistent() {
 template <class T, class Pol>
 __device__ __forceinline__ void tile_brick(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, T *sIn, T *sEl,
                                            int tile, int next, int ntx, int nty, T v[2][Pol::NIN][3],
-                                           double *red) {
+                                           pol_red_t<Pol> *red) {
     const int tid = threadIdx.x;
     const int i0 = (tile % ntx) * TILE, j0 = ((tile / ntx) % nty) * TILE, k0 = (tile / (ntx * nty)) * TILE;
     // ---- staged inputs (brick + halo, zero outside the domain) to shared memory ----
@@ -232,9 +248,9 @@ __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(c
     static_assert(TILE_STAGED <= 2 * TILE_THREADS, "staging assumes two passes");
     int ntx, nty;
     const int ntiles = tile_count(g, ntx, nty);
-    double red[Pol::NRED > 0 ? Pol::NRED : 1];
+    pol_red_t<Pol> red[Pol::NRED > 0 ? Pol::NRED : 1];
 #pragma unroll
-    for (int r = 0; r < (Pol::NRED > 0 ? Pol::NRED : 1); r++) red[r] = 0.0;
+    for (int r = 0; r < (Pol::NRED > 0 ? Pol::NRED : 1); r++) red[r] = 0;
     T v[2][Pol::NIN][3];
     if constexpr (tile_persistent<T>()) {
         if ((int)blockIdx.x < ntiles) tile_fetch<T>(pol, g, blockIdx.x, ntx, nty, v);
@@ -248,8 +264,10 @@ __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(c
         tile_brick<T>(g, C, pol, sIn, sEl, blockIdx.x, -1, ntx, nty, v, red);
     }
     if constexpr (Pol::NRED > 0) {
-        double tot[Pol::NRED];
-        if (grid_reduce<TILE_THREADS, Pol::NRED>(red, pol.part, tot)) pol.finish(tot);
+        double rd[Pol::NRED], tot[Pol::NRED];
+#pragma unroll
+        for (int r = 0; r < Pol::NRED; r++) rd[r] = (double)red[r];
+        if (grid_reduce<TILE_THREADS, Pol::NRED>(rd, pol.part, tot)) pol.finish(tot);
     }
 }
 
