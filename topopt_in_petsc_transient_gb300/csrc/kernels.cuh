@@ -451,6 +451,7 @@ static __global__ void k_mfcg_dot(long long ndof, const float *__restrict__ z, c
         S->gam = tot[1];
         S->beta = S->restart ? 0.0 : -tot[1] / S->pq;
         if (!isfinite(S->beta)) S->beta = 0.0;
+        S->beta32 = (float)S->beta;
         S->rescale = 0;
     }
 }

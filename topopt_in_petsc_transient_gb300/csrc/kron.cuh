@@ -315,6 +315,7 @@ static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
             S->gam = tot[1];
             S->beta = S->restart ? 0.0 : -tot[1] / S->pq;
             if (!isfinite(S->beta)) S->beta = 0.0;
+            S->beta32 = (float)S->beta;
             S->rescale = 0;
         }
     }

@@ -36,6 +36,7 @@ struct SolveScalars {
     // last FP64 residual), so FP32 never sees the absolute scale of the state
     double sigma, ndof;
     int rescale;
+    float beta32;     // beta of the FP32 recurrence in FP32 (read per staged node by PolPQ32)
 };
 
 // ---------------------------------------------------------------------------
@@ -176,7 +177,7 @@ struct PolPQ32 {
     SolveScalars *S;
     Partials<1> part;
     __device__ __forceinline__ void pnew(long long n, float v[3]) const {
-        const float beta = (float)S->beta;
+        const float beta = S->beta32;
         const float *pp = (S->it & 1) ? pb[1] : pb[0];  // a select: no local copy of pb
         for (int c = 0; c < 3; c++) v[c] = (beta == 0.0f) ? z[3 * n + c] : z[3 * n + c] + beta * pp[3 * n + c];
     }
@@ -401,6 +402,7 @@ struct PolChebDot {
         S->gam = t[1];
         S->beta = S->restart ? 0.0 : -t[1] / S->pq;
         if (!isfinite(S->beta)) S->beta = 0.0;
+        S->beta32 = (float)S->beta;
         S->rescale = 0;
     }
 };
