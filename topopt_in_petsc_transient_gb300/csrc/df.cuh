@@ -26,6 +26,35 @@ struct df {
     }
 };
 
+// Conversions between FP64 and FP32 on the integer pipes.  GB300 runs FP64
+// instructions, conversions included, at about 2 per clock and SM; a
+// streaming kernel that converts every value is then bound by them.  These
+// rebuild the bit patterns instead:
+//  * f64_to_f32: round to nearest (ties away from zero), values below 2^-126
+//    in magnitude flush to a signed zero (FP32 element math cannot use them
+//    anyway), infinities and NaNs map to their FP32 kinds; finite values
+//    above the FP32 range are not expected and become infinities;
+//  * f32_to_f64: exact for normal floats, subnormals flush to a signed zero.
+__device__ __forceinline__ float f64_to_f32(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    const unsigned sign = hi & 0x80000000u;
+    if (e < 897) return __uint_as_float(sign);
+    if (e > 1150) return __uint_as_float((e == 2047 && ((hi & 0xFFFFFu) | lo)) ? 0x7FC00000u : (sign | 0x7F800000u));
+    const unsigned mag = ((unsigned)(e - 896) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    return __uint_as_float(sign | (mag + ((lo >> 28) & 1u)));
+}
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xFFu;
+    const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    if (e == 255) return (double)f;
+    return __longlong_as_double(
+        (long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(b & 0x7FFFFFu) << 29)));
+}
+
 __host__ __device__ __forceinline__ double todbl(double v) { return v; }
 __host__ __device__ __forceinline__ double todbl(float v) { return (double)v; }
 __host__ __device__ __forceinline__ double todbl(df v) { return (double)v.hi + (double)v.lo; }

@@ -481,14 +481,14 @@ static __global__ void k_mfcg_update(long long ndof, double *__restrict__ x, flo
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            x[i + u * st] = xv[u] + ax * (double)pv[u];
+            x[i + u * st] = fma(ax, f32_to_f64(pv[u]), xv[u]);
             const float r = rv[u] - af * qv[u];
             r32[i + u * st] = r;
             s += r * r;
         }
     }
     for (; i < ndof; i += st) {
-        x[i] += ax * (double)p[i];
+        x[i] = fma(ax, f32_to_f64(p[i]), x[i]);
         float rv = r32[i] - af * q[i];
         r32[i] = rv;
         s += rv * rv;
@@ -570,7 +570,8 @@ __device__ __forceinline__ void fwd_prep(long long i, double u, double du, doubl
                                          double au, double av, double aa, double aa_prev, const FwdPrep &P) {
     P.KS[i] = P.ck[0] * u + P.ck[1] * du + P.ck[2] * ddu;
     P.BT[i] = P.cA[0] * au + P.cA[1] * av + P.cA[2] * aa;
-    double x = P.pred[0] * u + P.pred[1] * du, ax = P.pred[0] * au + P.pred[1] * av;
+    // the predictor's coefficient of u is 1 (fwd_prep_args): one FMA each
+    double x = fma(P.pred[1], du, u), ax = fma(P.pred[1], av, au);
     if (has_prev && P.use_pred2) {
         x += P.pred2[0] * ddu + P.pred2[1] * ddu_prev;
         ax += P.pred2[0] * aa + P.pred2[1] * aa_prev;
@@ -587,6 +588,11 @@ __device__ __forceinline__ void fwd_prep(long long i, double u, double du, doubl
 // A u = b - r (the solve's final, FP64-accurate residual; 0 when the solve
 // zeroed x), A du and A ddu by the same linear corrector; then the next
 // step's KS, X0 (into x), BT (into b) and AX (into r)
+// STD: Newmark beta = 1/4, gamma = 1/2 (a0 = -1, a1 = 0), where
+// a0 du + a1 ddu + a2 d is the single FMA a2 d - du with the same rounding:
+// GB300 issues about two FP64 FMAs per clock and SM, and FP64 work sets this
+// kernel's time
+template <bool STD>
 static __global__ void k_newmark_track(long long ndof, double *x, const StepCtx *st, const double *cp, double *Uh,
                                        double *DUh, double *DDUh, Newmark nm, double *b, double *r,
                                        const SolveScalars *S, double *AU, double *AV, double *AA, FwdPrep P) {
@@ -606,14 +612,14 @@ static __global__ void k_newmark_track(long long ndof, double *x, const StepCtx 
     const bool zx = S->zero_x != 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
         const double un = x[i], dU = un - u[i], dup = du[i], ddup = ddu[i];
-        const double dun = nm.a[0] * dup + nm.a[1] * ddup + nm.a[2] * dU;
+        const double dun = STD ? fma(nm.a[2], dU, -dup) : nm.a[0] * dup + nm.a[1] * ddup + nm.a[2] * dU;
         const double ddun = -nm.a[3] * dup - nm.a[4] * ddup + nm.a[5] * dU;
         uo[i] = un;
         duo[i] = dun;
         dduo[i] = ddun;
         const double aun = zx ? 0.0 : b[i] - r[i], d = aun - AU[i];
         const double av = AV[i], aa = AA[i];
-        const double avn = nm.a[0] * av + nm.a[1] * aa + nm.a[2] * d;
+        const double avn = STD ? fma(nm.a[2], d, -av) : nm.a[0] * av + nm.a[1] * aa + nm.a[2] * d;
         const double aan = -nm.a[3] * av - nm.a[4] * aa + nm.a[5] * d;
         AU[i] = aun;
         AV[i] = avn;
@@ -642,17 +648,14 @@ static __global__ void k_fwd_prep(long long ndof, const double *__restrict__ u, 
 // double-float (SolveStateBlock, LinearElasticity.cc:1317-1361).
 struct RhsLoad {
     const double *rhs0;
-    double load_scale;
-    int loadsignal;
+    const double *sig, *sig2;  // per-step load signals (k_load_table)
     long long load2_dof;
-    double load2_phase;
 };
 static __global__ void k_rhs_finish(long long ndof, const uint8_t *__restrict__ fixed, const double *__restrict__ y,
                                     RhsLoad L, const StepCtx *st, double *__restrict__ b, double *__restrict__ r,
                                     SolveScalars *S, cudaGraphConditionalHandle cond, int has_cond, Partials<2> part) {
     const int t = st->tsc * st->block + st->j + 1;
-    const double time = t * st->dt;
-    const double s = load_signal(L.loadsignal, time) * L.load_scale;
+    const double s = L.sig[t];
     double red[2] = {0.0, 0.0};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
         const long long n = i / 3;
@@ -662,7 +665,7 @@ static __global__ void k_rhs_finish(long long ndof, const uint8_t *__restrict__ 
             r[i] = 0.0;
             continue;
         }
-        const double f2 = (i == L.load2_dof) ? load2_signal(L.load2_phase, time) * L.load_scale : 0.0;
+        const double f2 = (i == L.load2_dof) ? L.sig2[t] : 0.0;
         const double bv = L.rhs0[i] * s + f2 + b[i] + y[i];
         const double rv = bv - r[i];
         b[i] = bv;

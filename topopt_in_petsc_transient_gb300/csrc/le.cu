@@ -375,6 +375,7 @@ struct TopoLE {
     // fine-level data
     double *N_host_dummy = nullptr;
     double *rhs0 = nullptr, *P = nullptr, *xPhys = nullptr;
+    double *sigtab = nullptr;  // [2][Ts]: Load(t)/(ny-1) and the second load's signal per step
     double *kf = nullptr, *dkf = nullptr, *mf = nullptr, *dmf = nullptr;
     df *kfx = nullptr, *mfx = nullptr;  // double-float copies for the mixed path
     ElemConst<df> Cx;
@@ -628,6 +629,10 @@ int le_alloc(TopoLE *le) {
         sc.dt = le->dt;
         CK(cudaMemcpy(le->st, &sc, sizeof(sc), cudaMemcpyHostToDevice));
     }
+    AG(le->sigtab, 2 * (size_t)le->Ts);
+    count_launch();
+    k_load_table<<<(le->Ts + 255) / 256, 256, 0, le->stream>>>(le->Ts, le->dt, p.loadsignal, 1.0 / (p.ny - 1),
+                                                                p.load2_phase, le->sigtab, le->sigtab + le->Ts);
     CK(cudaMemcpy(le->rhs0, rhs0.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(le->P, P.data(), sizeof(double) * ne, cudaMemcpyHostToDevice));
     count_launch();
@@ -1333,10 +1338,9 @@ static void fwd_rhs_t(TopoLE *le) {
     pr.DDUh = le->DDUh;
     pr.ndof = le->ndof;
     pr.rhs0 = le->rhs0;
-    pr.load_scale = 1.0 / (p.ny - 1);
-    pr.loadsignal = p.loadsignal;
+    pr.sig = le->sigtab;
+    pr.sig2 = le->sigtab + le->Ts;
     pr.load2_dof = p.load2_node >= 0 ? 3LL * p.load2_node + 2 : -1;
-    pr.load2_phase = p.load2_phase;
     // B1 u- + B2 du- + B3 ddu- = M (cM . s-) + K (cK . s-)  (LinearElasticity.cc:1028-1044)
     pr.cM[0] = a[5] + a[2] * p.dalpha;
     pr.cM[1] = a[3] - a[0] * p.dalpha;
@@ -1413,8 +1417,7 @@ static void product_t(TopoLE *le, const double *x, double *y, const double *P, d
 static void fwd_rhs_init(TopoLE *le, cudaGraphConditionalHandle cond, int has_cond) {
     const LEParams &p = le->p;
     product_t<df, true, false>(le, le->KSt, le->sq, nullptr, 1.0, 0.0);
-    RhsLoad L{le->rhs0, 1.0 / (p.ny - 1), p.loadsignal, p.load2_node >= 0 ? 3LL * p.load2_node + 2 : -1,
-              p.load2_phase};
+    RhsLoad L{le->rhs0, le->sigtab, le->sigtab + le->Ts, p.load2_node >= 0 ? 3LL * p.load2_node + 2 : -1};
     count_launch();
     k_rhs_finish<<<red_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, le->L[0].fixed, le->sq, L, le->st, le->sb,
                                                                le->sr, le->S, cond, has_cond, P2(le));
@@ -1475,10 +1478,14 @@ static int fwd_step(TopoLE *le, bool capturing) {
     Newmark nm;
     memcpy(nm.a, le->a, sizeof(nm.a));
     count_launch();
-    if (track)
-        k_newmark_track<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh, le->DUh,
-                                                           le->DDUh, nm, le->sb, le->sr, le->S, le->AUt, le->AVt,
-                                                           le->AAt, fwd_prep_args(le));
+    if (track && le->a[0] == -1.0 && le->a[1] == 0.0)
+        k_newmark_track<true><<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh, le->DUh,
+                                                                 le->DDUh, nm, le->sb, le->sr, le->S, le->AUt,
+                                                                 le->AVt, le->AAt, fwd_prep_args(le));
+    else if (track)
+        k_newmark_track<false><<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh,
+                                                                  le->DUh, le->DDUh, nm, le->sb, le->sr, le->S,
+                                                                  le->AUt, le->AVt, le->AAt, fwd_prep_args(le));
     else
         k_newmark<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh, le->DUh, le->DDUh,
                                                      nm);

@@ -482,6 +482,18 @@ __device__ __forceinline__ double load_signal(int which, double t) {
     return exp(-(s * s) / ((2 * c) * (2 * c))) * cos(4.0 * s) * cos(5.0 * s) * cos(6.0 * s) * cos(7.0 * s);
 }
 
+// Load(t) / (ny - 1) and the second load's signal at every time step t dt,
+// t = 0 .. Ts - 1, tabulated once per object by the same device functions: the
+// right-hand-side kernels read two doubles instead of evaluating exp/sin/cos
+// in FP64 per thread or per node (GB300 runs FP64 at 1/64 of the FP32 rate)
+static __global__ void k_load_table(int Ts, double dt, int which, double scale, double phase, double *sig,
+                                    double *sig2) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < Ts; t += gridDim.x * blockDim.x) {
+        sig[t] = load_signal(which, t * dt) * scale;
+        sig2[t] = load2_signal(phase, t * dt) * scale;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Newmark right-hand side of one forward step (plain FP64 path):
 //   b = N (f(t) + B1 u- + B2 du- + B3 ddu-),  B_i = N (cMi M + cKi K) N
@@ -499,10 +511,8 @@ struct PolRhsFwd {
     const double *Uh, *DUh, *DDUh;      // block history [tsc][ndof]
     long long ndof;
     const double *rhs0;                 // RHSLocation (LoadLocation, LinearElasticity.cc:616-675)
-    double load_scale;                  // 1/(ny-1)
-    int loadsignal;
+    const double *sig, *sig2;           // Load(t)/(ny-1) and the second load's signal per step (k_load_table)
     long long load2_dof;                // z DOF of the second point load (-1: none)
-    double load2_phase;
     double cK[3], cM[3];                // combination coefficients of (u-, du-, ddu-)
     double pred[3];                     // predictor coefficients (u-, du-, ddu-)
     double pred2[2];                    // with an older acceleration ddu--: (ddu-, ddu--)
@@ -546,11 +556,11 @@ struct PolRhsFwd {
         else if (use_pred2 && st->j == 1)
             ddu2 = cp + (long long)st->block * 3 * ndof + 2 * ndof;
         int t = st->tsc * st->block + st->j + 1;
-        double s = load_signal(loadsignal, t * st->dt) * load_scale;
+        const double s = sig[t];
         uint8_t f = fixed[n];
         for (int c = 0; c < 3; c++) {
             bool fx = (f >> c) & 1;
-            const double f2 = (3 * n + c == load2_dof) ? load2_signal(load2_phase, t * st->dt) * load_scale : 0.0;
+            const double f2 = (3 * n + c == load2_dof) ? sig2[t] : 0.0;
             b[3 * n + c] = fx ? 0.0 : (rhs0[3 * n + c] * s + f2 + todbl(y[c]));
             double xv = pred[0] * u[3 * n + c] + pred[1] * du[3 * n + c];
             if (ddu2)

@@ -267,6 +267,16 @@ __device__ __forceinline__ void sens_states(const SensArgs &A, long long ndof, c
     }
 }
 
+// c . (v0, v1, v2) evaluated as c0 v0 followed by FMAs, skipping the terms
+// whose coefficient is exactly zero (several are for Newmark beta = 1/4,
+// gamma = 1/2): the same value with fewer FP64 operations
+__device__ __forceinline__ double comb3(const double c[3], double v0, double v1, double v2) {
+    double s = c[0] * v0;
+    if (c[1] != 0.0) s = fma(c[1], v1, s);
+    if (c[2] != 0.0) s = fma(c[2], v2, s);
+    return s;
+}
+
 // wK = aK . (u, du, ddu) + bK . (u-, du-, ddu-) and wM likewise, once per DOF
 // (every node is shared by up to 8 elements, so this is 8x less FP64 work
 // than forming them inside the element loop)
@@ -276,22 +286,22 @@ static __global__ void k_sens_nodal(const SensArgs A) {
     sens_states(A, ndof, u, du, ddu, up, dup, ddup);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ndof; q += (long long)gridDim.x * blockDim.x) {
         double s0 = u[q], s1 = du[q], s2 = ddu[q];
-        double wk = A.aK[0] * s0 + A.aK[1] * s1 + A.aK[2] * s2;
-        double wm = A.aM[0] * s0 + A.aM[1] * s1 + A.aM[2] * s2;
+        double wk = comb3(A.aK, s0, s1, s2);
+        double wm = comb3(A.aM, s0, s1, s2);
         if (!A.t0mode) {
             double p0 = up[q], p1 = dup[q], p2 = ddup[q];
-            wk += A.bK[0] * p0 + A.bK[1] * p1 + A.bK[2] * p2;
-            wm += A.bM[0] * p0 + A.bM[1] * p1 + A.bM[2] * p2;
+            wk += comb3(A.bK, p0, p1, p2);
+            wm += comb3(A.bM, p0, p1, p2);
         }
         if (A.wKd) {
             A.wKd[q] = wk;
             A.wMd[q] = wm;
-        } else {
-            A.wKf[q] = (float)wk;
-            A.wMf[q] = (float)wm;
-            A.lamf[q] = (float)A.lam[q];
-            if (A.uf) A.uf[q] = (float)s0;
-            if (A.duf) A.duf[q] = (float)s1;
+        } else {  // FP32 element math: conversions on the integer pipes
+            A.wKf[q] = f64_to_f32(wk);
+            A.wMf[q] = f64_to_f32(wm);
+            A.lamf[q] = f64_to_f32(A.lam[q]);
+            if (A.uf) A.uf[q] = f64_to_f32(s0);
+            if (A.duf) A.duf[q] = f64_to_f32(s1);
         }
     }
 }
