@@ -16,13 +16,24 @@
 
 namespace topo {
 
+__device__ __forceinline__ float f64_to_f32(double v);
+__device__ __forceinline__ double f32_to_f64(float f);
+
 struct df {
     float hi, lo;
     __host__ __device__ df() : hi(0.0f), lo(0.0f) {}
     __host__ __device__ df(float h, float l) : hi(h), lo(l) {}
+    // hi = v rounded to FP32, lo = the rest rounded to FP32 (v - hi is exact
+    // in FP64).  On the device the conversions run on the integer pipes, one
+    // FP64 subtraction remains (magnitudes below 2^-126 flush to zero)
     __host__ __device__ df(double v) {
+#ifdef __CUDA_ARCH__
+        hi = f64_to_f32(v);
+        lo = f64_to_f32(v - f32_to_f64(hi));
+#else
         hi = (float)v;
         lo = (float)(v - (double)hi);
+#endif
     }
 };
 
@@ -57,7 +68,13 @@ __device__ __forceinline__ double f32_to_f64(float f) {
 
 __host__ __device__ __forceinline__ double todbl(double v) { return v; }
 __host__ __device__ __forceinline__ double todbl(float v) { return (double)v; }
-__host__ __device__ __forceinline__ double todbl(df v) { return (double)v.hi + (double)v.lo; }
+__host__ __device__ __forceinline__ double todbl(df v) {
+#ifdef __CUDA_ARCH__
+    return f32_to_f64(v.hi) + f32_to_f64(v.lo);
+#else
+    return (double)v.hi + (double)v.lo;
+#endif
+}
 
 #ifdef __CUDA_ARCH__
 #define DF_ADD(a, b) __fadd_rn((a), (b))
