@@ -369,11 +369,17 @@ def roofline(args, wl, opt):
     #     z pass reads its input, r, the masked scale and q and writes z
     #     (60 B/node)
     #   smoothing step: x, b, 1/diag, d read, d and x written (72 B/node), mask, kf/mf
+    #   double-float products: FP64 x staged, FP64 y written (48 B/node), the
+    #     replacement also reads the mask; double-float factors (8 B each)
     classes = [(1, "k_tile<float,PolPQ32> (FCG operator product q = A p with p = z + beta p_prev, FP32)",
                 49.0 * nn + 8.0 * nel),
                (2, "k_kron_pass<float> (one axis pass of the Kronecker mass inverse, 17-tap stencil, FP32)",
                 (36.0 + 24.0 + 60.0) / 3.0 * nn),
-               (0, "k_tile<float,PolCheb> (FP32 Chebyshev-Jacobi smoothing step)", 73.0 * nn + 8.0 * nel)]
+               (0, "k_tile<float,PolCheb> (FP32 Chebyshev-Jacobi smoothing step)", 73.0 * nn + 8.0 * nel),
+               (3, "k_tile<df,PolReplaceProduct> (FP64-accurate A x of a residual replacement, double-float; "
+                   "launches without a due replacement exit at once and are averaged in)", 49.0 * nn + 16.0 * nel),
+               (4, "k_tile<df,PolProduct> (double-float K or A products of right-hand sides, anchors and adjoint "
+                   "steps)", 48.0 * nn + 8.0 * nel)]
     kern = []
     for cls, name, nbytes in classes:
         _lib.check(L.topo_le_kernel_timing(probe.physics._h, cls, 1, None, None), "kernel_timing")

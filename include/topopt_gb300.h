@@ -202,6 +202,8 @@ int topo_le_time_apply(topo_le *le, int precision, int warmup, int reps, double 
 #define TOPO_KT_PQ32 1    /* FP32 FCG operator product q = A p, p.q (tile)    */
 #define TOPO_KT_KRON 2    /* one stencil pass of the Kronecker mass inverse   */
 #define TOPO_KT_REPLACE 3 /* FP64-accurate residual replacement (tile)        */
+#define TOPO_KT_DFPROD 4  /* double-float operator products outside the Krylov
+                             loop: right-hand-side, anchor and adjoint products */
 int topo_le_kernel_timing(topo_le *le, int kclass, int enable, double *ms_total, long long *launches);
 /* SOMMG reduced system of the current design (the public members QQ, Kr,
  * Mr, Pr of SOMMG, SOMMG.h:21-22): Q (basis x 3*nn, row b = basis vector b),

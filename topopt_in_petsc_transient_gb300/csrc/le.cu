@@ -224,7 +224,8 @@ struct Arena {
 // events on its stream.  Launches recorded into a CUDA graph are not timed.
 // Classes: TOPO_KT_SMOOTH (PolCheb / PolChebDot in FP32), TOPO_KT_PQ32,
 // TOPO_KT_KRON (each Kronecker stencil pass), TOPO_KT_REPLACE (the residual
-// replacement pass, FP64-accurate).
+// replacement pass, FP64-accurate), TOPO_KT_DFPROD (double-float products of
+// the right-hand sides, anchors and adjoint steps).
 struct LaunchTimer {
     int cls = -1;
     long long nn = -1;
@@ -257,17 +258,19 @@ constexpr int tile_class() {
     return (std::is_same<Pol, PolCheb<float>>::value || std::is_same<Pol, PolChebDot>::value) ? TOPO_KT_SMOOTH
            : std::is_same<Pol, PolPQ32>::value                                                 ? TOPO_KT_PQ32
            : std::is_same<Pol, PolReplaceProduct<T>>::value                                    ? TOPO_KT_REPLACE
+           : (std::is_same<T, df>::value && std::is_same<Pol, PolProduct<df, Pol::HAS_K, Pol::HAS_M>>::value)
+               ? TOPO_KT_DFPROD
                                                                                                : -1;
 }
 
-// FP32 tile kernels are persistent: as many CTAs as are resident on the device
-// at once (occupancy of this instantiation x SM count), capped by the brick
-// count; the others launch one CTA per brick
+// FP32 tile kernels and kernels staged by asynchronous copies are persistent: as many
+// CTAs as are resident on the device at once (occupancy of this instantiation
+// x SM count), capped by the brick count; the others launch one CTA per brick
 template <class T, class Pol>
 static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol, cudaStream_t s) {
     static int resident_dev[MAX_DEVICES] = {};
     int &resident = resident_dev[device_slot()];
-    const size_t sm = tile_smem_bytes<T, Pol>();
+    const size_t sm = TileSmem<T, Pol>::bytes;
     if (!resident) {
         cudaFuncSetAttribute(k_tile<T, Pol>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         int dev = 0, nsm = 0, per_sm = 0;
@@ -280,7 +283,7 @@ static void launch_tile(const GridDesc &g, const ElemConst<T> &C, const Pol &pol
     const int ntiles = tile_count(g, ntx, nty);
     const bool timed = tile_class<T, Pol>() >= 0 && timer_begin(tile_class<T, Pol>(), g.nn(), s);
     count_launch();
-    const int grid = tile_persistent<T>() ? std::min(ntiles, resident) : ntiles;
+    const int grid = (tile_persistent<T>() || tile_async<T, Pol>()) ? std::min(ntiles, resident) : ntiles;
     k_tile<T, Pol><<<(unsigned)grid, TILE_THREADS, sm, s>>>(g, C, pol);
     timer_end(timed, s);
 }
@@ -2604,7 +2607,7 @@ int le_time_apply(TopoLE *le, int precision, int warmup, int reps, double *ms) {
 int le_kernel_timing(TopoLE *le, int kclass, int enable, double *ms_total, long long *launches) {
     static LaunchTimer timer;
     if (enable) {
-        if (kclass < TOPO_KT_SMOOTH || kclass > TOPO_KT_REPLACE) {
+        if (kclass < TOPO_KT_SMOOTH || kclass > TOPO_KT_DFPROD) {
             set_error("unknown kernel class " + std::to_string(kclass));
             return TOPO_ERR_ARG;
         }

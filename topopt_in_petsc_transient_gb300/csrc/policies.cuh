@@ -242,6 +242,15 @@ struct PolReplaceProduct {
         v[0][2] = T(x[3 * n + 2]);
         mask3(fixed[n], v[0]);
     }
+    // asynchronous staging (tile.cuh): x and the clamp mask
+    using Src = double;
+    static constexpr int NSRC = 1;
+    static constexpr bool MASK = true;
+    __device__ const double *src(int) const { return x; }
+    __device__ void xform(const double raw[][3], uint8_t f, T v[1][3]) const {
+        for (int c = 0; c < 3; c++) v[0][c] = T(raw[0][c]);
+        mask3(f, v[0]);
+    }
     __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
     __device__ void epilogue(long long n, int, int, int, const T yv[3], double *) const {
         y[3 * n] = todbl(yv[0]);
@@ -447,6 +456,14 @@ struct PolProduct {
         v[0][0] = T(x[3 * n]);
         v[0][1] = T(x[3 * n + 1]);
         v[0][2] = T(x[3 * n + 2]);
+    }
+    // asynchronous staging (tile.cuh): x, no mask
+    using Src = double;
+    static constexpr int NSRC = 1;
+    static constexpr bool MASK = false;
+    __device__ const double *src(int) const { return x; }
+    __device__ void xform(const double raw[][3], uint8_t, T v[1][3]) const {
+        for (int c = 0; c < 3; c++) v[0][c] = T(raw[0][c]);
     }
     __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
     __device__ void epilogue(long long n, int, int, int, const T yv[3], double *) const {
