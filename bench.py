@@ -267,6 +267,8 @@ def run_gb300(args):
     value = replica_value(args.steps, ws, t_total)
     iters_per_solve = ((le_stats1["cg_iterations"] - le_stats0["cg_iterations"]) /
                        max(1, le_stats1["solves"] - le_stats0["solves"]))
+    replacements_per_solve = ((le_stats1["replacements"] - le_stats0["replacements"]) /
+                              max(1, le_stats1["solves"] - le_stats0["solves"]))
 
     # ---- plain FP64 path: the same design iterations (after the same
     # number of warm-up iterations), and iteration 1's objective and
@@ -330,6 +332,7 @@ def run_gb300(args):
                             * 8 / 1e9),
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "objective": fxs[-1] if fxs else None, "seconds": spread(times), "krylov_iters_per_solve": iters_per_solve,
+        "fp64_replacements_per_solve": replacements_per_solve,
         "dof_updates_per_s": 2.0 * 3 * (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1) * args.nsteps
                              * value / ws,
         "plain_fp64": plain, "accuracy_vs_oracle": acc, "fd_check": fd, "e2e": e2e, "roofline": roof,

@@ -114,6 +114,8 @@ typedef struct topo_le_stats {
     int step_precond;         /* preconditioner of the current design's Newmark
                                  step solves: 0 multigrid V-cycle, 1 Kronecker
                                  mass preconditioner, -1 before the first design */
+    long long replacements;   /* FP64-accurate residual replacements of the
+                                 mixed-precision solves since creation */
 } topo_le_stats;
 
 /* fills p with the reference defaults for a cantilever of nelx x nely x nelz

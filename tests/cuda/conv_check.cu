@@ -1,9 +1,12 @@
 // conv_check.cu -- the integer-pipe conversions of df.cuh (f64_to_f32,
-// f32_to_f64) against the hardware conversions on random and edge values.
-// Prints "conversions OK" and exits 0 when every value agrees as specified:
-// f64_to_f32 equals round-to-nearest except on exact ties (rounded away from
-// zero) and below 2^-126 (signed zero); f32_to_f64 is exact for normal floats
-// and flushes subnormals to a signed zero.
+// f32_to_f64, f64_to_df) against the hardware conversions on random and edge
+// values.  Prints "conversions OK" and exits 0 when every value agrees as
+// specified: f64_to_f32 equals round-to-nearest except on exact ties (rounded
+// away from zero) and below 2^-126 (signed zero); f32_to_f64 is exact for
+// normal floats and flushes subnormals to a signed zero; f64_to_df gives the
+// hi of f64_to_f32 and lo = v - hi (exact in FP64) rounded to nearest FP32,
+// zero below 2^-126; scaled_f32 is within 2^-22 of sigma v (or zero below
+// 2^-125).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -37,6 +40,30 @@ __global__ void k_check(int n, const double *d, const float *f, unsigned *bad) {
         else
             ok2 = __double_as_longlong(w) == __double_as_longlong((double)x);
         if (!ok2) atomicAdd(&bad[1], 1u);
+        const df sp = f64_to_df(v);
+        bool ok3 = __float_as_uint(sp.hi) == __float_as_uint(got);
+        if (ok3 && !tiny && isfinite(v) && isfinite(sp.hi)) {
+            const double r = v - (double)sp.hi;
+            const float lref = fabs(r) < 1.1754943508222875e-38 ? 0.0f : __double2float_rn(r);
+            ok3 = (sp.lo == 0.0f && lref == 0.0f) || __float_as_uint(sp.lo) == __float_as_uint(lref);
+        } else if (ok3) {
+            ok3 = sp.lo == 0.0f;
+        }
+        if (!ok3) atomicAdd(&bad[2], 1u);
+        // scaled_f32: sigma v rounded to FP32 with two roundings (relative
+        // error below 2^-22); results below 2^-125 may flush to zero
+        if (isfinite(v)) {
+            const double sg = ldexp(1.0 + 0.5 * fabs(__sinf((float)i)), (int)(i % 81) - 40);
+            const double pr = sg * v;
+            const float sf = scaled_f32(v, scale_split(sg));
+            bool ok4;
+            if (fabs(pr) > 3.0e38)
+                ok4 = true;  // outside the FP32 range: not used
+            else
+                ok4 = fabs((double)sf - pr) <= ldexp(fabs(pr), -22) ||
+                      (fabs(pr) < 2.3509887016445750e-38 && sf == 0.0f);
+            if (!ok4) atomicAdd(&bad[3], 1u);
+        }
     }
 }
 
@@ -77,18 +104,19 @@ int main() {
     unsigned *bad;
     cudaMalloc(&d, sizeof(double) * n);
     cudaMalloc(&f, sizeof(float) * n);
-    cudaMalloc(&bad, 2 * sizeof(unsigned));
+    cudaMalloc(&bad, 4 * sizeof(unsigned));
     cudaMemcpy(d, hd, sizeof(double) * n, cudaMemcpyHostToDevice);
     cudaMemcpy(f, hf, sizeof(float) * n, cudaMemcpyHostToDevice);
-    cudaMemset(bad, 0, 2 * sizeof(unsigned));
+    cudaMemset(bad, 0, 4 * sizeof(unsigned));
     k_check<<<512, 256>>>(n, d, f, bad);
-    unsigned hb[2] = {1, 1};
+    unsigned hb[4] = {1, 1, 1, 1};
     cudaError_t e = cudaMemcpy(hb, bad, sizeof(hb), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
         printf("CUDA error %s\n", cudaGetErrorString(e));
         return 2;
     }
-    printf("f64_to_f32 mismatches %u, f32_to_f64 mismatches %u\n", hb[0], hb[1]);
-    if (hb[0] == 0 && hb[1] == 0) printf("conversions OK\n");
-    return (hb[0] || hb[1]) ? 1 : 0;
+    printf("f64_to_f32 mismatches %u, f32_to_f64 mismatches %u, f64_to_df mismatches %u, scaled_f32 mismatches %u\n",
+           hb[0], hb[1], hb[2], hb[3]);
+    if (hb[0] == 0 && hb[1] == 0 && hb[2] == 0 && hb[3] == 0) printf("conversions OK\n");
+    return (hb[0] || hb[1] || hb[2] || hb[3]) ? 1 : 0;
 }

@@ -1,7 +1,8 @@
 """The integer-pipe FP64/FP32 conversions of csrc/df.cuh (used by the
-streaming kernels, where FP64 conversions on GB300's FP64 pipe set the time)
-against the hardware conversions: tests/cuda/conv_check.cu, built with nvcc
-for sm_103a and run on the GPU."""
+streaming kernels, where FP64 conversions on GB300's FP64 pipe set the time,
+and by the double-float staging of the element passes) against the hardware
+conversions: tests/cuda/conv_check.cu, built with nvcc for sm_103a and run on
+the GPU."""
 import os
 import shutil
 import subprocess

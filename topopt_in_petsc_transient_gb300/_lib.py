@@ -48,7 +48,7 @@ class LEParams(C.Structure):
 class LEStats(C.Structure):
     _fields_ = [("cg_iterations", C.c_longlong), ("solves", C.c_longlong), ("device_bytes", C.c_double),
                 ("last_fx", C.c_double), ("graph_body_launches", C.c_longlong), ("mg_solves", C.c_longlong),
-                ("step_precond", C.c_int)]
+                ("step_precond", C.c_int), ("replacements", C.c_longlong)]
 
 
 EXPORTS = [

@@ -261,14 +261,35 @@ __device__ __forceinline__ void block_reduce(double v[NV], double *smem /* [NV][
     }
 }
 
-// Called by every thread of every CTA (1D-linearised block id).  Returns true
-// in exactly one thread (thread 0 of the last CTA to finish); on that thread
-// `tot` holds the grid sums.
+// FP32 partials: the warp-level tree in FP32 (GB300 runs FP64 at 1/64 of the
+// FP32 rate, and an FP64 tree costs every thread five FP64 additions per
+// value), then the warp sums widened once and added in FP64 by thread 0
 template <int NT, int NV>
-__device__ __forceinline__ bool grid_reduce(double v[NV], const Partials<NV> &P, double tot[NV]) {
-    __shared__ double sred[NV * (NT / 32)];
+__device__ __forceinline__ void block_reduce_f32(const float vf[NV], double v[NV], double *smem /* [NV][NT/32] */) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        float x = vf[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) smem[i * (NT / 32) + wid] = (double)x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+            double s = 0.0;
+            for (int w = 0; w < NT / 32; w++) s += smem[i * (NT / 32) + w];
+            v[i] = s;
+        }
+    }
+}
+
+// the grid stage of grid_reduce: v holds the CTA sums in thread 0
+template <int NT, int NV>
+__device__ __forceinline__ bool grid_reduce_blocks(double v[NV], const Partials<NV> &P, double tot[NV],
+                                                   double *sred) {
     __shared__ bool last;
-    block_reduce<NT, NV>(v, sred);
     const unsigned int nblk = gridDim.x * gridDim.y * gridDim.z;
     const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
     if (threadIdx.x == 0) {
@@ -298,6 +319,24 @@ __device__ __forceinline__ bool grid_reduce(double v[NV], const Partials<NV> &P,
         return true;
     }
     return false;
+}
+
+// Called by every thread of every CTA (1D-linearised block id).  Returns true
+// in exactly one thread (thread 0 of the last CTA to finish); on that thread
+// `tot` holds the grid sums.
+template <int NT, int NV>
+__device__ __forceinline__ bool grid_reduce(double v[NV], const Partials<NV> &P, double tot[NV]) {
+    __shared__ double sred[NV * (NT / 32)];
+    block_reduce<NT, NV>(v, sred);
+    return grid_reduce_blocks<NT, NV>(v, P, tot, sred);
+}
+// the same from FP32 per-thread partials (block_reduce_f32)
+template <int NT, int NV>
+__device__ __forceinline__ bool grid_reduce(const float vf[NV], const Partials<NV> &P, double tot[NV]) {
+    __shared__ double sred[NV * (NT / 32)];
+    double v[NV];
+    block_reduce_f32<NT, NV>(vf, v, sred);
+    return grid_reduce_blocks<NT, NV>(v, P, tot, sred);
 }
 
 }  // namespace topo

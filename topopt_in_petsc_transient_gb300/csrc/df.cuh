@@ -13,28 +13,22 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
+#include <string.h>
 
 namespace topo {
 
 __device__ __forceinline__ float f64_to_f32(double v);
 __device__ __forceinline__ double f32_to_f64(float f);
+struct df;
+__host__ __device__ __forceinline__ df f64_to_df(double v);
 
 struct df {
     float hi, lo;
     __host__ __device__ df() : hi(0.0f), lo(0.0f) {}
     __host__ __device__ df(float h, float l) : hi(h), lo(l) {}
-    // hi = v rounded to FP32, lo = the rest rounded to FP32 (v - hi is exact
-    // in FP64).  On the device the conversions run on the integer pipes, one
-    // FP64 subtraction remains (magnitudes below 2^-126 flush to zero)
-    __host__ __device__ df(double v) {
-#ifdef __CUDA_ARCH__
-        hi = f64_to_f32(v);
-        lo = f64_to_f32(v - f32_to_f64(hi));
-#else
-        hi = (float)v;
-        lo = (float)(v - (double)hi);
-#endif
-    }
+    // hi = v rounded to FP32, lo = the rest rounded to FP32; no FP64
+    // instruction (f64_to_df)
+    __host__ __device__ df(double v);
 };
 
 // Conversions between FP64 and FP32 on the integer pipes.  GB300 runs FP64
@@ -64,6 +58,77 @@ __device__ __forceinline__ double f32_to_f64(float f) {
     if (e == 255) return (double)f;
     return __longlong_as_double(
         (long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(b & 0x7FFFFFu) << 29)));
+}
+
+// FP64 -> double-float split from the bit pattern: hi = v rounded to FP32
+// (nearest, ties away, as f64_to_f32); v - hi is exactly R ulp(v) with R a
+// 29-bit signed integer (the low mantissa bits, minus 2^29 when hi rounded
+// up), so lo = R rounded to FP32 by one int-to-float conversion, scaled by
+// ulp(v) in its exponent field.  No FP64 instruction.  |v| below 2^-126
+// flushes to zero, as does a lo below 2^-126; finite values above the FP32
+// range are not expected and give an infinite hi.
+__host__ __device__ __forceinline__ df f64_to_df(double v) {
+    unsigned long long b;
+    memcpy(&b, &v, sizeof b);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    const unsigned sign = hi & 0x80000000u;
+    unsigned hb, lb = 0u;
+    if (e < 897) {
+        hb = sign;
+    } else if (e > 1150) {
+        hb = (e == 2047 && ((hi & 0xFFFFFu) | lo)) ? 0x7FC00000u : (sign | 0x7F800000u);
+    } else {
+        const unsigned mag = ((unsigned)(e - 896) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+        const unsigned rnd = (lo >> 28) & 1u;
+        hb = sign | (mag + rnd);
+        const int R = (int)(lo & 0x1FFFFFFFu) - (int)(rnd << 29);
+        if (R != 0) {
+#ifdef __CUDA_ARCH__
+            const float fr = __int2float_rn(R);
+#else
+            const float fr = (float)R;
+#endif
+            unsigned fb;
+            memcpy(&fb, &fr, sizeof fb);
+            const int k = e - 1075;  // ulp(v) = 2^k
+            if ((int)((fb >> 23) & 0xFFu) + k >= 1) lb = (fb + (unsigned)(k * (1 << 23))) ^ sign;
+        }
+    }
+    df r;
+    memcpy(&r.hi, &hb, sizeof hb);
+    memcpy(&r.lo, &lb, sizeof lb);
+    return r;
+}
+__host__ __device__ __forceinline__ df::df(double v) { *this = f64_to_df(v); }
+
+// FP32 copies of FP64 values scaled by a positive factor s (the residual
+// rescaling r32 = sigma r of the mixed FCG) without FP64 instructions: s is
+// split once into 2^k m with m in [1, 2); each value gets k added to its FP64
+// exponent field on the integer pipes, is rounded to FP32 (f64_to_f32) and
+// multiplied by m in FP32 (two roundings instead of one).  Zero stays zero;
+// v 2^k below 2^-126 flushes to zero, as in f64_to_f32, so results below
+// 2^-125 may flush (the rescaling brings residuals to unit mean square).
+struct ScaleF64 {
+    int k;
+    float m;
+};
+__device__ __forceinline__ ScaleF64 scale_split(double s) {
+    const long long b = __double_as_longlong(s);
+    const int e = (int)((b >> 52) & 0x7FF);
+    ScaleF64 r;
+    r.k = e - 1023;
+    r.m = f64_to_f32(__longlong_as_double((b & 0x800FFFFFFFFFFFFFll) | (1023ll << 52)));
+    return r;
+}
+__device__ __forceinline__ float scaled_f32(double v, ScaleF64 s) {
+    long long b = __double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF);
+    const int en = e + s.k;
+    if (e == 0 || en <= 0) return __uint_as_float((unsigned)((unsigned long long)b >> 32) & 0x80000000u);
+    if (en >= 2047) b = (b & (long long)0x8000000000000000ull) | (0x7FFll << 52);  // infinity
+    else b += (long long)s.k * (1ll << 52);
+    return f64_to_f32(__longlong_as_double(b)) * s.m;
 }
 
 __host__ __device__ __forceinline__ double todbl(double v) { return v; }

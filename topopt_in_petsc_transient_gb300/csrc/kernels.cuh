@@ -209,11 +209,11 @@ static __global__ void k_cheb0_rescale(long long ndof, const double *__restrict_
                                        const SolveScalars *S) {
     const float c2 = (float)coef[1];
     const bool rs = S->rescale != 0;
-    const double sg = S->sigma;
+    const ScaleF64 sg = scale_split(S->sigma);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
         float bv;
         if (rs) {
-            bv = (float)(sg * r[i]);
+            bv = scaled_f32(r[i], sg);
             b[i] = bv;
         } else {
             bv = b[i];
@@ -431,9 +431,9 @@ static __global__ void k_fcg_update(long long ndof, double *x, double *r, float 
 // r32 = sigma * r after an FP64 residual (init or replacement)
 static __global__ void k_mfcg_scale(long long ndof, const double *__restrict__ r, float *r32, const SolveScalars *S) {
     if (!S->rescale) return;
-    double sg = S->sigma;
+    const ScaleF64 sg = scale_split(S->sigma);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)
-        r32[i] = (float)(sg * r[i]);
+        r32[i] = scaled_f32(r[i], sg);
 }
 
 static __global__ void k_mfcg_dot(long long ndof, const float *__restrict__ z, const float *__restrict__ r32,
@@ -444,7 +444,7 @@ static __global__ void k_mfcg_dot(long long ndof, const float *__restrict__ z, c
         s0 += zi * r32[i];
         s1 += zi * q32[i];
     }
-    double v[2] = {(double)s0, (double)s1};
+    const float v[2] = {s0, s1};
     double tot[2];
     if (grid_reduce<EW, 2>(v, part, tot)) {
         S->rho = tot[0];
@@ -462,9 +462,10 @@ static __global__ void k_mfcg_update(long long ndof, double *__restrict__ x, flo
                                      const float *pb0, const float *pb1, const float *__restrict__ q, SolveScalars *S,
                                      Partials<1> part) {
     const float *__restrict__ p = ((S->it + 1) & 1) ? pb1 : pb0;
-    double alpha = S->alpha;
-    float af = (float)alpha;
-    double ax = alpha / S->sigma;  // correction in unscaled units
+    // alpha in FP32 and in unscaled units, formed once by PolPQ32 (an FP64
+    // division per thread would cost more FP64-pipe time than the x update)
+    const float af = S->alpha32;
+    const double ax = S->alpha_x;
     float s = 0.0f;
     // four grid strides per trip: all loads of a trip are issued before its stores
     const long long st = (long long)gridDim.x * blockDim.x;
@@ -493,7 +494,7 @@ static __global__ void k_mfcg_update(long long ndof, double *__restrict__ x, flo
         r32[i] = rv;
         s += rv * rv;
     }
-    double v[1] = {(double)s};
+    const float v[1] = {s};
     double tot[1];
     if (grid_reduce<EW, 1>(v, part, tot)) {
         S->it += 1;
@@ -523,6 +524,7 @@ static __global__ void k_fcg_zero_x(long long ndof, double *x, const SolveScalar
 // ---------------------------------------------------------------------------
 struct Newmark {
     double a[6];
+    df da[6];  // the same as double-float pairs (k_newmark_track)
 };
 
 static __global__ void k_newmark(long long ndof, const double *__restrict__ x, const StepCtx *st, const double *cp, double *Uh,
@@ -565,33 +567,41 @@ struct FwdPrep {
     double pred2[2];       // with ddu--: u + pred1 du + pred2[0] ddu + pred2[1] ddu--
     int use_pred2;
     double *KS, *X0, *BT, *AX;
+    // the coefficients as double-float pairs, split on the host
+    df dck[3], dcA[3], dpred[3], dpred2[2];
 };
-__device__ __forceinline__ void fwd_prep(long long i, double u, double du, double ddu, double ddu_prev, bool has_prev,
-                                         double au, double av, double aa, double aa_prev, const FwdPrep &P) {
-    P.KS[i] = P.ck[0] * u + P.ck[1] * du + P.ck[2] * ddu;
-    P.BT[i] = P.cA[0] * au + P.cA[1] * av + P.cA[2] * aa;
-    // the predictor's coefficient of u is 1 (fwd_prep_args): one FMA each
-    double x = fma(P.pred[1], du, u), ax = fma(P.pred[1], av, au);
+// in double-float arithmetic (FP32 pipes): GB300 runs FP64 at about two FMAs
+// per clock and SM, and the FP64 form of these combinations set the time of
+// the kernels that call this; one FP64 addition per output joins hi + lo
+__device__ __forceinline__ void fwd_prep(long long i, df u, df du, df ddu, df ddu_prev, bool has_prev, df au, df av,
+                                         df aa, df aa_prev, const FwdPrep &P) {
+    P.KS[i] = todbl(P.dck[0] * u + P.dck[1] * du + P.dck[2] * ddu);
+    P.BT[i] = todbl(P.dcA[0] * au + P.dcA[1] * av + P.dcA[2] * aa);
+    // the predictor's coefficient of u is 1 (fwd_prep_args)
+    df x = P.dpred[1] * du + u, ax = P.dpred[1] * av + au;
     if (has_prev && P.use_pred2) {
-        x += P.pred2[0] * ddu + P.pred2[1] * ddu_prev;
-        ax += P.pred2[0] * aa + P.pred2[1] * aa_prev;
+        x += P.dpred2[0] * ddu + P.dpred2[1] * ddu_prev;
+        ax += P.dpred2[0] * aa + P.dpred2[1] * aa_prev;
     } else {
-        x += P.pred[2] * ddu;
-        ax += P.pred[2] * aa;
+        x += P.dpred[2] * ddu;
+        ax += P.dpred[2] * aa;
     }
-    P.X0[i] = x;
-    P.AX[i] = ax;
+    P.X0[i] = todbl(x);
+    P.AX[i] = todbl(ax);
 }
 
 // after a forward solve (Newmark corrector, LinearElasticity.cc:1363-1375):
 // the new state into history slot j; the tracked products of the new state,
 // A u = b - r (the solve's final, FP64-accurate residual; 0 when the solve
 // zeroed x), A du and A ddu by the same linear corrector; then the next
-// step's KS, X0 (into x), BT (into b) and AX (into r)
-// STD: Newmark beta = 1/4, gamma = 1/2 (a0 = -1, a1 = 0), where
-// a0 du + a1 ddu + a2 d is the single FMA a2 d - du with the same rounding:
-// GB300 issues about two FP64 FMAs per clock and SM, and FP64 work sets this
-// kernel's time
+// step's KS, X0 (into x), BT (into b) and AX (into r).
+// The differences that cancel (u+ - u, b - r, A u+ - A u) are formed in FP64;
+// the combinations run in double-float arithmetic on the FP32 pipes, with the
+// FP64 inputs split on the integer pipes (f64_to_df) and one FP64 addition
+// per output: GB300 issues about two FP64 FMAs per clock and SM, and the
+// all-FP64 form (23 FP64 operations per DOF) was bound by that rate at
+// about twice its DRAM time.
+// STD: Newmark beta = 1/4, gamma = 1/2 (a0 = -1, a1 = 0).
 template <bool STD>
 static __global__ void k_newmark_track(long long ndof, double *x, const StepCtx *st, const double *cp, double *Uh,
                                        double *DUh, double *DDUh, Newmark nm, double *b, double *r,
@@ -611,19 +621,20 @@ static __global__ void k_newmark_track(long long ndof, double *x, const StepCtx 
     double *uo = Uh + (long long)j * ndof, *duo = DUh + (long long)j * ndof, *dduo = DDUh + (long long)j * ndof;
     const bool zx = S->zero_x != 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
-        const double un = x[i], dU = un - u[i], dup = du[i], ddup = ddu[i];
-        const double dun = STD ? fma(nm.a[2], dU, -dup) : nm.a[0] * dup + nm.a[1] * ddup + nm.a[2] * dU;
-        const double ddun = -nm.a[3] * dup - nm.a[4] * ddup + nm.a[5] * dU;
-        uo[i] = un;
-        duo[i] = dun;
-        dduo[i] = ddun;
-        const double aun = zx ? 0.0 : b[i] - r[i], d = aun - AU[i];
-        const double av = AV[i], aa = AA[i];
-        const double avn = STD ? fma(nm.a[2], d, -av) : nm.a[0] * av + nm.a[1] * aa + nm.a[2] * d;
-        const double aan = -nm.a[3] * av - nm.a[4] * aa + nm.a[5] * d;
-        AU[i] = aun;
-        AV[i] = avn;
-        AA[i] = aan;
+        const double un64 = x[i];
+        const df un(un64), dU(un64 - u[i]), dup(du[i]), ddup(ddu[i]);
+        const df dun = STD ? nm.da[2] * dU - dup : nm.da[0] * dup + nm.da[1] * ddup + nm.da[2] * dU;
+        const df ddun = nm.da[5] * dU - nm.da[3] * dup - nm.da[4] * ddup;
+        uo[i] = un64;
+        duo[i] = todbl(dun);
+        dduo[i] = todbl(ddun);
+        const double aun64 = zx ? 0.0 : b[i] - r[i];
+        const df aun(aun64), d(aun64 - AU[i]), av(AV[i]), aa(AA[i]);
+        const df avn = STD ? nm.da[2] * d - av : nm.da[0] * av + nm.da[1] * aa + nm.da[2] * d;
+        const df aan = nm.da[5] * d - nm.da[3] * av - nm.da[4] * aa;
+        AU[i] = aun64;
+        AV[i] = todbl(avn);
+        AA[i] = todbl(aan);
         fwd_prep(i, un, dun, ddun, ddup, true, aun, avn, aan, aa, P);
     }
 }
@@ -635,8 +646,8 @@ static __global__ void k_fwd_prep(long long ndof, const double *__restrict__ u, 
                                   const double *__restrict__ AU, const double *__restrict__ AV,
                                   const double *__restrict__ AA, const double *__restrict__ AAprev, FwdPrep P) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)
-        fwd_prep(i, u[i], du[i], ddu[i], ddu_prev ? ddu_prev[i] : 0.0, ddu_prev != nullptr, AU[i], AV[i], AA[i],
-                 AAprev ? AAprev[i] : 0.0, P);
+        fwd_prep(i, df(u[i]), df(du[i]), df(ddu[i]), df(ddu_prev ? ddu_prev[i] : 0.0), ddu_prev != nullptr,
+                 df(AU[i]), df(AV[i]), df(AA[i]), df(AAprev ? AAprev[i] : 0.0), P);
 }
 
 // Mixed forward step, after the K-only double-float product y = K KS:
@@ -665,8 +676,12 @@ static __global__ void k_rhs_finish(long long ndof, const uint8_t *__restrict__ 
             r[i] = 0.0;
             continue;
         }
-        const double f2 = (i == L.load2_dof) ? L.sig2[t] : 0.0;
-        const double bv = L.rhs0[i] * s + f2 + b[i] + y[i];
+        // the load terms are nonzero on a few DOFs only: tested on the bit
+        // patterns (integer pipes), formed in FP64 where present
+        double bv = b[i] + y[i];
+        const double f0 = L.rhs0[i];
+        if (__double_as_longlong(f0) << 1) bv += f0 * s;
+        if (i == L.load2_dof) bv += L.sig2[t];
         const double rv = bv - r[i];
         b[i] = bv;
         r[i] = rv;

@@ -181,7 +181,7 @@ __device__ __forceinline__ void kron_x_body(const GridDesc &g, int kx, R *r, con
     const long long line0 = (long long)blockIdx.x * kx;
     const int nl = (int)(nlines - line0 < kx ? nlines - line0 : kx);
     const bool rs = S != nullptr && S->rescale != 0;
-    const double sg = rs ? S->sigma : 1.0;
+    const ScaleF64 sg = scale_split(rs ? S->sigma : 1.0);
     kron_stage_interior(B, 0, g.nx, tint);
     const long long q0 = line0 * row;
     const int nv = nl * row;
@@ -192,7 +192,7 @@ __device__ __forceinline__ void kron_x_body(const GridDesc &g, int kx, R *r, con
         const long long q = q0 + t;
         R rv;
         if (rs) {
-            rv = (R)(sg * r64[q]);
+            rv = (R)scaled_f32(r64[q], sg);
             r[q] = rv;
         } else {
             rv = r[q];
@@ -308,7 +308,8 @@ static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
         }
     }
     if constexpr (DOT) {
-        double red[2] = {(double)sr, (double)sq}, tot[2];
+        const float red[2] = {sr, sq};
+        double tot[2];
         if (grid_reduce<KRON_THREADS, 2>(red, kd.part, tot)) {
             SolveScalars *S = kd.S;
             S->rho = tot[0];

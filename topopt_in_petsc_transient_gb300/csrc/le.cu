@@ -1404,6 +1404,12 @@ static FwdPrep fwd_prep_args(TopoLE *le) {
     P.X0 = le->sx;
     P.BT = le->sb;
     P.AX = le->sr;
+    for (int i = 0; i < 3; i++) {
+        P.dck[i] = f64_to_df(P.ck[i]);
+        P.dcA[i] = f64_to_df(P.cA[i]);
+        P.dpred[i] = f64_to_df(P.pred[i]);
+    }
+    for (int i = 0; i < 2; i++) P.dpred2[i] = f64_to_df(P.pred2[i]);
     return P;
 }
 
@@ -1480,6 +1486,7 @@ static int fwd_step(TopoLE *le, bool capturing) {
     if (rc) return rc;
     Newmark nm;
     memcpy(nm.a, le->a, sizeof(nm.a));
+    for (int i = 0; i < 6; i++) nm.da[i] = f64_to_df(nm.a[i]);
     count_launch();
     if (track && le->a[0] == -1.0 && le->a[1] == 0.0)
         k_newmark_track<true><<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->st, le->cp, le->Uh, le->DUh,
@@ -1610,6 +1617,14 @@ static AdjCombine adj_args(TopoLE *le, int t0mode) {
         A.sK = 0.0;
         A.sM = 1.0;
     }
+    for (int i = 0; i < 6; i++) A.da[i] = f64_to_df(A.a[i]);
+    for (int i = 0; i < 3; i++) {
+        A.dcM[i] = f64_to_df(A.cM[i]);
+        A.dcK[i] = f64_to_df(A.cK[i]);
+    }
+    A.ddt = f64_to_df(A.dt);
+    A.dsK = f64_to_df(A.sK);
+    A.dsM = f64_to_df(A.sM);
     return A;
 }
 
@@ -1658,6 +1673,12 @@ static SensArgs sens_args(TopoLE *le, int t0mode) {
     S.df = le->df;
     S.fx = &le->st->fx;
     S.part = P1(le);
+    for (int i = 0; i < 3; i++) {
+        S.daK[i] = f64_to_df(S.aK[i]);
+        S.dbK[i] = f64_to_df(S.bK[i]);
+        S.daM[i] = f64_to_df(S.aM[i]);
+        S.dbM[i] = f64_to_df(S.bM[i]);
+    }
     return S;
 }
 
@@ -1709,6 +1730,14 @@ static void adj_kl(TopoLE *le) {
         product<true, false>(le, le->Lp1, le->KL, nullptr, 1.0, 0.0);
 }
 
+// the mixed path forms the adjoint right-hand side in double-float arithmetic
+static void launch_adj_combine(TopoLE *le, const AdjCombine &A) {
+    if (le->p.mixed)
+        k_adj_combine<df><<<ew_blocks(le->nn), EW, 0, le->stream>>>(A);
+    else
+        k_adj_combine<double><<<ew_blocks(le->nn), EW, 0, le->stream>>>(A);
+}
+
 static int adj_step(TopoLE *le, bool capturing) {
     cudaStream_t s = le->stream;
     // K L+ and M L+ (the B1..B3 products of LinearElasticity.cc:897-899)
@@ -1716,7 +1745,7 @@ static int adj_step(TopoLE *le, bool capturing) {
     if (!al_mode(le)) product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
     objective_products(le, 0);
     count_launch();
-    k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 0));
+    launch_adj_combine(le, adj_args(le, 0));
     le->ax0_pending = le->KLh1 != nullptr;
     int rc = solve(le, 0, le->sb, capturing);
     le->ax0_pending = false;
@@ -1738,7 +1767,7 @@ static int lagrange0(TopoLE *le) {
     if (!al_mode(le)) product<false, true>(le, le->Lp1, le->ML, nullptr, 0.0, 1.0);
     objective_products(le, 1);
     count_launch();
-    k_adj_combine<<<ew_blocks(le->nn), EW, 0, s>>>(adj_args(le, 1));
+    launch_adj_combine(le, adj_args(le, 1));
     le->ax0_pending = le->KLh1 != nullptr;
     int rc = solve(le, 1, le->sb, false);
     le->ax0_pending = false;
@@ -2536,6 +2565,7 @@ int le_stats(TopoLE *le, LEStats *out) {
     le->stats.mg_solves = le->mg_solves;
     le->stats.step_precond = le->design_ready ? (le->ops[0].kron ? 1 : 0) : -1;
     le->stats.graph_body_launches = (h.total_it - le->direct_iters) * le->body_kernels;
+    le->stats.replacements = h.replacements;
     *out = le->stats;
     return TOPO_OK;
 }

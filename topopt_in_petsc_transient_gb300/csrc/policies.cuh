@@ -37,6 +37,8 @@ struct SolveScalars {
     double sigma, ndof;
     int rescale;
     float beta32;     // beta of the FP32 recurrence in FP32 (read per staged node by PolPQ32)
+    float alpha32;    // alpha of the FP32 recurrence in FP32 and alpha / sigma (the
+    double alpha_x;   // step of the unscaled FP64 x): set once with alpha by PolPQ32
 };
 
 // ---------------------------------------------------------------------------
@@ -218,6 +220,8 @@ struct PolPQ32 {
         } else {
             S->alpha = S->rho / t[0];
         }
+        S->alpha32 = (float)S->alpha;
+        S->alpha_x = S->alpha / S->sigma;
     }
 };
 

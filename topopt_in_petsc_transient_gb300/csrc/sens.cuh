@@ -44,8 +44,26 @@ struct AdjCombine {
     double *ax0;
     const double *KLh1, *MLh1, *KLh2, *MLh2;
     double sK, sM;  // A = sK K + sM M
+    // the coefficients as double-float pairs (split on the host) for the
+    // double-float form of the mixed path
+    df da[6], dcM[3], dcK[3], ddt, dsK, dsM;
 };
+template <class R>
+__device__ __forceinline__ R adj_coef(double d, const df &f);
+template <>
+__device__ __forceinline__ double adj_coef<double>(double d, const df &) {
+    return d;
+}
+template <>
+__device__ __forceinline__ df adj_coef<df>(double, const df &f) {
+    return f;
+}
 
+// R = double: the plain FP64 path.  R = df: the mixed path, in
+// double-float arithmetic on the FP32 pipes with the FP64 inputs split on the
+// integer pipes and one FP64 addition per output (about 25 FP64 operations per
+// DOF otherwise, which GB300 runs at two per clock and SM).
+template <class R>
 static __global__ void k_adj_combine(AdjCombine A) {
     long long nn = A.ndof / 3;
     const double *u, *du, *ddu;
@@ -59,78 +77,93 @@ static __global__ void k_adj_combine(AdjCombine A) {
         du = A.DUstate + off;
         ddu = A.DDUstate + off;
     }
-    const double *a = A.a;
+    R a[6], cM[3], cK[3];
+#pragma unroll
+    for (int k = 0; k < 6; k++) a[k] = adj_coef<R>(A.a[k], A.da[k]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        cM[k] = adj_coef<R>(A.cM[k], A.dcM[k]);
+        cK[k] = adj_coef<R>(A.cK[k], A.dcK[k]);
+    }
+    const R dt = adj_coef<R>(A.dt, A.ddt), sK = adj_coef<R>(A.sK, A.dsK), sM = adj_coef<R>(A.sM, A.dsM);
+    const R zero = R(0.0);
+    const bool ax_is_mx = A.sK == 0.0 && A.sM == 1.0;  // mixed path: the ML slots hold A L
     const int nadj = A.st->nadj;  // adjoint steps done: lambda+, ++, +++ valid when nadj >= 1, 2, 3
+    // x0 = w1 L+ + w2 L++ + w3 L+++
+    double w1 = 1.0, w2 = 0.0, w3 = 0.0;
+    if (A.extrapolate >= 2 && nadj >= 3) {
+        w1 = 3.0;
+        w2 = -3.0;
+        w3 = 1.0;
+    } else if (A.extrapolate >= 1 && nadj >= 2) {
+        w1 = 2.0;
+        w2 = -1.0;
+    }
+    const R W1 = R(w1), W2 = R(w2), W3 = R(w3);
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
         uint8_t f = A.fixed[n];
-        double cnt = A.cntP[n];
+        const R cnt = R((double)A.cntP[n]);
         for (int c = 0; c < 3; c++) {
             long long i = 3 * n + c;
-            double hu = 0.0, hdu = 0.0, hddu = 0.0;
+            R hu = zero, hdu = zero, hddu = zero;
             switch (A.objective) {
-            case 0: hu = A.dt * cnt * u[i]; break;
-            case 1: hdu = A.dt * cnt * du[i]; break;
-            case 2: hddu = A.dt * cnt * ddu[i]; break;
-            case 3: hu = A.hK[i]; break;
-            case 4: hdu = A.hM[i]; break;
+            case 0: hu = dt * cnt * R(u[i]); break;
+            case 1: hdu = dt * cnt * R(du[i]); break;
+            case 2: hddu = dt * cnt * R(ddu[i]); break;
+            case 3: hu = R(A.hK[i]); break;
+            case 4: hdu = R(A.hM[i]); break;
             case 5:
-                hu = A.hK[i];
-                hdu = A.hM[i];
+                hu = R(A.hK[i]);
+                hdu = R(A.hM[i]);
                 break;
             case 7:  // extension: dt/2 u_out^2, gradient dt u_out at the output DOF
                 if (i == A.out_dof) {
-                    hu = A.dt * u[i];
+                    hu = dt * R(u[i]);
                     *A.fx += 0.5 * A.dt * u[i] * u[i];  // the one thread of this DOF
                 }
                 break;
-            default: hdu = A.hK[i]; break;
+            default: hdu = R(A.hK[i]); break;
             }
             bool fx = (f >> c) & 1;
-            double kl = fx ? 0.0 : A.KL[i], ml = fx ? 0.0 : A.ML[i];
-            double B1 = A.cM[0] * ml + A.cK[0] * kl;
-            double B2 = A.cM[1] * ml + A.cK[1] * kl;
-            double B3 = A.cM[2] * ml + A.cK[2] * kl;
-            double dlp = A.DLp1[i], ddlp = A.DDLp1[i];
+            const R kl = fx ? zero : R(A.KL[i]), ml = fx ? zero : R(A.ML[i]);
+            const R B1 = cM[0] * ml + cK[0] * kl;
+            const R B2 = cM[1] * ml + cK[1] * kl;
+            const R B3 = cM[2] * ml + cK[2] * kl;
+            const R dlp = R(A.DLp1[i]), ddlp = R(A.DDLp1[i]);
             if (A.t0mode) {
                 // SolveLagrange0 R3 (LinearElasticity.cc:753-758)
-                double r3 = -(hddu + B3 - a[1] * dlp + a[4] * ddlp);
-                A.b[i] = fx ? 0.0 : r3;
+                const R r3 = -(hddu + B3 - a[1] * dlp + a[4] * ddlp);
+                A.b[i] = fx ? 0.0 : todbl(r3);
                 A.x0[i] = 0.0;
                 if (A.ax0) A.ax0[i] = 0.0;
             } else {
-                double DL = -(hdu + B2 - a[0] * dlp + a[3] * ddlp);
-                double DDL = -(hddu + B3 + a[4] * ddlp);
-                double R1 = -(hu + B1 + a[2] * dlp + a[5] * ddlp) + a[2] * DL + a[5] * DDL;
-                A.DL[i] = DL;
-                A.DDL[i] = DDL;
+                const R DL = -(hdu + B2 - a[0] * dlp + a[3] * ddlp);
+                const R DDL = -(hddu + B3 + a[4] * ddlp);
+                const R R1 = -(hu + B1 + a[2] * dlp + a[5] * ddlp) + a[2] * DL + a[5] * DDL;
+                A.DL[i] = todbl(DL);
+                A.DDL[i] = todbl(DDL);
                 // the reference solves (N A N + I - N) L = R1 with A = -Keff
                 // (LinearElasticity.cc:1022-1026, :924): Keff L = -R1 on free DOFs
-                A.b[i] = fx ? 0.0 : -R1;
-                // x0 = w1 L+ + w2 L++ + w3 L+++
-                double w1 = 1.0, w2 = 0.0, w3 = 0.0;
-                if (A.extrapolate >= 2 && nadj >= 3) {
-                    w1 = 3.0;
-                    w2 = -3.0;
-                    w3 = 1.0;
-                } else if (A.extrapolate >= 1 && nadj >= 2) {
-                    w1 = 2.0;
-                    w2 = -1.0;
-                }
-                double g = w1 * A.Lp1[i];
-                if (w2 != 0.0) g += w2 * A.Lp2[i];
-                if (w3 != 0.0) g += w3 * A.Lp3[i];
-                A.x0[i] = fx ? 0.0 : g;
+                A.b[i] = fx ? 0.0 : todbl(-R1);
+                R g = W1 * R(A.Lp1[i]);
+                if (w2 != 0.0) g += W2 * R(A.Lp2[i]);
+                if (w3 != 0.0) g += W3 * R(A.Lp3[i]);
+                A.x0[i] = fx ? 0.0 : todbl(g);
                 if (A.ax0) {
-                    double mx = w1 * A.ML[i];
-                    if (w2 != 0.0) mx += w2 * A.MLh1[i];
-                    if (w3 != 0.0) mx += w3 * A.MLh2[i];
-                    double kx = 0.0;
-                    if (A.sK != 0.0) {  // mixed path: the ML slots hold A L and sK = 0
-                        kx = w1 * A.KL[i];
-                        if (w2 != 0.0) kx += w2 * A.KLh1[i];
-                        if (w3 != 0.0) kx += w3 * A.KLh2[i];
+                    R mx = W1 * R(A.ML[i]);
+                    if (w2 != 0.0) mx += W2 * R(A.MLh1[i]);
+                    if (w3 != 0.0) mx += W3 * R(A.MLh2[i]);
+                    R ax = mx;
+                    if (!ax_is_mx) {
+                        R kx = zero;
+                        if (A.sK != 0.0) {
+                            kx = W1 * R(A.KL[i]);
+                            if (w2 != 0.0) kx += W2 * R(A.KLh1[i]);
+                            if (w3 != 0.0) kx += W3 * R(A.KLh2[i]);
+                        }
+                        ax = sK * kx + sM * mx;
                     }
-                    A.ax0[i] = fx ? 0.0 : A.sK * kx + A.sM * mx;
+                    A.ax0[i] = fx ? 0.0 : todbl(ax);
                 }
             }
         }
@@ -238,6 +271,9 @@ struct SensArgs {
     double *df;
     double *fx;                              // device accumulator
     Partials<1> part;
+    // aK, bK, aM, bM as double-float pairs (split on the host), for the
+    // FP32-output form of k_sens_nodal
+    topo::df daK[3], dbK[3], daM[3], dbM[3];
 };
 
 // current state (t0mode: the t = 0 state) and previous state of the step
@@ -277,32 +313,60 @@ __device__ __forceinline__ double comb3(const double c[3], double v0, double v1,
     return s;
 }
 
+// the same in double-float; nz holds the nonzero pattern of c (bit k: c[k])
+__device__ __forceinline__ topo::df comb3(const topo::df c[3], int nz, topo::df v0, topo::df v1, topo::df v2) {
+    topo::df s = c[0] * v0;
+    if (nz & 2) s += c[1] * v1;
+    if (nz & 4) s += c[2] * v2;
+    return s;
+}
+__host__ __device__ __forceinline__ int comb3_nz(const double c[3]) {
+    return (c[0] != 0.0 ? 1 : 0) | (c[1] != 0.0 ? 2 : 0) | (c[2] != 0.0 ? 4 : 0);
+}
+
 // wK = aK . (u, du, ddu) + bK . (u-, du-, ddu-) and wM likewise, once per DOF
-// (every node is shared by up to 8 elements, so this is 8x less FP64 work
-// than forming them inside the element loop)
+// (every node is shared by up to 8 elements, so this is 8x less work than
+// forming them inside the element loop).  FP64 element math: FP64
+// combinations.  FP32 element math: the combinations in double-float on the
+// FP32 pipes from inputs split on the integer pipes, rounded to FP32 (the hi
+// part): no FP64 instruction, where the FP64 form was bound by GB300's FP64
+// rate.
 static __global__ void k_sens_nodal(const SensArgs A) {
     const long long ndof = 3 * A.g.nn();
     const double *u, *du, *ddu, *up, *dup, *ddup;
     sens_states(A, ndof, u, du, ddu, up, dup, ddup);
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ndof; q += (long long)gridDim.x * blockDim.x) {
-        double s0 = u[q], s1 = du[q], s2 = ddu[q];
-        double wk = comb3(A.aK, s0, s1, s2);
-        double wm = comb3(A.aM, s0, s1, s2);
-        if (!A.t0mode) {
-            double p0 = up[q], p1 = dup[q], p2 = ddup[q];
-            wk += comb3(A.bK, p0, p1, p2);
-            wm += comb3(A.bM, p0, p1, p2);
-        }
-        if (A.wKd) {
+    if (A.wKd) {
+        for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ndof;
+             q += (long long)gridDim.x * blockDim.x) {
+            double s0 = u[q], s1 = du[q], s2 = ddu[q];
+            double wk = comb3(A.aK, s0, s1, s2);
+            double wm = comb3(A.aM, s0, s1, s2);
+            if (!A.t0mode) {
+                double p0 = up[q], p1 = dup[q], p2 = ddup[q];
+                wk += comb3(A.bK, p0, p1, p2);
+                wm += comb3(A.bM, p0, p1, p2);
+            }
             A.wKd[q] = wk;
             A.wMd[q] = wm;
-        } else {  // FP32 element math: conversions on the integer pipes
-            A.wKf[q] = f64_to_f32(wk);
-            A.wMf[q] = f64_to_f32(wm);
-            A.lamf[q] = f64_to_f32(A.lam[q]);
-            if (A.uf) A.uf[q] = f64_to_f32(s0);
-            if (A.duf) A.duf[q] = f64_to_f32(s1);
         }
+        return;
+    }
+    const int nzaK = comb3_nz(A.aK), nzaM = comb3_nz(A.aM), nzbK = comb3_nz(A.bK), nzbM = comb3_nz(A.bM);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ndof; q += (long long)gridDim.x * blockDim.x) {
+        const double s0 = u[q], s1 = du[q];
+        const topo::df d0(s0), d1(s1), d2(ddu[q]);
+        topo::df wk = comb3(A.daK, nzaK, d0, d1, d2);
+        topo::df wm = comb3(A.daM, nzaM, d0, d1, d2);
+        if (!A.t0mode) {
+            const topo::df p0(up[q]), p1(dup[q]), p2(ddup[q]);
+            wk += comb3(A.dbK, nzbK, p0, p1, p2);
+            wm += comb3(A.dbM, nzbM, p0, p1, p2);
+        }
+        A.wKf[q] = wk.hi;
+        A.wMf[q] = wm.hi;
+        A.lamf[q] = f64_to_f32(A.lam[q]);
+        if (A.uf) A.uf[q] = d0.hi;
+        if (A.duf) A.duf[q] = d1.hi;
     }
 }
 

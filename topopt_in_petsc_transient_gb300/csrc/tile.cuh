@@ -418,10 +418,8 @@ __global__ void __launch_bounds__(TILE_THREADS, sizeof(T) == 4 ? 2 : 1) k_tile(c
         }
     }
     if constexpr (Pol::NRED > 0) {
-        double rd[Pol::NRED], tot[Pol::NRED];
-#pragma unroll
-        for (int r = 0; r < Pol::NRED; r++) rd[r] = (double)red[r];
-        if (grid_reduce<TILE_THREADS, Pol::NRED>(rd, pol.part, tot)) pol.finish(tot);
+        double tot[Pol::NRED];
+        if (grid_reduce<TILE_THREADS, Pol::NRED>(red, pol.part, tot)) pol.finish(tot);
     }
 }
 

@@ -299,7 +299,7 @@ class LinearElasticity:
         check(_lib.load().topo_le_get_stats(self._h, C.byref(s)), "get_stats")
         return {"cg_iterations": s.cg_iterations, "solves": s.solves, "device_bytes": s.device_bytes,
                 "last_fx": s.last_fx, "graph_body_launches": s.graph_body_launches, "mg_solves": s.mg_solves,
-                "step_precond": s.step_precond}
+                "step_precond": s.step_precond, "replacements": s.replacements}
 
 
 class SOMMG:
