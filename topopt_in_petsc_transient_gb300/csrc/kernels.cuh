@@ -603,7 +603,7 @@ __device__ __forceinline__ void fwd_prep(long long i, df u, df du, df ddu, df dd
 // about twice its DRAM time.
 // STD: Newmark beta = 1/4, gamma = 1/2 (a0 = -1, a1 = 0).
 template <bool STD>
-static __global__ void k_newmark_track(long long ndof, double *x, const StepCtx *st, const double *cp, double *Uh,
+static __global__ void __launch_bounds__(EW, 4) k_newmark_track(long long ndof, double *x, const StepCtx *st, const double *cp, double *Uh,
                                        double *DUh, double *DDUh, Newmark nm, double *b, double *r,
                                        const SolveScalars *S, double *AU, double *AV, double *AA, FwdPrep P) {
     const int j = st->j;
@@ -662,32 +662,50 @@ struct RhsLoad {
     const double *sig, *sig2;  // per-step load signals (k_load_table)
     long long load2_dof;
 };
-static __global__ void k_rhs_finish(long long ndof, const uint8_t *__restrict__ fixed, const double *__restrict__ y,
+static __global__ void __launch_bounds__(EW, 4) k_rhs_finish(long long ndof, const uint8_t *__restrict__ fixed, const double *__restrict__ y,
                                     RhsLoad L, const StepCtx *st, double *__restrict__ b, double *__restrict__ r,
                                     SolveScalars *S, cudaGraphConditionalHandle cond, int has_cond, Partials<2> part) {
     const int t = st->tsc * st->block + st->j + 1;
     const double s = L.sig[t];
     double red[2] = {0.0, 0.0};
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
-        const long long n = i / 3;
-        const int c = (int)(i - 3 * n);
-        if ((fixed[n] >> c) & 1) {
+    // the load terms are nonzero on a few DOFs only: tested on the bit
+    // patterns (integer pipes), formed in FP64 where present
+    auto one = [&](long long i, uint8_t f, double bi, double yi, double f0, double ri) {
+        const int c = (int)(i % 3);
+        if ((f >> c) & 1) {
             b[i] = 0.0;
             r[i] = 0.0;
-            continue;
+            return;
         }
-        // the load terms are nonzero on a few DOFs only: tested on the bit
-        // patterns (integer pipes), formed in FP64 where present
-        double bv = b[i] + y[i];
-        const double f0 = L.rhs0[i];
+        double bv = bi + yi;
         if (__double_as_longlong(f0) << 1) bv += f0 * s;
         if (i == L.load2_dof) bv += L.sig2[t];
-        const double rv = bv - r[i];
+        const double rv = bv - ri;
         b[i] = bv;
         r[i] = rv;
         red[0] += bv * bv;
         red[1] += rv * rv;
+    };
+    // four grid strides per trip: all loads of a trip are issued before the
+    // FP64 reductions that depend on them
+    const long long gs = (long long)gridDim.x * blockDim.x;
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i + 3 * gs < ndof; i += 4 * gs) {
+        uint8_t f[4];
+        double bi[4], yi[4], fi[4], ri[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const long long k = i + u * gs;
+            f[u] = fixed[k / 3];
+            bi[u] = b[k];
+            yi[u] = y[k];
+            fi[u] = L.rhs0[k];
+            ri[u] = r[k];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) one(i + u * gs, f[u], bi[u], yi[u], fi[u], ri[u]);
     }
+    for (; i < ndof; i += gs) one(i, fixed[i / 3], b[i], y[i], L.rhs0[i], r[i]);
     double tot[2];
     if (grid_reduce<EW, 2>(red, part, tot)) init_finish(S, tot, true, cond, has_cond, false);
 }
