@@ -96,6 +96,12 @@ __host__ __device__ inline ElemConst<T> make_elem_const_base(double hx, double h
     return c;
 }
 
+// sums of the element math; df.cuh overloads them for double-float pairs
+__host__ __device__ __forceinline__ float tadd(float a, float b) { return a + b; }
+__host__ __device__ __forceinline__ double tadd(double a, double b) { return a + b; }
+__host__ __device__ __forceinline__ float tsub(float a, float b) { return a - b; }
+__host__ __device__ __forceinline__ double tsub(double a, double b) { return a - b; }
+
 // nodal -> mode transform of one component (local node L = ax + 2ay + 4az)
 template <class T>
 __host__ __device__ __forceinline__ void mode_fwd(T v[8]) {
@@ -106,8 +112,8 @@ __host__ __device__ __forceinline__ void mode_fwd(T v[8]) {
         for (int L = 0; L < 8; L++) {
             if (L & b) continue;
             T a0 = v[L], a1 = v[L | b];
-            v[L] = a0 + a1;
-            v[L | b] = a1 - a0;
+            v[L] = tadd(a0, a1);
+            v[L | b] = tsub(a1, a0);
         }
     }
 }
@@ -122,8 +128,8 @@ __host__ __device__ __forceinline__ void mode_bwd(T v[8]) {
         for (int L = 0; L < 8; L++) {
             if (L & b) continue;
             T sv = v[L], dv = v[L | b];
-            v[L] = sv - dv;
-            v[L | b] = sv + dv;
+            v[L] = tsub(sv, dv);
+            v[L | b] = tadd(sv, dv);
         }
     }
 }
@@ -196,24 +202,25 @@ __host__ __device__ __forceinline__ void mode_khat(const ElemConst<T> &C, const 
             const int ir = kh_idx(b, r);
             T acc = C.K[k + r * n] * U[kh_idx(b, 0) / 8][kh_idx(b, 0) % 8];
 #pragma unroll
-            for (int s = 1; s < n; s++) acc += C.K[k + r * n + s] * U[kh_idx(b, s) / 8][kh_idx(b, s) % 8];
+            for (int s = 1; s < n; s++) acc = tadd(acc, C.K[k + r * n + s] * U[kh_idx(b, s) / 8][kh_idx(b, s) % 8]);
             Y[ir / 8][ir % 8] = acc;
         }
         k += n * n;
     }
 }
 
-// Y = ck Khat U + cm W .* U (stiffness + mass in mode space); each U entry
-// is consumed by one block, so the live range shrinks as blocks complete
-template <class T>
+// Y = ck Khat U + cm W .* U (stiffness + mass in mode space; MASS = false:
+// ck Khat U alone); each U entry is consumed by one block, so the live range
+// shrinks as blocks complete
+template <bool MASS = true, class T>
 __host__ __device__ __forceinline__ void mode_khat_mass(const ElemConst<T> &C, T ck, T cm, const T U[3][8],
                                                         T Y[3][8]) {
     T cw[8];
 #pragma unroll
-    for (int m = 0; m < 8; m++) cw[m] = cm * C.W[m];
-    Y[0][0] = cw[0] * U[0][0];
-    Y[1][0] = cw[0] * U[1][0];
-    Y[2][0] = cw[0] * U[2][0];
+    for (int m = 0; m < 8; m++) cw[m] = MASS ? cm * C.W[m] : T(0);
+    Y[0][0] = MASS ? cw[0] * U[0][0] : T(0);
+    Y[1][0] = MASS ? cw[0] * U[1][0] : T(0);
+    Y[2][0] = MASS ? cw[0] * U[2][0] : T(0);
     int k = 0;
 #pragma unroll
     for (int b = 0; b < KH_NB; b++) {
@@ -223,8 +230,8 @@ __host__ __device__ __forceinline__ void mode_khat_mass(const ElemConst<T> &C, T
             const int ir = kh_idx(b, r);
             T acc = C.K[k + r * n] * U[kh_idx(b, 0) / 8][kh_idx(b, 0) % 8];
 #pragma unroll
-            for (int s = 1; s < n; s++) acc += C.K[k + r * n + s] * U[kh_idx(b, s) / 8][kh_idx(b, s) % 8];
-            Y[ir / 8][ir % 8] = ck * acc + cw[ir % 8] * U[ir / 8][ir % 8];
+            for (int s = 1; s < n; s++) acc = tadd(acc, C.K[k + r * n + s] * U[kh_idx(b, s) / 8][kh_idx(b, s) % 8]);
+            Y[ir / 8][ir % 8] = MASS ? tadd(ck * acc, cw[ir % 8] * U[ir / 8][ir % 8]) : ck * acc;
         }
         k += n * n;
     }

@@ -145,6 +145,8 @@ __device__ __forceinline__ void tile_elements(const GridDesc &g, const ElemConst
         T Y[3][8];
         if (Pol::HAS_K && Pol::HAS_M && Pol::NIN == 1) {
             mode_khat_mass(C, ck, cm, U, Y);
+        } else if (Pol::HAS_K && !Pol::HAS_M) {
+            mode_khat_mass<false>(C, ck, cm, U, Y);
         } else {
             if (Pol::HAS_K) {
                 mode_khat(C, U, Y);
@@ -174,7 +176,7 @@ __device__ __forceinline__ void tile_elements(const GridDesc &g, const ElemConst
                         for (int m = 0; m < 8; m++) V[m] = U[b][m];
                     }
 #pragma unroll
-                    for (int m = 0; m < 8; m++) Y[b][m] += (cm * C.W[m]) * V[m];
+                    for (int m = 0; m < 8; m++) Y[b][m] = tadd(Y[b][m], (cm * C.W[m]) * V[m]);
                 }
             }
         }
@@ -201,7 +203,7 @@ __device__ __forceinline__ void tile_gather(const Pol &pol, const T *sEl, long l
         int ax = L & 1, ay = (L >> 1) & 1, az = L >> 2;
         int le = (tx + 1 - ax) + TILE_E * ((ty + 1 - ay) + TILE_E * (tz + 1 - az));
 #pragma unroll
-        for (int c = 0; c < 3; c++) y[c] += sEl[le * EL_STRIDE + L * 3 + c];
+        for (int c = 0; c < 3; c++) y[c] = tadd(y[c], sEl[le * EL_STRIDE + L * 3 + c]);
     }
     pol_epi(pol, on, oi, oj, ok, y, red, pre, 0);
 }
