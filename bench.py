@@ -47,7 +47,15 @@ TRAFFIC = {
     ("96x48x48", "k_tile<float,PolPQ32>"): 7.627e6,
     ("192x96x96", "k_kron_pass<float>"): (43.62e6 + 0.437e6 + 21.82e6 + 87.26e6 + 5.977e6) / 3.0,
     ("192x96x96", "k_tile<float,PolPQ32>"): 59.60e6 + 6.723e6,
+    ("192x96x96", "k_tile<df,PolProduct>"): 57.80e6 + 7.868e6,
 }
+# warp instructions per launch of the instruction-issue-bound classes (ncu,
+# smsp__inst_executed.sum of one launch; profiles/): the double-float tile
+# kernels are bound by issue, not by HBM, and this is their roofline
+ISSUE = {
+    ("192x96x96", "k_tile<df,PolProduct>"): 208.4e6,
+}
+SMSP_PER_SM = 4  # warp schedulers per SM: one warp instruction each per clock
 UNIT = "design_iter/s"
 
 
@@ -360,6 +368,8 @@ def roofline(args, wl, opt):
     L = _lib.load()
     nel = opt_nel(wl)
     nn = (wl["nelx"] + 1) * (wl["nely"] + 1) * (wl["nelz"] + 1)
+    import torch
+    nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     probe = TopOpt(mixed=True, **dict(wl, use_graphs=False)).setup()
     for _ in range(args.warmup):
         design_iteration(probe)
@@ -380,24 +390,38 @@ def roofline(args, wl, opt):
                 (36.0 + 24.0 + 60.0) / 3.0 * nn),
                (0, "k_tile<float,PolCheb> (FP32 Chebyshev-Jacobi smoothing step)", 73.0 * nn + 8.0 * nel),
                (3, "k_tile<df,PolReplaceProduct> (FP64-accurate A x of a residual replacement, double-float; "
-                   "launches without a due replacement exit at once and are averaged in)", 49.0 * nn + 16.0 * nel),
+                   "launches without a due replacement exit at once: algorithmic bytes per launch = bytes of a "
+                   "replacement x replacements / launches)", 49.0 * nn + 16.0 * nel),
                (4, "k_tile<df,PolProduct> (double-float K or A products of right-hand sides, anchors and adjoint "
                    "steps)", 48.0 * nn + 8.0 * nel)]
     kern = []
     for cls, name, nbytes in classes:
         _lib.check(L.topo_le_kernel_timing(probe.physics._h, cls, 1, None, None), "kernel_timing")
+        repl0 = probe.physics.stats()["replacements"]
         design_iteration(probe)
         tot_ms, nlaunch = C.c_double(), C.c_longlong()
         _lib.check(L.topo_le_kernel_timing(probe.physics._h, cls, 0, C.byref(tot_ms), C.byref(nlaunch)),
                    "kernel_timing")
         if nlaunch.value == 0:
             continue
+        if cls == 3:  # only launches with a due replacement do the element work
+            nbytes *= min(1.0, (probe.physics.stats()["replacements"] - repl0) / nlaunch.value)
         ms_launch = tot_ms.value / nlaunch.value
         ach = nbytes / (ms_launch * 1e-3) / 1e9
-        kern.append({"kernel": name, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach / peaks["hbm_gbs"], "ms_per_launch": ms_launch, "launches_timed": nlaunch.value,
-                     "ms_per_design_iter": tot_ms.value, "algorithmic_bytes": nbytes,
-                     "traffic": TRAFFIC.get((args.mesh, name.split(" ")[0]))})
+        entry = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                 "frac": ach / peaks["hbm_gbs"], "ms_per_launch": ms_launch, "launches_timed": nlaunch.value,
+                 "ms_per_design_iter": tot_ms.value, "algorithmic_bytes": nbytes,
+                 "traffic": TRAFFIC.get((args.mesh, name.split(" ")[0]))}
+        ninst = ISSUE.get((args.mesh, name.split(" ")[0]))
+        if ninst:
+            issue_peak = nsm * SMSP_PER_SM * peaks["sm_max_mhz"] * 1e6
+            entry["issue"] = {"warp_instructions_per_launch": ninst,
+                              "achieved_warp_inst_per_s": ninst / (ms_launch * 1e-3),
+                              "peak_warp_inst_per_s": issue_peak,
+                              "frac": ninst / (ms_launch * 1e-3) / issue_peak,
+                              "note": "instruction-issue bound (double-float arithmetic on the FP32 pipes); "
+                                      "peak = SMs x 4 schedulers x max SM clock"}
+        kern.append(entry)
     ms_fp64 = C.c_double()
     _lib.check(L.topo_le_time_apply(probe.physics._h, 0, 5, 50, C.byref(ms_fp64)), "time_apply")
     del probe
@@ -516,10 +540,11 @@ def load_peaks():
             if isinstance(hbm, dict):
                 hbm = hbm.get("value")
             if hbm:
-                return {"hbm_gbs": float(hbm), "source": "measured (MEASURED_PEAKS.json)"}
+                return {"hbm_gbs": float(hbm), "source": "measured (MEASURED_PEAKS.json)",
+                        "sm_max_mhz": float(d.get("sm_max_mhz") or 2070.0)}
         except (ValueError, OSError):
             pass
-    return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s"}
+    return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s", "sm_max_mhz": 2070.0}
 
 
 def oracle_le(wl, steps, dt, rtol):

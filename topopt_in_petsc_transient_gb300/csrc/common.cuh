@@ -96,11 +96,23 @@ __host__ __device__ inline ElemConst<T> make_elem_const_base(double hx, double h
     return c;
 }
 
+// (i, j, k) of lexicographic index n on an nx x ny x . grid with 32-bit
+// unsigned divisions: node and element indices stay far below 2^32 on every
+// grid that fits in HBM (the 64-bit division sequences cost several times more)
+__host__ __device__ __forceinline__ void lex3(long long n, int nx, int ny, int &i, int &j, int &k) {
+    const unsigned u = (unsigned)n, q = u / (unsigned)nx;
+    i = (int)(u - q * (unsigned)nx);
+    k = (int)(q / (unsigned)ny);
+    j = (int)(q - (unsigned)k * (unsigned)ny);
+}
+
 // sums of the element math; df.cuh overloads them for double-float pairs
 __host__ __device__ __forceinline__ float tadd(float a, float b) { return a + b; }
 __host__ __device__ __forceinline__ double tadd(double a, double b) { return a + b; }
 __host__ __device__ __forceinline__ float tsub(float a, float b) { return a - b; }
 __host__ __device__ __forceinline__ double tsub(double a, double b) { return a - b; }
+__host__ __device__ __forceinline__ float tmul(float a, float b) { return a * b; }
+__host__ __device__ __forceinline__ double tmul(double a, double b) { return a * b; }
 
 // nodal -> mode transform of one component (local node L = ax + 2ay + 4az)
 template <class T>
@@ -217,10 +229,10 @@ __host__ __device__ __forceinline__ void mode_khat_mass(const ElemConst<T> &C, T
                                                         T Y[3][8]) {
     T cw[8];
 #pragma unroll
-    for (int m = 0; m < 8; m++) cw[m] = MASS ? cm * C.W[m] : T(0);
-    Y[0][0] = MASS ? cw[0] * U[0][0] : T(0);
-    Y[1][0] = MASS ? cw[0] * U[1][0] : T(0);
-    Y[2][0] = MASS ? cw[0] * U[2][0] : T(0);
+    for (int m = 0; m < 8; m++) cw[m] = MASS ? tmul(cm, C.W[m]) : T(0);
+    Y[0][0] = MASS ? tmul(cw[0], U[0][0]) : T(0);
+    Y[1][0] = MASS ? tmul(cw[0], U[1][0]) : T(0);
+    Y[2][0] = MASS ? tmul(cw[0], U[2][0]) : T(0);
     int k = 0;
 #pragma unroll
     for (int b = 0; b < KH_NB; b++) {
@@ -228,10 +240,11 @@ __host__ __device__ __forceinline__ void mode_khat_mass(const ElemConst<T> &C, T
 #pragma unroll
         for (int r = 0; r < n; r++) {
             const int ir = kh_idx(b, r);
-            T acc = C.K[k + r * n] * U[kh_idx(b, 0) / 8][kh_idx(b, 0) % 8];
+            T acc = tmul(C.K[k + r * n], U[kh_idx(b, 0) / 8][kh_idx(b, 0) % 8]);
 #pragma unroll
-            for (int s = 1; s < n; s++) acc = tadd(acc, C.K[k + r * n + s] * U[kh_idx(b, s) / 8][kh_idx(b, s) % 8]);
-            Y[ir / 8][ir % 8] = MASS ? tadd(ck * acc, cw[ir % 8] * U[ir / 8][ir % 8]) : ck * acc;
+            for (int s = 1; s < n; s++)
+                acc = tadd(acc, tmul(C.K[k + r * n + s], U[kh_idx(b, s) / 8][kh_idx(b, s) % 8]));
+            Y[ir / 8][ir % 8] = MASS ? tadd(tmul(ck, acc), tmul(cw[ir % 8], U[ir / 8][ir % 8])) : tmul(ck, acc);
         }
         k += n * n;
     }

@@ -58,7 +58,8 @@ __global__ void k_filt_apply(GridDesc g, KFMat KF, const double *__restrict__ x,
     long long nn = g.nn();
     double v[1] = {0.0};
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
+        int i, j, k;
+        lex3(n, g.nx, g.ny, i, j, k);
         double acc = 0.0;
         for (int c = 0; c < 8; c++) {
             int ei = i - (c & 1), ej = j - ((c >> 1) & 1), ek = k - (c >> 2);
@@ -88,7 +89,8 @@ __global__ void k_filt_apply(GridDesc g, KFMat KF, const double *__restrict__ x,
 __global__ void k_T(GridDesc g, double vol, const double *__restrict__ x, double *rhs) {
     long long nn = g.nn();
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
+        int i, j, k;
+        lex3(n, g.nx, g.ny, i, j, k);
         double acc = 0.0;
         for (int c = 0; c < 8; c++) {
             int ei = i - (c & 1), ej = j - ((c >> 1) & 1), ek = k - (c >> 2);
@@ -106,7 +108,8 @@ __global__ void k_Tt(GridDesc g, const double *__restrict__ u, double *xout, dou
     long long nel = g.nel();
     double den = tanh(beta * eta) + tanh(beta * (1.0 - eta));
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(e % g.ex), j = (int)((e / g.ex) % g.ey), k = (int)(e / ((long long)g.ex * g.ey));
+        int i, j, k;
+        lex3(e, g.ex, g.ey, i, j, k);
         double acc = 0.0;
         for (int L = 0; L < 8; L++)
             acc += 0.125 * u[(i + (L & 1)) + (long long)g.nx * ((j + ((L >> 1) & 1)) + (long long)g.ny * (k + (L >> 2)))];
@@ -134,7 +137,8 @@ __global__ void k_chain(long long nel, const double *__restrict__ xt, double *df
 __global__ void k_filt_dinv(GridDesc g, KFMat KF, double *dinv) {
     long long nn = g.nn();
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
+        int i, j, k;
+        lex3(n, g.nx, g.ny, i, j, k);
         double acc = 0.0;
         for (int c = 0; c < 8; c++) {
             int ei = i - (c & 1), ej = j - ((c >> 1) & 1), ek = k - (c >> 2);

@@ -99,7 +99,8 @@ static __global__ void k_dinv(GridDesc g, const uint8_t *__restrict__ fixed, con
                        double *dinvd, float *dinvf) {
     long long nn = g.nn();
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
+        int i, j, k;
+        lex3(n, g.nx, g.ny, i, j, k);
         double sk = 0.0, sm = 0.0;
         for (int c = 0; c < 8; c++) {
             int ei = i - (c & 1), ej = j - ((c >> 1) & 1), ek = k - (c >> 2);
@@ -307,8 +308,10 @@ static __global__ void k_coarse_assemble(GridDesc g, const uint8_t *__restrict__
         long long r = t / nd, s = t % nd;
         long long nr = r / 3, ns = s / 3;
         int cr = (int)(r % 3), cs = (int)(s % 3);
-        int ir = (int)(nr % g.nx), jr = (int)((nr / g.nx) % g.ny), kr = (int)(nr / ((long long)g.nx * g.ny));
-        int is = (int)(ns % g.nx), js = (int)((ns / g.nx) % g.ny), ks = (int)(ns / ((long long)g.nx * g.ny));
+        int ir, jr, kr;
+        lex3(nr, g.nx, g.ny, ir, jr, kr);
+        int is, js, ks;
+        lex3(ns, g.nx, g.ny, is, js, ks);
         bool fr = (fixed[nr] >> cr) & 1, fs = (fixed[ns] >> cs) & 1;
         double v = 0.0;
         if (fr || fs) {
@@ -511,6 +514,8 @@ static __global__ void k_mfcg_update(long long ndof, double *__restrict__ x, flo
     }
 }
 
+// almost always a no-op (the solve zeroes x only for a zero right-hand side):
+// launched as one wave of grid-stride CTAs, so the check costs one wave
 static __global__ void k_fcg_zero_x(long long ndof, double *x, const SolveScalars *S) {
     if (!S->zero_x) return;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x)

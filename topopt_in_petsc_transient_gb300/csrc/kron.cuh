@@ -31,7 +31,8 @@ static __global__ void k_kron_scale(GridDesc g, const uint8_t *__restrict__ fixe
                                     double sM, T *ms) {
     long long nn = g.nn();
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
+        int i, j, k;
+        lex3(n, g.nx, g.ny, i, j, k);
         double s = 0.0;
         int cnt = 0;
         for (int c = 0; c < 8; c++) {
@@ -185,9 +186,12 @@ __device__ __forceinline__ void kron_x_body(const GridDesc &g, int kx, R *r, con
     kron_stage_interior(B, 0, g.nx, tint);
     const long long q0 = line0 * row;
     const int nv = nl * row;
+    // t / row by a multiply-high with ceil(2^32 / row), exact for t < 2^32 / row
+    // (nv is a few thousand): no integer division sequence per value
+    const unsigned mrow = (unsigned)((0x100000000ull + (unsigned)row - 1) / (unsigned)row);
 #pragma unroll 4
     for (int t = threadIdx.x; t < nv; t += KRON_THREADS) {
-        const int l = t / row, w = t - l * row;  // line and position of value t
+        const int l = (int)__umulhi((unsigned)t, mrow), w = t - l * row;  // line and position of value t
         const int i = w / 3, c = w - 3 * i;
         const long long q = q0 + t;
         R rv;
@@ -216,7 +220,7 @@ __device__ __forceinline__ void kron_x_body(const GridDesc &g, int kx, R *r, con
     __syncthreads();
 #pragma unroll 4
     for (int t = threadIdx.x; t < nv; t += KRON_THREADS) {
-        const int l = t / row, w = t - l * row;
+        const int l = (int)__umulhi((unsigned)t, mrow), w = t - l * row;
         const int i = w / 3, c = w - 3 * i;
         out[q0 + t] = otile[(l * 3 + c) * LP + i];
     }
@@ -263,19 +267,23 @@ static __global__ void __launch_bounds__(KRON_THREADS, sizeof(T) == 4 ? 4 : 2)
     const long long S = AXIS == 1 ? (long long)row : (long long)row * g.ny;
     const long long base = AXIS == 1 ? (long long)other * row * g.ny + w0 : (long long)other * row + w0;
     kron_stage_interior(B, AXIS, len, tint);
-#pragma unroll 4
+    // the staging is a pure copy: cp.async puts every copy of the chunk in
+    // flight at once, with no register round trip
+    static_assert(std::is_same<T, R>::value, "staged r is copied, not converted");
     for (int t = threadIdx.x; t < len * KW; t += KRON_THREADS) {
         const int p = t / KW, w = t - p * KW;
         if (w < wn) {
             const long long q = base + p * S + w;
-            tile[t] = in[q];
+            cp_async<(int)sizeof(T)>(tile + t, in + q);
             if (AXIS == 2) {
-                rt[t] = (T)r[q];
-                mt[t] = ms[q];
-                if (DOT) qt[t] = kd.q32[q];
+                cp_async<(int)sizeof(T)>(rt + t, r + q);
+                cp_async<(int)sizeof(T)>(mt + t, ms + q);
+                if (DOT) cp_async<4>(qt + t, kd.q32 + q);
             }
         }
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     // the FCG dot products: FP32 per thread (at most a few dozen terms), FP64
     // across threads (GB300 runs FP64 at 1/64 of the FP32 rate)

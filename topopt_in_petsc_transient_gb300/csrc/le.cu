@@ -1213,7 +1213,7 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
         } else {
             if (le->ops[o].depth == 1 && le->nlev == 1 && le->coarse_dense) {
                 count_launch();  // the dense coarse solve has no smoothing step to carry the rescaling
-                k_mfcg_scale<<<ew_blocks(nd), EW, 0, s>>>(nd, le->sr, le->sr32, le->S);
+                k_mfcg_scale<<<red_blocks(nd), EW, 0, s>>>(nd, le->sr, le->sr32, le->S);
             }
             z = vcycle<float>(le, o, 0, le->sr32, &fz);
         }
@@ -1266,7 +1266,7 @@ static int solve_direct(TopoLE *le, int o, const double *b) {
         le->direct_iters++;
     }
     count_launch();
-    k_fcg_zero_x<<<ew_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, le->sx, le->S);
+    k_fcg_zero_x<<<red_blocks(le->ndof), EW, 0, le->stream>>>(le->ndof, le->sx, le->S);
     count_launch();
     k_solve_check<<<1, 1, 0, le->stream>>>(le->S, le->err);
     le->nsolves++;
@@ -1313,7 +1313,7 @@ static int solve_captured(TopoLE *le, int o, const double *b) {
     cudaStreamDestroy(bs);
     CK(e1);
     count_launch();
-    k_fcg_zero_x<<<ew_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->S);
+    k_fcg_zero_x<<<red_blocks(le->ndof), EW, 0, s>>>(le->ndof, le->sx, le->S);
     count_launch();
     k_solve_check<<<1, 1, 0, s>>>(le->S, le->err);
     return TOPO_OK;

@@ -50,9 +50,13 @@ struct Weights {
     const double *P;   // optional region mask
     T sK, sM;
     __device__ __forceinline__ void get(long long e, T &ck, T &cm) const {
-        T w = P ? (T)P[e] : T(1);
-        ck = kf ? sK * kf[e] * w : T(0);
-        cm = mf ? sM * mf[e] * w : T(0);
+        ck = kf ? sK * kf[e] : T(0);
+        cm = mf ? sM * mf[e] : T(0);
+        if (P) {  // region mask: only when the caller passes one
+            const T w = (T)P[e];
+            ck = ck * w;
+            cm = cm * w;
+        }
     }
 };
 

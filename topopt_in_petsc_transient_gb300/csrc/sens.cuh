@@ -174,7 +174,8 @@ static __global__ void k_adj_combine(AdjCombine A) {
 static __global__ void k_count_region(GridDesc g, const double *__restrict__ P, float *cnt) {
     long long nn = g.nn();
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(n % g.nx), j = (int)((n / g.nx) % g.ny), k = (int)(n / ((long long)g.nx * g.ny));
+        int i, j, k;
+        lex3(n, g.nx, g.ny, i, j, k);
         double s = 0.0;
         for (int c = 0; c < 8; c++) {
             int ei = i - (c & 1), ej = j - ((c >> 1) & 1), ek = k - (c >> 2);
@@ -418,7 +419,8 @@ static __global__ void __launch_bounds__(EW) k_sens(const SensArgs A, const Elem
     const auto sdu = sens_src(du, A.duf, T());
     double fxv[1] = {0.0};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(e % g.ex), jj = (int)((e / g.ex) % g.ey), k = (int)(e / ((long long)g.ex * g.ey));
+        int i, jj, k;
+        lex3(e, g.ex, g.ey, i, jj, k);
         long long nodes[8];
 #pragma unroll
         for (int L = 0; L < 8; L++)

@@ -434,7 +434,8 @@ static __global__ void __launch_bounds__(EW) k_red_sens(const RedSens<QT> A, con
     const GridDesc g = A.g;
     const long long nel = g.nel(), nd = 3 * g.nn();
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nel; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % g.ex), j = (int)((e / g.ex) % g.ey), k = (int)(e / ((long long)g.ex * g.ey));
+        int i, j, k;
+        lex3(e, g.ex, g.ey, i, j, k);
         long long nodes[8];
 #pragma unroll
         for (int L = 0; L < 8; L++)

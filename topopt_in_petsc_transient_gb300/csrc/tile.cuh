@@ -176,7 +176,7 @@ __device__ __forceinline__ void tile_elements(const GridDesc &g, const ElemConst
                         for (int m = 0; m < 8; m++) V[m] = U[b][m];
                     }
 #pragma unroll
-                    for (int m = 0; m < 8; m++) Y[b][m] = tadd(Y[b][m], (cm * C.W[m]) * V[m]);
+                    for (int m = 0; m < 8; m++) Y[b][m] = tadd(Y[b][m], tmul(tmul(cm, C.W[m]), V[m]));
                 }
             }
         }
