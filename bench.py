@@ -382,16 +382,18 @@ def roofline(args, wl, opt):
     #     z pass reads its input, r, the masked scale and q and writes z
     #     (60 B/node)
     #   smoothing step: x, b, 1/diag, d read, d and x written (72 B/node), mask, kf/mf
-    #   double-float products: FP64 x staged, FP64 y written (48 B/node), the
-    #     replacement also reads the mask; double-float factors (8 B each)
+    #   double-float products: FP64 x staged, FP64 y written (48 B/node);
+    #     the replacement stages x and the mask, reads b and writes r
+    #     (73 B/node); double-float factors (8 B each)
     classes = [(1, "k_tile<float,PolPQ32> (FCG operator product q = A p with p = z + beta p_prev, FP32)",
                 49.0 * nn + 8.0 * nel),
                (2, "k_kron_pass<float> (one axis pass of the Kronecker mass inverse, 17-tap stencil, FP32)",
                 (36.0 + 24.0 + 60.0) / 3.0 * nn),
                (0, "k_tile<float,PolCheb> (FP32 Chebyshev-Jacobi smoothing step)", 73.0 * nn + 8.0 * nel),
-               (3, "k_tile<df,PolReplaceProduct> (FP64-accurate A x of a residual replacement, double-float; "
-                   "launches without a due replacement exit at once: algorithmic bytes per launch = bytes of a "
-                   "replacement x replacements / launches)", 49.0 * nn + 16.0 * nel),
+               (3, "k_tile<df,PolReplace> (FP64-accurate residual replacement: A x in double-float, then "
+                   "r = b - A x, r.r and the convergence decision in the epilogue; launches without a due "
+                   "replacement exit at once: algorithmic bytes per launch = bytes of a replacement x "
+                   "replacements / launches)", 73.0 * nn + 16.0 * nel),
                (4, "k_tile<df,PolProduct> (double-float K or A products of right-hand sides, anchors and adjoint "
                    "steps)", 48.0 * nn + 8.0 * nel)]
     kern = []

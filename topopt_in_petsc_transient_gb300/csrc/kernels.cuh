@@ -715,27 +715,6 @@ static __global__ void __launch_bounds__(EW, 4) k_rhs_finish(long long ndof, con
     if (grid_reduce<EW, 2>(red, part, tot)) init_finish(S, tot, true, cond, has_cond, false);
 }
 
-// Residual replacement of the mixed FCG, part 2 (after PolReplaceProduct):
-// r = b - y on free DOFs, b - x on clamped ones, r.r and the convergence
-// decision.  Every CTA reads the replacement flag before any CTA can reach the
-// grid reduction whose last CTA clears it.
-static __global__ void k_replace_finish(long long ndof, const uint8_t *__restrict__ fixed, const double *__restrict__ x,
-                                        const double *__restrict__ b, const double *__restrict__ y,
-                                        double *__restrict__ r, SolveScalars *S, cudaGraphConditionalHandle cond,
-                                        int has_cond, Partials<1> part) {
-    if (S->need_replace == 0) return;
-    double red[1] = {0.0};
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
-        const long long n = i / 3;
-        const int c = (int)(i - 3 * n);
-        const double rv = b[i] - (((fixed[n] >> c) & 1) ? x[i] : y[i]);
-        r[i] = rv;
-        red[0] += rv * rv;
-    }
-    double tot[1];
-    if (grid_reduce<EW, 1>(red, part, tot)) replace_finish(S, tot[0], cond, has_cond);
-}
-
 static __global__ void k_step_set(StepCtx *st, int block, int j) {
     st->block = block;
     st->j = j;

@@ -257,7 +257,7 @@ template <class T, class Pol>
 constexpr int tile_class() {
     return (std::is_same<Pol, PolCheb<float>>::value || std::is_same<Pol, PolChebDot>::value) ? TOPO_KT_SMOOTH
            : std::is_same<Pol, PolPQ32>::value                                                 ? TOPO_KT_PQ32
-           : std::is_same<Pol, PolReplaceProduct<T>>::value                                    ? TOPO_KT_REPLACE
+           : std::is_same<Pol, PolReplace<T>>::value                                           ? TOPO_KT_REPLACE
            : (std::is_same<T, df>::value && std::is_same<Pol, PolProduct<df, Pol::HAS_K, Pol::HAS_M>>::value)
                ? TOPO_KT_DFPROD
                                                                                                : -1;
@@ -1228,11 +1228,8 @@ static void solve_iteration(TopoLE *le, int o, cudaGraphConditionalHandle cond, 
         k_mfcg_update<<<red_blocks(nd), EW, 0, s>>>(nd, le->sx, le->sr32, le->sp32, le->sp32b, le->sq32, le->S,
                                                     P1(le));
         Weights<df> wd = fine_weights<df>(le, op.sK != 0.0, true, nullptr, op.sK, op.sM);
-        PolReplaceProduct<df> rp{l0.fixed, wd, le->sx, le->sq, le->S, {}};
+        PolReplace<df> rp{l0.fixed, wd, le->sx, cur_b(le), le->sr, le->S, cond, has_cond, P1(le)};
         launch_tile<df>(l0.g, le->Cx, rp, s);
-        count_launch();
-        k_replace_finish<<<red_blocks(nd), EW, 0, s>>>(nd, l0.fixed, le->sx, cur_b(le), le->sq, le->sr, le->S, cond,
-                                                       has_cond, P1(le));
         return;
     } else {
         double *z = op.kron ? kron_smooth<double>(le, o, le->sr, kron_apply<double>(le, o, le->sr), nullptr)

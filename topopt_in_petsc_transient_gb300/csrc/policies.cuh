@@ -229,45 +229,6 @@ struct PolPQ32 {
     }
 };
 
-// Residual replacement of the mixed FCG, part 1: y = (N A N) x, FP64-accurate
-// (T = double-float), only when a replacement is due (the whole grid exits
-// otherwise); k_replace_finish forms r = b - (N A N + I - N) x, decides
-// convergence and drives the graph condition.
-template <class T>
-struct PolReplaceProduct {
-    static constexpr int NIN = 1, NRED = 0;
-    static constexpr bool HAS_K = true, HAS_M = true;
-    const uint8_t *fixed;
-    Weights<T> w;
-    const double *x;
-    double *y;
-    const SolveScalars *S;
-    Partials<1> part;
-    __device__ bool skip() const { return S->need_replace == 0; }
-    __device__ void load(long long n, T v[1][3]) const {
-        v[0][0] = T(x[3 * n]);
-        v[0][1] = T(x[3 * n + 1]);
-        v[0][2] = T(x[3 * n + 2]);
-        mask3(fixed[n], v[0]);
-    }
-    // asynchronous staging (tile.cuh): x and the clamp mask
-    using Src = double;
-    static constexpr int NSRC = 1;
-    static constexpr bool MASK = true;
-    __device__ const double *src(int) const { return x; }
-    __device__ void xform(const double raw[][3], uint8_t f, T v[1][3]) const {
-        for (int c = 0; c < 3; c++) v[0][c] = T(raw[0][c]);
-        mask3(f, v[0]);
-    }
-    __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
-    __device__ void epilogue(long long n, int, int, int, const T yv[3], double *) const {
-        y[3 * n] = todbl(yv[0]);
-        y[3 * n + 1] = todbl(yv[1]);
-        y[3 * n + 2] = todbl(yv[2]);
-    }
-    __device__ void finish(const double *) const {}
-};
-
 // solver state after a residual replacement with true residual norm^2 rr
 __device__ __forceinline__ void replace_finish(SolveScalars *S, double rr, cudaGraphConditionalHandle cond,
                                                int has_cond) {
@@ -290,6 +251,66 @@ __device__ __forceinline__ void replace_finish(SolveScalars *S, double rr, cudaG
     }
     if (has_cond) cudaGraphSetConditional(cond, S->done ? 0u : 1u);
 }
+
+// Residual replacement of the mixed FCG, only when one is due (the whole grid
+// exits otherwise): y = (N A N) x FP64-accurate (T = double-float), then in
+// the epilogue r = b - y on free DOFs and b - x on clamped ones, r.r and the
+// convergence decision (replace_finish), which drives the graph condition.
+// b, x and the mask of the output node are loaded before the element phase.
+// Every CTA reads the replacement flag before it can reach the grid
+// reduction whose last CTA clears it.
+template <class T>
+struct PolReplace {
+    static constexpr int NIN = 1, NRED = 1;
+    static constexpr bool HAS_K = true, HAS_M = true;
+    const uint8_t *fixed;
+    Weights<T> w;
+    const double *x;
+    const double *b;
+    double *r;
+    SolveScalars *S;
+    cudaGraphConditionalHandle cond;
+    int has_cond;
+    Partials<1> part;
+    __device__ bool skip() const { return S->need_replace == 0; }
+    __device__ void load(long long n, T v[1][3]) const {
+        v[0][0] = T(x[3 * n]);
+        v[0][1] = T(x[3 * n + 1]);
+        v[0][2] = T(x[3 * n + 2]);
+        mask3(fixed[n], v[0]);
+    }
+    // asynchronous staging (tile.cuh): x and the clamp mask
+    using Src = double;
+    static constexpr int NSRC = 1;
+    static constexpr bool MASK = true;
+    __device__ const double *src(int) const { return x; }
+    __device__ void xform(const double raw[][3], uint8_t f, T v[1][3]) const {
+        for (int c = 0; c < 3; c++) v[0][c] = T(raw[0][c]);
+        mask3(f, v[0]);
+    }
+    __device__ void coef(long long e, T &ck, T &cm) const { w.get(e, ck, cm); }
+    struct Pre {
+        double b[3], x[3];
+        uint8_t f;
+    };
+    __device__ Pre pre(long long n) const {
+        Pre q;
+        for (int c = 0; c < 3; c++) {
+            q.b[c] = b[3 * n + c];
+            q.x[c] = x[3 * n + c];
+        }
+        q.f = fixed[n];
+        return q;
+    }
+    __device__ void epilogue(long long n, int, int, int, const T yv[3], double red[1], const Pre &q) const {
+        for (int c = 0; c < 3; c++) {
+            const double rv = q.b[c] - (((q.f >> c) & 1) ? q.x[c] : todbl(yv[c]));
+            r[3 * n + c] = rv;
+            red[0] += rv * rv;
+        }
+    }
+    __device__ void finish(const double t[1]) const { replace_finish(S, t[0], cond, has_cond); }
+};
 
 // ---------------------------------------------------------------------------
 // Chebyshev-Jacobi smoothing step (one operator application):
