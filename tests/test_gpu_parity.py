@@ -136,6 +136,9 @@ def test_mixed_default_fp32_sensitivities(gpu, nlvls, coarse_smooth):
     fx, df = _run_gpu(le, x)
     st = le.stats()
     assert st["step_precond"] == 0 and st["mg_solves"] == st["solves"]
+    # convergence of a mixed solve is decided on an FP64-accurate replacement
+    # residual: a few per solve at most
+    assert 1 <= st["replacements"] <= 4 * st["solves"]
     ref = O.LinearElasticity(*n, **kw)
     rc, fx_r, df_r = ref.objective_sensitivities(x)
     assert abs(fx - fx_r) <= 1e-6 * abs(fx_r)
@@ -536,6 +539,7 @@ def test_sommg_basis_solves_descend_the_multigrid_hierarchy(gpu):
     s1 = le.stats()
     its = (s1["cg_iterations"] - s0["cg_iterations"]) / (s1["solves"] - s0["solves"])
     assert its < 25
+    assert s1["replacements"] == 0  # the plain FP64 path has no replacement residuals
 
 
 @pytest.mark.parametrize("ftype,R,h", [(1, 3.0, (1.0, 1.0, 1.0)), (0, 3.0, (1.0, 1.0, 1.0)), (1, 2.0, (1.0, 1.0, 1.0)),
