@@ -626,15 +626,20 @@ static __global__ void __launch_bounds__(EW, 4) k_newmark_track(long long ndof, 
     double *uo = Uh + (long long)j * ndof, *duo = DUh + (long long)j * ndof, *dduo = DDUh + (long long)j * ndof;
     const bool zx = S->zero_x != 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
-        const double un64 = x[i];
-        const df un(un64), dU(un64 - u[i]), dup(du[i]), ddup(ddu[i]);
+        // every input is loaded before the first store: the outputs may alias
+        // the inputs as far as the compiler knows, so a load after a store
+        // would wait for a second memory round trip (the kernel is bound by
+        // load latency, not by bandwidth)
+        const double un64 = x[i], u64 = u[i], du64 = du[i], ddu64 = ddu[i];
+        const double b64 = b[i], r64 = r[i], au64 = AU[i], av64 = AV[i], aa64 = AA[i];
+        const df un(un64), dU(un64 - u64), dup(du64), ddup(ddu64);
         const df dun = STD ? nm.da[2] * dU - dup : nm.da[0] * dup + nm.da[1] * ddup + nm.da[2] * dU;
         const df ddun = nm.da[5] * dU - nm.da[3] * dup - nm.da[4] * ddup;
         uo[i] = un64;
         duo[i] = todbl(dun);
         dduo[i] = todbl(ddun);
-        const double aun64 = zx ? 0.0 : b[i] - r[i];
-        const df aun(aun64), d(aun64 - AU[i]), av(AV[i]), aa(AA[i]);
+        const double aun64 = zx ? 0.0 : b64 - r64;
+        const df aun(aun64), d(aun64 - au64), av(av64), aa(aa64);
         const df avn = STD ? nm.da[2] * d - av : nm.da[0] * av + nm.da[1] * aa + nm.da[2] * d;
         const df aan = nm.da[5] * d - nm.da[3] * av - nm.da[4] * aa;
         AU[i] = aun64;

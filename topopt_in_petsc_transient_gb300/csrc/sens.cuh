@@ -125,11 +125,29 @@ static __global__ void k_adj_combine(AdjCombine A) {
             default: hdu = R(A.hK[i]); break;
             }
             bool fx = (f >> c) & 1;
-            const R kl = fx ? zero : R(A.KL[i]), ml = fx ? zero : R(A.ML[i]);
+            // the inputs of this DOF are loaded before its first store (the
+            // outputs may alias them as far as the compiler knows, and a load
+            // after a store waits for another memory round trip)
+            const double KLi = A.KL[i], MLi = A.ML[i], DLp1i = A.DLp1[i], DDLp1i = A.DDLp1[i];
+            double Lp1i = 0.0, Lp2i = 0.0, Lp3i = 0.0, MLh1i = 0.0, MLh2i = 0.0, KLh1i = 0.0, KLh2i = 0.0;
+            if (!A.t0mode) {
+                Lp1i = A.Lp1[i];
+                if (w2 != 0.0) Lp2i = A.Lp2[i];
+                if (w3 != 0.0) Lp3i = A.Lp3[i];
+                if (A.ax0) {
+                    if (w2 != 0.0) MLh1i = A.MLh1[i];
+                    if (w3 != 0.0) MLh2i = A.MLh2[i];
+                    if (!ax_is_mx && A.sK != 0.0) {
+                        if (w2 != 0.0) KLh1i = A.KLh1[i];
+                        if (w3 != 0.0) KLh2i = A.KLh2[i];
+                    }
+                }
+            }
+            const R kl = fx ? zero : R(KLi), ml = fx ? zero : R(MLi);
             const R B1 = cM[0] * ml + cK[0] * kl;
             const R B2 = cM[1] * ml + cK[1] * kl;
             const R B3 = cM[2] * ml + cK[2] * kl;
-            const R dlp = R(A.DLp1[i]), ddlp = R(A.DDLp1[i]);
+            const R dlp = R(DLp1i), ddlp = R(DDLp1i);
             if (A.t0mode) {
                 // SolveLagrange0 R3 (LinearElasticity.cc:753-758)
                 const R r3 = -(hddu + B3 - a[1] * dlp + a[4] * ddlp);
@@ -145,21 +163,21 @@ static __global__ void k_adj_combine(AdjCombine A) {
                 // the reference solves (N A N + I - N) L = R1 with A = -Keff
                 // (LinearElasticity.cc:1022-1026, :924): Keff L = -R1 on free DOFs
                 A.b[i] = fx ? 0.0 : todbl(-R1);
-                R g = W1 * R(A.Lp1[i]);
-                if (w2 != 0.0) g += W2 * R(A.Lp2[i]);
-                if (w3 != 0.0) g += W3 * R(A.Lp3[i]);
+                R g = W1 * R(Lp1i);
+                if (w2 != 0.0) g += W2 * R(Lp2i);
+                if (w3 != 0.0) g += W3 * R(Lp3i);
                 A.x0[i] = fx ? 0.0 : todbl(g);
                 if (A.ax0) {
-                    R mx = W1 * R(A.ML[i]);
-                    if (w2 != 0.0) mx += W2 * R(A.MLh1[i]);
-                    if (w3 != 0.0) mx += W3 * R(A.MLh2[i]);
+                    R mx = W1 * R(MLi);
+                    if (w2 != 0.0) mx += W2 * R(MLh1i);
+                    if (w3 != 0.0) mx += W3 * R(MLh2i);
                     R ax = mx;
                     if (!ax_is_mx) {
                         R kx = zero;
                         if (A.sK != 0.0) {
-                            kx = W1 * R(A.KL[i]);
-                            if (w2 != 0.0) kx += W2 * R(A.KLh1[i]);
-                            if (w3 != 0.0) kx += W3 * R(A.KLh2[i]);
+                            kx = W1 * R(KLi);
+                            if (w2 != 0.0) kx += W2 * R(KLh1i);
+                            if (w3 != 0.0) kx += W3 * R(KLh2i);
                         }
                         ax = sK * kx + sM * mx;
                     }
@@ -203,22 +221,29 @@ struct KMHist {
 static __global__ void k_adj_advance(long long ndof, const double *__restrict__ lam, const double *__restrict__ DL,
                               const double *__restrict__ DDL, double *Lp1, double *DLp1, double *DDLp1, double *Lp2,
                               double *Lp3, KMHist H) {
+    const bool zx = H.b && H.S->zero_x;
+    // every value is loaded before the first store: the slots may alias as
+    // far as the compiler knows, and a load after a store would wait for a
+    // second memory round trip
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndof; i += (long long)gridDim.x * blockDim.x) {
+        const double lp2 = Lp2[i], lp1 = Lp1[i], l = lam[i], dl = DL[i], ddl = DDL[i];
         if (H.b) {  // AL mode: A L++ <- A L+, A L+ <- A lambda_j
-            H.MLh2[i] = H.MLh1[i];
-            H.MLh1[i] = H.ML[i];
-            H.ML[i] = H.S->zero_x ? 0.0 : H.b[i] - H.r[i];
+            const double m1 = H.MLh1[i], m0 = H.ML[i], bv = H.b[i], rv = H.r[i];
+            H.MLh2[i] = m1;
+            H.MLh1[i] = m0;
+            H.ML[i] = zx ? 0.0 : bv - rv;
         } else if (H.KLh1) {  // K, M products follow their lambdas: K L++ <- K L+, ...
-            H.KLh2[i] = H.KLh1[i];
-            H.MLh2[i] = H.MLh1[i];
-            H.KLh1[i] = H.KL[i];
-            H.MLh1[i] = H.ML[i];
+            const double k1 = H.KLh1[i], m1 = H.MLh1[i], k0 = H.KL[i], m0 = H.ML[i];
+            H.KLh2[i] = k1;
+            H.MLh2[i] = m1;
+            H.KLh1[i] = k0;
+            H.MLh1[i] = m0;
         }
-        Lp3[i] = Lp2[i];
-        Lp2[i] = Lp1[i];
-        Lp1[i] = lam[i];
-        DLp1[i] = DL[i];
-        DDLp1[i] = DDL[i];
+        Lp3[i] = lp2;
+        Lp2[i] = lp1;
+        Lp1[i] = l;
+        DLp1[i] = dl;
+        DDLp1[i] = ddl;
     }
 }
 
