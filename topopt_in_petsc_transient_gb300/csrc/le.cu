@@ -1730,9 +1730,9 @@ static void adj_kl(TopoLE *le) {
 // the mixed path forms the adjoint right-hand side in double-float arithmetic
 static void launch_adj_combine(TopoLE *le, const AdjCombine &A) {
     if (le->p.mixed)
-        k_adj_combine<df><<<ew_blocks(le->nn), EW, 0, le->stream>>>(A);
+        k_adj_combine<df><<<ew_blocks(le->ndof), EW, 0, le->stream>>>(A);
     else
-        k_adj_combine<double><<<ew_blocks(le->nn), EW, 0, le->stream>>>(A);
+        k_adj_combine<double><<<ew_blocks(le->ndof), EW, 0, le->stream>>>(A);
 }
 
 static int adj_step(TopoLE *le, bool capturing) {

@@ -100,11 +100,14 @@ static __global__ void k_adj_combine(AdjCombine A) {
         w2 = -1.0;
     }
     const R W1 = R(w1), W2 = R(w2), W3 = R(w3);
-    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn; n += (long long)gridDim.x * blockDim.x) {
+    // one DOF per thread: its inputs are all loaded before its stores
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 3 * nn;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long n = i / 3;
+        const int c = (int)(i - 3 * n);
         uint8_t f = A.fixed[n];
         const R cnt = R((double)A.cntP[n]);
-        for (int c = 0; c < 3; c++) {
-            long long i = 3 * n + c;
+        {
             R hu = zero, hdu = zero, hddu = zero;
             switch (A.objective) {
             case 0: hu = dt * cnt * R(u[i]); break;
@@ -379,18 +382,26 @@ static __global__ void k_sens_nodal(const SensArgs A) {
     }
     const int nzaK = comb3_nz(A.aK), nzaM = comb3_nz(A.aM), nzbK = comb3_nz(A.bK), nzbM = comb3_nz(A.bM);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ndof; q += (long long)gridDim.x * blockDim.x) {
-        const double s0 = u[q], s1 = du[q];
-        const topo::df d0(s0), d1(s1), d2(ddu[q]);
+        // every input is loaded before the first store (a load behind a
+        // possibly aliasing store waits for another memory round trip)
+        const double s0 = u[q], s1 = du[q], s2 = ddu[q], lq = A.lam[q];
+        double p0v = 0.0, p1v = 0.0, p2v = 0.0;
+        if (!A.t0mode) {
+            p0v = up[q];
+            p1v = dup[q];
+            p2v = ddup[q];
+        }
+        const topo::df d0(s0), d1(s1), d2(s2);
         topo::df wk = comb3(A.daK, nzaK, d0, d1, d2);
         topo::df wm = comb3(A.daM, nzaM, d0, d1, d2);
         if (!A.t0mode) {
-            const topo::df p0(up[q]), p1(dup[q]), p2(ddup[q]);
+            const topo::df p0(p0v), p1(p1v), p2(p2v);
             wk += comb3(A.dbK, nzbK, p0, p1, p2);
             wm += comb3(A.dbM, nzbM, p0, p1, p2);
         }
         A.wKf[q] = wk.hi;
         A.wMf[q] = wm.hi;
-        A.lamf[q] = f64_to_f32(A.lam[q]);
+        A.lamf[q] = f64_to_f32(lq);
         if (A.uf) A.uf[q] = d0.hi;
         if (A.duf) A.duf[q] = d1.hi;
     }
