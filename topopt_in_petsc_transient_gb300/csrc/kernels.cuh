@@ -333,28 +333,56 @@ static __global__ void k_coarse_assemble(GridDesc g, const uint8_t *__restrict__
     }
 }
 
-// In-place Gauss-Jordan inversion (SPD, no pivoting), step k in two passes.
-static __global__ void k_gj_save(const double *A, int n, int k, double *rowk, double *colk) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        rowk[t] = A[(size_t)k * n + t];
-        colk[t] = A[(size_t)t * n + k];
+// Dense coarsest-level operator (SPD, FP64).  Cholesky factor A = L L' in
+// place in the lower triangle, right-looking, one column per step in two
+// passes: the updated column k is saved (k_chol_save), then scaled into
+// L(:, k) and the trailing lower triangle updated, A(i, j) -= L(i, k) L(j, k)
+// (k_chol_update).  Then W = L^-1 by forward substitution (row i of W scaled
+// by 1 / L(i, i), then subtracted from the rows below) and A^-1 = W' W, so the
+// V-cycle's coarse solve stays one dense matrix-vector product.
+static __global__ void k_chol_save(const double *A, int n, int k, double *col) {
+    for (int t = k + blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        col[t] = A[(size_t)t * n + k];
+}
+static __global__ void k_chol_update(double *A, int n, int k, const double *__restrict__ col) {
+    const long long m = n - k;
+    const double p = col[k], d = sqrt(p);
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < m * m; t += (long long)gridDim.x * blockDim.x) {
+        const int i = k + (int)(t / m), j = k + (int)(t % m);
+        if (j > i) continue;
+        double &a = A[(size_t)i * n + j];
+        if (j == k)
+            a = (i == k) ? d : col[i] / d;
+        else
+            a -= (col[i] / p) * col[j];  // L(i, k) L(j, k) = col_i col_j / col_k
     }
 }
-static __global__ void k_gj_update(double *A, int n, int k, const double *__restrict__ rowk, const double *__restrict__ colk) {
-    long long tot = (long long)n * n;
-    double p = rowk[k];
+static __global__ void k_chol_identity(double *W, int n) {
+    const long long tot = (long long)n * n;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x)
+        W[t] = (t / n == t % n) ? 1.0 : 0.0;
+}
+// forward substitution step i: row i of W (columns <= i) divided by L(i, i)
+static __global__ void k_chol_trsv_scale(const double *L, double *W, int n, int i) {
+    const double d = L[(size_t)i * n + i];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c <= i; c += gridDim.x * blockDim.x) W[(size_t)i * n + c] /= d;
+}
+// rows r > i of W (columns <= i) minus L(r, i) times row i
+static __global__ void k_chol_trsv_update(const double *L, double *W, int n, int i) {
+    const long long w = i + 1, tot = (long long)(n - i - 1) * w;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(t / n), j = (int)(t % n);
-        double v;
-        if (i == k && j == k)
-            v = 1.0 / p;
-        else if (i == k)
-            v = rowk[j] / p;
-        else if (j == k)
-            v = -colk[i] / p;
-        else
-            v = A[t] - colk[i] * rowk[j] / p;
-        A[t] = v;
+        const int r = i + 1 + (int)(t / w), c = (int)(t % w);
+        W[(size_t)r * n + c] -= L[(size_t)r * n + i] * W[(size_t)i * n + c];
+    }
+}
+// A^-1 = W' W with W = L^-1 lower triangular: Ainv(i, j) = sum over r >= max(i, j) of W(r, i) W(r, j)
+static __global__ void k_chol_gram(const double *__restrict__ W, int n, double *Ainv) {
+    const long long tot = (long long)n * n;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / n), j = (int)(t % n);
+        double s = 0.0;
+        for (int r = i > j ? i : j; r < n; r++) s += W[(size_t)r * n + i] * W[(size_t)r * n + j];
+        Ainv[t] = s;
     }
 }
 

@@ -401,7 +401,7 @@ struct TopoLE {
     float *sr32 = nullptr, *sp32 = nullptr, *sp32b = nullptr, *sq32 = nullptr;
     int coarse_dense = 1;
     // coarse assembly scratch
-    double *KEc = nullptr, *MEc = nullptr, *Acoarse = nullptr, *gj_row = nullptr, *gj_col = nullptr;
+    double *KEc = nullptr, *MEc = nullptr, *chol_w = nullptr, *chol_col = nullptr;  // coarse Cholesky scratch
     int ncoarse = 0;
     // control block
     SolveScalars *S = nullptr;
@@ -733,9 +733,8 @@ int le_alloc(TopoLE *le) {
             AG(le->MEc, 576);
             CK(cudaMemcpy(le->KEc, KE, sizeof(KE), cudaMemcpyHostToDevice));
             CK(cudaMemcpy(le->MEc, ME, sizeof(ME), cudaMemcpyHostToDevice));
-            AG(le->Acoarse, (size_t)lnd * lnd);
-            AG(le->gj_row, lnd);
-            AG(le->gj_col, lnd);
+            AG(le->chol_w, (size_t)lnd * lnd);
+            AG(le->chol_col, lnd);
         }
     }
     le->L[0].kfd = le->kf;
@@ -884,7 +883,7 @@ static int setup_operator(TopoLE *le, int o) {
             }
         }
     }
-    // dense coarsest operator and its inverse (FP64 Gauss-Jordan); not needed
+    // dense coarsest operator and its inverse (FP64 Cholesky); not needed
     // when the V-cycle of this operator stops above the coarsest level
     if (!le->coarse_dense || op.depth < le->nlev) {
         CK(cudaGetLastError());
@@ -896,12 +895,27 @@ static int setup_operator(TopoLE *le, int o) {
     count_launch();
     k_coarse_assemble<<<ew_blocks((long long)n * n), EW, 0, s>>>(lc.g, lc.fixed, kfp, lc.mfd, op.sK, op.sM, le->KEc,
                                                                  le->MEc, op.Ainv_d);
+    // FP64 Cholesky factor of the coarsest operator, then its inverse from the
+    // factor (k_chol_*): A^-1 = L^-T L^-1
     for (int k = 0; k < n; k++) {
         count_launch();
-        k_gj_save<<<(n + EW - 1) / EW, EW, 0, s>>>(op.Ainv_d, n, k, le->gj_row, le->gj_col);
+        k_chol_save<<<(n + EW - 1) / EW, EW, 0, s>>>(op.Ainv_d, n, k, le->chol_col);
         count_launch();
-        k_gj_update<<<ew_blocks((long long)n * n), EW, 0, s>>>(op.Ainv_d, n, k, le->gj_row, le->gj_col);
+        k_chol_update<<<ew_blocks((long long)(n - k) * (n - k)), EW, 0, s>>>(op.Ainv_d, n, k, le->chol_col);
     }
+    count_launch();
+    k_chol_identity<<<ew_blocks((long long)n * n), EW, 0, s>>>(le->chol_w, n);
+    for (int i = 0; i < n; i++) {
+        count_launch();
+        k_chol_trsv_scale<<<(i + EW) / EW, EW, 0, s>>>(op.Ainv_d, le->chol_w, n, i);
+        if (i + 1 < n) {
+            count_launch();
+            k_chol_trsv_update<<<ew_blocks((long long)(n - i - 1) * (i + 1)), EW, 0, s>>>(op.Ainv_d, le->chol_w,
+                                                                                           n, i);
+        }
+    }
+    count_launch();
+    k_chol_gram<<<ew_blocks((long long)n * n), EW, 0, s>>>(le->chol_w, n, op.Ainv_d);
     count_launch();
     k_d2f<<<ew_blocks((long long)n * n), EW, 0, s>>>((long long)n * n, op.Ainv_d, op.Ainv_f);
     CK(cudaGetLastError());
