@@ -59,9 +59,10 @@ typedef struct topo_le_params {
     int smooth;              /* Chebyshev degree of pre/post smoothing              */
     double cheb_ratio;       /* Chebyshev lower bound = max(lo_bound, hi/ratio)     */
     int use_graphs;          /* 1: CUDA graphs with device-side loop control        */
-    int coarse_dense_max;    /* coarsest level solved by a dense FP64-factored
-                                inverse when it has at most this many DOFs,
-                                otherwise by Chebyshev-Jacobi smoothing           */
+    int coarse_dense_max;    /* coarsest level solved by a dense inverse from an
+                                FP64 Cholesky factor when it has at most this
+                                many DOFs, otherwise by Chebyshev-Jacobi
+                                smoothing                                         */
     int coarse_smooth;       /* Chebyshev degree of the iterative coarse solve      */
     int sens_fp32;           /* mixed mode: FP32 element math in the sensitivity
                                 kernel (state combinations still formed in FP64)  */
