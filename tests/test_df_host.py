@@ -1,8 +1,11 @@
-"""The integer-pipe FP64 -> double-float split (csrc/df.cuh, f64_to_df) on the
-host: it also builds the double-float element constants, and on the GPU it
-replaces an FP64 subtraction per staged value.  tests/cuda/df_host_check.cu
-is compiled for the host with nvcc and checks exactness on 3 M values (the
-device form is checked against the hardware conversions by
+"""The integer-pipe FP64 -> double-float split (csrc/df.cuh, f64_to_df) and
+the double-float arithmetic on the host: the split also builds the
+double-float element constants, and on the GPU it replaces an FP64
+subtraction per staged value.  tests/cuda/df_host_check.cu is compiled for the
+host with nvcc; it checks the split for exactness on 3 M values and the error
+bounds of operator+, add_lazy (the element math's unrenormalised sums),
+operator* and an 8-point butterfly of lazy sums against long double (the
+device split is checked against the hardware conversions by
 tests/test_gpu_conversions.py)."""
 import os
 import shutil
